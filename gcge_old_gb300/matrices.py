@@ -1,0 +1,173 @@
+"""Seeded synthetic problem generators for the GCG eigensolver workloads.
+
+Every generator returns a :class:`CSRMatrix` (0-based int32 ``rowptr`` and
+``col``, float64 ``val``, columns sorted within each row: the layout of the
+reference's ``CSR_MAT``, app/csr/gcge_app_csr.h:27-41) or ``None`` for B = I.
+The same arrays feed the CUDA solver, the oracle port and the reference
+oracle, so all three see bit-identical inputs.
+
+Workloads (sizes given as defaults, every generator takes a smaller grid for
+tests):
+
+* ``laplace2d``      5-point Dirichlet Laplacian [4; -1 x4] on an m x m
+                     interior grid, B = I.                 (n = 16,384 at m=128)
+* ``laplace3d_mass`` 7-point Laplacian scaled by h (h = 1/(m+1)) and a
+                     diagonal lumped mass h^3 (1 + U(-0.1, 0.1)).
+                                                           (n = 2,097,152 at m=128)
+* ``diffusion27``    trilinear (Q1) finite-element stiffness with per-cell
+                     coefficient exp(N(0,1)) on an m^3 interior grid, kept in
+                     its full 27-point pattern, and the Q1 consistent mass
+                     (centre 8/27, face 2/27, edge 1/54, corner 1/216) h^3.
+                                                           (n = 4,096,000 at m=160)
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+@dataclass
+class CSRMatrix:
+    n: int
+    rowptr: np.ndarray  # int32, n+1
+    col: np.ndarray     # int32, nnz
+    val: np.ndarray     # float64, nnz
+
+    @property
+    def nnz(self) -> int:
+        return int(self.rowptr[-1])
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.rowptr), shape=(self.n, self.n))
+
+    @staticmethod
+    def from_scipy(m) -> "CSRMatrix":
+        m = m.tocsr()
+        m.sort_indices()
+        return CSRMatrix(m.shape[0], np.ascontiguousarray(m.indptr, dtype=np.int32),
+                         np.ascontiguousarray(m.indices, dtype=np.int32),
+                         np.ascontiguousarray(m.data, dtype=np.float64))
+
+    def matvec(self, x: np.ndarray) -> np.ndarray:
+        return self.to_scipy() @ x
+
+
+def _tridiag(m: int, diag: float, off: float):
+    import scipy.sparse as sp
+    e = np.ones(m)
+    return sp.diags([off * e[:-1], diag * e, off * e[:-1]], [-1, 0, 1], format="csr")
+
+
+def laplace2d(m: int = 128) -> CSRMatrix:
+    """5-point stencil [4; -1 x 4] on an m x m interior grid (Dirichlet)."""
+    import scipy.sparse as sp
+    t = _tridiag(m, 2.0, -1.0)
+    i = sp.identity(m, format="csr")
+    return CSRMatrix.from_scipy(sp.kron(i, t) + sp.kron(t, i))
+
+
+def laplace3d(m: int) -> CSRMatrix:
+    """Unscaled 7-point stencil [6; -1 x 6] on an m^3 interior grid."""
+    import scipy.sparse as sp
+    t = _tridiag(m, 2.0, -1.0)
+    i = sp.identity(m, format="csr")
+    a = sp.kron(sp.kron(i, i), t) + sp.kron(sp.kron(i, t), i) + sp.kron(sp.kron(t, i), i)
+    return CSRMatrix.from_scipy(a)
+
+
+def diag_matrix(d: np.ndarray) -> CSRMatrix:
+    n = d.shape[0]
+    return CSRMatrix(n, np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32),
+                     np.ascontiguousarray(d, dtype=np.float64))
+
+
+def laplace3d_mass(m: int = 128, seed: int = 0):
+    """A = h * 7-point Laplacian, B = diag(h^3 (1 + U(-0.1, 0.1))), h = 1/(m+1)."""
+    h = 1.0 / (m + 1)
+    a = laplace3d(m)
+    a.val *= h
+    rng = np.random.default_rng(seed)
+    b = diag_matrix(h ** 3 * (1.0 + rng.uniform(-0.1, 0.1, size=m ** 3)))
+    return a, b
+
+
+def _q1_assemble(m: int, cell_coef: np.ndarray | None, weights) -> CSRMatrix:
+    """Assemble a 27-point operator on the m^3 interior nodes of an (m+1)^3
+    cell grid.  ``weights[d]`` is the element-matrix entry for two vertices
+    that differ in d coordinates; node-pair entries sum over the shared cells,
+    weighted by ``cell_coef`` (or 1)."""
+    nc = m + 1
+    if cell_coef is None:
+        cell_coef = np.ones((nc, nc, nc))
+    idx = np.arange(m)
+    rows, cols, vals = [], [], []
+    node = lambda x, y, z: (z * m + y) * m + x
+    X, Y, Z = np.meshgrid(idx, idx, idx, indexing="ij")
+    for oz in (-1, 0, 1):
+        for oy in (-1, 0, 1):
+            for ox in (-1, 0, 1):
+                d = abs(ox) + abs(oy) + abs(oz)
+                # cells shared by node p=(x,y,z) (interior index) and p+o: node
+                # interior index i sits at grid point i+1; a cell c touches grid
+                # points c..c+1 per axis.  Shared cells per axis: offset 0 ->
+                # {i, i+1}; offset +1 -> {i+1}; offset -1 -> {i}.
+                sx = [0, 1] if ox == 0 else ([1] if ox > 0 else [0])
+                sy = [0, 1] if oy == 0 else ([1] if oy > 0 else [0])
+                sz = [0, 1] if oz == 0 else ([1] if oz > 0 else [0])
+                xs, ys, zs = X + ox, Y + oy, Z + oz
+                valid = (xs >= 0) & (xs < m) & (ys >= 0) & (ys < m) & (zs >= 0) & (zs < m)
+                acc = np.zeros((m, m, m))
+                for cx in sx:
+                    for cy in sy:
+                        for cz in sz:
+                            acc += cell_coef[cx:cx + m, cy:cy + m, cz:cz + m]
+                v = acc * weights[d]
+                rows.append(node(X, Y, Z)[valid])
+                cols.append(node(xs, ys, zs)[valid])
+                vals.append(v[valid])
+    import scipy.sparse as sp
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    v = np.concatenate(vals)
+    a = sp.coo_matrix((v, (r, c)), shape=(m ** 3, m ** 3)).tocsr()
+    # keep structural zeros (face entries of the Q1 stiffness are exactly 0)
+    a.sum_duplicates()
+    return CSRMatrix.from_scipy(a)
+
+
+def diffusion27(m: int = 160, seed: int = 0):
+    """Q1 FE stiffness with per-cell kappa = exp(N(0,1)) and the Q1 consistent
+    mass, both scaled for grid spacing h = 1/(m+1), full 27-point pattern."""
+    h = 1.0 / (m + 1)
+    rng = np.random.default_rng(seed)
+    kappa = np.exp(rng.standard_normal((m + 1, m + 1, m + 1)))
+    # trilinear element stiffness / h: d=0: 1/3, d=1: 0, d=2: -1/12, d=3: -1/12
+    a = _q1_assemble(m, kappa, [h / 3.0, 0.0, -h / 12.0, -h / 12.0])
+    # trilinear element mass: h^3/216 * (8, 4, 2, 1)
+    b = _q1_assemble(m, None, [h ** 3 * 8 / 216, h ** 3 * 4 / 216, h ** 3 * 2 / 216, h ** 3 / 216])
+    return a, b
+
+
+def initial_block(n: int, nev: int, seed: int = 0) -> np.ndarray:
+    """Seeded N(0,1) initial block, column-major n x nev (shape (nev, n) in C
+    order, so column j is ``x0[j]``)."""
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((nev, n))
+
+
+def read_csr_text(path: str) -> CSRMatrix:
+    """Reader for the reference's CSR text format (app/csr/gcge_app_csr.c:185-236):
+    ``nrow ncol nnz`` then ``rowptr[n+1]``, ``col[nnz]``, ``val[nnz]``, 0-based."""
+    with open(path) as f:
+        tok = f.read().split()
+    nrow, ncol, nnz = int(tok[0]), int(tok[1]), int(tok[2])
+    p = 3
+    rowptr = np.array(tok[p:p + nrow + 1], dtype=np.int64); p += nrow + 1
+    col = np.array(tok[p:p + nnz], dtype=np.int64); p += nnz
+    val = np.array(tok[p:p + nnz], dtype=np.float64)
+    assert ncol == nrow
+    import scipy.sparse as sp
+    m = sp.csr_matrix((val, col, rowptr), shape=(nrow, ncol))
+    return CSRMatrix.from_scipy(m)
