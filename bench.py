@@ -1,0 +1,407 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 GCG eigensolver (one JSON line on stdout).
+
+Workload (the reference's headline GPU configuration): 3D 7-point Laplacian
+scaled by h on a 128^3 interior grid (n = 2,097,152, nnz = 14,581,760),
+h = 1/129, B = diagonal lumped mass h^3 (1 + U(-0.1, 0.1)) from seed 0,
+nev = 50 smallest pairs, relative residual ||Ax - lambda Bx|| / (|lambda| ||x||)
+<= 1e-10 for every pair (the reference's "R" criterion with ev_tol = 1e-10:
+all lambda > 1), seeded N(0,1) initial block.  A step is one complete solve.
+
+value: seconds per solve of the mixed-precision form (FP32 block CG, FP64
+everything else) with the matrices and the initial block resident in HBM,
+timed with CUDA events on the solver's stream; fp64_s: the all-FP64 form.
+e2e: the same solve through the C ABI with HOST buffers: matrix upload,
+initial block upload and eigenvector download inside the timed region.
+roofline: the FP64 CSR SpMM on the W block (k = block size = 10), algorithmic
+bytes nnz*12 + 4(n+1) + 2*k*n*8 per launch.
+cpu_baseline: the oracle port (C restatement of the reference, OpenMP on all
+host cores) on a bounded sample of the same solve: the start phase plus one
+GCG iteration, extrapolated to the reference's iteration count.
+
+--impl reference runs that CPU path alone (rank 0), each step one bounded
+sample, and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "s to nev eigenpairs @1e-10 resid: mixed vs FP64 on GB300; SpMM HBM GB/s"
+# iteration count of the reference GCGE on this workload (num_iter, counted
+# as para->num_iter: the start RR check, the [X,W] step, then one per loop)
+REF_ITERS_FILE = os.path.join(HERE, "tests", "golden", "cfg2_reference_summary.json")
+
+
+def workload(small: bool):
+    from gcge_old_gb300 import matrices as M
+    m = 48 if small else 128
+    A, B = M.laplace3d_mass(m, seed=0)
+    nev = 50
+    x0 = M.initial_block(A.n, nev, seed=0)
+    return A, B, nev, x0, m
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.p = None
+        self.path = os.path.join("/tmp", "gcge_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_solves(torch, S, L, dA, dB, nev, x0_dev, precision, warmup, steps):
+    """Solves with device-resident inputs; returns (times_s, stats, eval, evec_dev)."""
+    lib = L.load()
+    s = S.GCGESolver(dA, dB, nev, ev_tol=1e-10, ev_max_it=1000, precision=precision)
+    evec_dev = torch.empty_like(x0_dev)
+    L.check(lib.GCGE_CUDA_SOLVER_SetEigenvectorsDevice(s.handle, C.c_void_p(evec_dev.data_ptr())),
+            "SetEigenvectorsDevice")
+    sp = C.c_void_p()
+    L.check(lib.GCGE_CUDA_SOLVER_GetStream(s.handle, C.byref(sp)), "GetStream")
+    stream = torch.cuda.ExternalStream(sp.value)
+    times = []
+    stats = []
+    for it in range(warmup + steps):
+        evec_dev.copy_(x0_dev)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.check(lib.GCGE_CUDA_SOLVER_Solve(s.handle), "Solve")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if it >= warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+            stats.append(s.stats())
+    ev = s.eval.copy()
+    s.close()
+    return times, stats, ev, evec_dev
+
+
+def spmm_roofline(torch, L, dA, A, k, launches=20):
+    lib = L.load()
+    n = A.n
+    X = [torch.randn(n, dtype=torch.float64, device="cuda") for _ in range(k)]
+    Y = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(k)]
+    xp = (C.c_void_p * k)(*[C.c_void_p(t.data_ptr()) for t in X])
+    yp = (C.c_void_p * k)(*[C.c_void_p(t.data_ptr()) for t in Y])
+    st = torch.cuda.Stream()
+    for _ in range(3):
+        L.check(lib.GCGE_CUDA_MatDotMultiVecAsync(dA.handle, xp, yp, k, C.c_void_p(st.cuda_stream)), "spmm")
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(launches):
+        L.check(lib.GCGE_CUDA_MatDotMultiVecAsync(dA.handle, xp, yp, k, C.c_void_p(st.cuda_stream)), "spmm")
+    e1.record(st)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / launches
+    # check against scipy on one column
+    y0 = Y[0].cpu().numpy()
+    ref = A.to_scipy() @ X[0].cpu().numpy()
+    assert np.allclose(y0, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    nbytes = A.nnz * 12 + 4 * (n + 1) + 2 * k * n * 8
+    # FP32 SpMM of the mixed inner solve (same k)
+    X32 = [t.float() for t in X]
+    Y32 = [torch.empty(n, dtype=torch.float32, device="cuda") for _ in range(k)]
+    xp32 = (C.c_void_p * k)(*[C.c_void_p(t.data_ptr()) for t in X32])
+    yp32 = (C.c_void_p * k)(*[C.c_void_p(t.data_ptr()) for t in Y32])
+    for _ in range(3):
+        L.check(lib.GCGE_CUDA_MatDotMultiVecF32Async(dA.handle, xp32, yp32, k, C.c_void_p(st.cuda_stream)), "spmm32")
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(launches):
+        L.check(lib.GCGE_CUDA_MatDotMultiVecF32Async(dA.handle, xp32, yp32, k, C.c_void_p(st.cuda_stream)), "spmm32")
+    e1.record(st)
+    torch.cuda.synchronize()
+    t32 = e0.elapsed_time(e1) / 1e3 / launches
+    nbytes32 = A.nnz * 8 + 4 * (n + 1) + 2 * k * n * 4
+    return t, nbytes, t32, nbytes32
+
+
+def e2e_solves(torch, S, L, A, B, nev, x0, precision, warmup, steps):
+    """Through the public C ABI with pinned HOST buffers: MatCreate (H2D of
+    the CSR arrays), Solve reading the host initial block and writing host
+    eigenvectors, eigenvalues back on the host."""
+    lib = L.load()
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.dtype("float64"): torch.float64,
+                                        np.dtype("int32"): torch.int32}[a.dtype], pin_memory=True)
+        t.numpy()[...] = a
+        return t
+
+    ha = [pinned(A.rowptr), pinned(A.col), pinned(A.val)]
+    hb = [pinned(B.rowptr), pinned(B.col), pinned(B.val)]
+    hx = pinned(np.ascontiguousarray(x0.reshape(nev, A.n)))
+    hv = pinned(np.zeros((nev, A.n)))
+    hev = np.zeros(nev)
+    h2d = sum(t.numel() * t.element_size() for t in ha + hb) + hx.numel() * 8
+    d2h = hv.numel() * 8 + nev * 8
+    times = []
+    for it in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ma, mb, s = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        L.check(lib.GCGE_CUDA_MatCreate(C.byref(ma), A.n, C.c_void_p(ha[0].data_ptr()),
+                                        C.c_void_p(ha[1].data_ptr()), C.c_void_p(ha[2].data_ptr()), 0), "MatCreate A")
+        L.check(lib.GCGE_CUDA_MatCreate(C.byref(mb), B.n, C.c_void_p(hb[0].data_ptr()),
+                                        C.c_void_p(hb[1].data_ptr()), C.c_void_p(hb[2].data_ptr()), 0), "MatCreate B")
+        L.check(lib.GCGE_CUDA_SOLVER_Create(C.byref(s)), "Create")
+        lib.GCGE_CUDA_SOLVER_SetMatA(s, ma)
+        lib.GCGE_CUDA_SOLVER_SetMatB(s, mb)
+        lib.GCGE_CUDA_SOLVER_SetNumEigen(s, nev)
+        lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"num_init_evec", nev)
+        lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"ev_max_it", 1000)
+        lib.GCGE_CUDA_SOLVER_SetParamDouble(s, b"ev_tol", 1e-10)
+        lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"precision", 1 if precision == "mixed" else 0)
+        lib.GCGE_CUDA_SOLVER_SetEigenvalues(s, C.c_void_p(hev.ctypes.data))
+        # the initial block is read from the result array (num_init_evec = nev)
+        hv.copy_(hx)
+        lib.GCGE_CUDA_SOLVER_SetEigenvectors(s, C.c_void_p(hv.data_ptr()))
+        L.check(lib.GCGE_CUDA_SOLVER_Setup(s), "Setup")
+        L.check(lib.GCGE_CUDA_SOLVER_Solve(s), "Solve")
+        lib.GCGE_CUDA_SOLVER_Free(C.byref(s))
+        lib.GCGE_CUDA_MatDestroy(C.byref(ma))
+        lib.GCGE_CUDA_MatDestroy(C.byref(mb))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        if it >= warmup:
+            times.append(t1 - t0)
+    return times, h2d, d2h, hev.copy(), hv.numpy().copy()
+
+
+def true_residuals_gpu(torch, A, B, ev, evec_rows):
+    """FP64 post-check ||A x - lambda B x|| / (|lambda| ||x||) per pair (torch
+    sparse on the GPU; checking only, outside the timed region)."""
+    a = torch.sparse_csr_tensor(torch.from_numpy(A.rowptr.astype(np.int64)),
+                                torch.from_numpy(A.col.astype(np.int64)),
+                                torch.from_numpy(A.val), size=(A.n, A.n)).to("cuda")
+    bd = torch.from_numpy(B.val).to("cuda")
+    X = evec_rows.T.contiguous()  # n x nev
+    AX = a @ X
+    lam = torch.from_numpy(ev).to("cuda")
+    R = AX - lam[None, :] * (bd[:, None] * X)
+    return (R.norm(dim=0) / (lam.abs() * X.norm(dim=0))).cpu().numpy()
+
+
+def reference_iters():
+    if os.path.exists(REF_ITERS_FILE):
+        return int(json.load(open(REF_ITERS_FILE))["iters"]), "reference run (tests/golden)"
+    return None, None
+
+
+def cpu_sample(A, B, nev, x0, threads, fallback_iters):
+    """Oracle port on the host: start phase + one GCG iteration, extrapolated
+    to the full iteration count."""
+    from oracle import oracle as O
+    p = O.default_para(nev, ev_tol=1e-10, ev_max_it=1000)
+    r = O.port_solve(A, B, nev, x0, p, max_outer=1, threads=threads)
+    iters, src = reference_iters()
+    if iters is None:
+        iters, src = fallback_iters, "GPU FP64 iteration count"
+    t_iter = r["t_loop"] / max(1, r["loop_iters"])
+    est = r["t_init"] + max(0, iters - 2) * t_iter
+    sample = ("oracle port, %d threads: start phase (X orth, RR, [X,W] step) %.2f s + 1 GCG iteration "
+              "%.2f s, extrapolated to %d iterations (%s)" % (threads, r["t_init"], t_iter, iters, src))
+    return est, r["t_init"] + r["t_loop"], sample
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    A, B, nev, x0, m = workload(args.small)
+    threads = os.cpu_count() or 1
+    vals = []
+    wall = []
+    sample = ""
+    for it in range(args.warmup + args.steps):
+        est, w, sample = cpu_sample(A, B, nev, x0, threads, 60)
+        if it >= args.warmup:
+            vals.append(est)
+            wall.append(w)
+    v = statistics.mean(vals)
+    out = {"metric": METRIC, "value": v, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(wall),
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded generator)",
+           "config": {"workload": "laplace3d_7pt_%d^3_diagmass_nev50_tol1e-10" % m,
+                      "n": A.n, "nnz": A.nnz, "nev": nev, "block_size": 10},
+           "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--small", action="store_true", help="48^3 grid (quick check)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+    if rank == 0:
+        g.build()
+    if world > 1:
+        dist.barrier()
+    from gcge_old_gb300 import lib as L
+    from gcge_old_gb300 import solver as S
+    L.load()
+
+    A, B, nev, x0, m = workload(args.small)
+    dA, dB = S.DeviceMatrix(A), S.DeviceMatrix(B)
+    x0_dev = torch.from_numpy(np.ascontiguousarray(x0)).to("cuda")
+
+    sampler = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    t_mixed, st_mixed, ev_mixed, vec_mixed = time_solves(torch, S, L, dA, dB, nev, x0_dev, "mixed",
+                                                         args.warmup, args.steps)
+    t_fp64, st_fp64, ev_fp64, vec_fp64 = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64",
+                                                     max(1, args.warmup // 3), max(1, args.steps // 2))
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    v_mixed = statistics.mean(t_mixed)
+    v_fp64 = statistics.mean(t_fp64)
+    if world > 1:
+        tt = torch.tensor([v_mixed, v_fp64], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        v_mixed, v_fp64 = tt.tolist()
+
+    # correctness of the timed solves (outside the timed region)
+    res_m = true_residuals_gpu(torch, A, B, ev_mixed, vec_mixed)
+    res_d = true_residuals_gpu(torch, A, B, ev_fp64, vec_fp64)
+    ev_rel = float(np.max(np.abs(ev_mixed - ev_fp64) / np.abs(ev_fp64)))
+
+    t_spmm, b_spmm, t_spmm32, b_spmm32 = spmm_roofline(torch, L, dA, A, 10)
+    peak, peak_src = peaks()
+    ach = b_spmm / t_spmm / 1e9
+
+    e2e_t, h2d, d2h, _, _ = e2e_solves(torch, S, L, A, B, nev, x0, "mixed", 1, max(1, args.steps // 2))
+    e2e_v = statistics.mean(e2e_t)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        est, wall, sample = cpu_sample(A, B, nev, x0, threads, st_fp64[-1]["num_iter"])
+        cpu = {"value": est, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
+
+    traffic = None
+    tf = os.path.join(HERE, "profiles", "spmm_traffic.json")
+    if os.path.exists(tf) and not args.small:
+        traffic = json.load(open(tf)).get("bytes_per_launch")
+
+    launches = int(statistics.mean([s["kernel_launches"] for s in st_mixed]))
+    out = {
+        "metric": METRIC, "value": v_mixed, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * v_mixed, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": "laplace3d_7pt_%d^3_diagmass_nev50_tol1e-10" % m, "n": A.n,
+                   "nnz": A.nnz, "nev": nev, "block_size": 10, "parallelism": "replicas only",
+                   "l2": "inputs larger than L2 (A 175 MB, basis 1.5 GB)"},
+        "fp64_s": v_fp64, "mixed_s": v_mixed, "mixed_speedup_vs_fp64": v_fp64 / v_mixed,
+        "gcg_iterations": {"mixed": st_mixed[-1]["num_iter"], "fp64": st_fp64[-1]["num_iter"]},
+        "max_residual": {"mixed": float(res_m.max()), "fp64": float(res_d.max())},
+        "eigenvalue_rel_diff_mixed_vs_fp64": ev_rel,
+        "phase_s_mixed": {k: round(v, 4) for k, v in st_mixed[-1].items() if k.startswith("t_")},
+        "roofline": {"kernel": "k_spmm<double,8> (CSR SpMM, k=10)", "bound": "hbm",
+                     "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes": b_spmm, "us_per_launch": t_spmm * 1e6,
+                     "fp32_spmm_gbs": b_spmm32 / t_spmm32 / 1e9},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

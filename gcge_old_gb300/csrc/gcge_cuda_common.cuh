@@ -1,0 +1,97 @@
+// Shared definitions for the GB300 GCG eigensolver kernels.
+//
+// Multivectors are arrays of device column pointers, the device analogue of
+// the reference's default "void**" multivector (src/gcge_ops.c:52-398): a
+// column swap is a pointer swap, and a kernel receives the columns it works
+// on as a ColList passed by value in its parameter block.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GCGE_MAXCOLS 256
+
+template <typename T>
+struct ColList {
+  T* p[GCGE_MAXCOLS];
+};
+
+struct DblList {
+  double v[GCGE_MAXCOLS];
+};
+
+struct GcgeDevCsr {
+  int n = 0, nnz = 0;
+  int* rp = nullptr;
+  int* ci = nullptr;
+  double* v = nullptr;
+  float* v32 = nullptr;   // FP32 copy for the mixed-precision inner solve
+  double* diag = nullptr; // set when the matrix is diagonal (rp[i] = i, ci[i] = i)
+  float* diag32 = nullptr;
+};
+
+
+// Definition of the opaque GCGE_CUDA_MAT of include/gcge_cuda.h.
+struct GCGE_CUDA_MAT_ {
+  GcgeDevCsr m;
+};
+
+// ---------------------------------------------------------------- launchers
+// All kernels run on the given stream; sizes are checked by the callers.
+namespace gcge {
+
+constexpr int kRowBlocks = 2 * 152;  // row-split blocks for reductions (2 per SM)
+
+// Y[:,j] = A X[:,j] for j < k.
+void spmm_f64(const GcgeDevCsr& A, const ColList<double>& X, const ColList<double>& Y, int k,
+              cudaStream_t st);
+// Y[:,j] = A X[:,j] in FP32 on the FP32 copy of A.
+void spmm_f32(const GcgeDevCsr& A, const ColList<float>& X, const ColList<float>& Y, int k,
+              cudaStream_t st);
+// B X, or a copy when B is the identity (B == nullptr).
+void apply_b_f64(const GcgeDevCsr* B, const ColList<double>& X, const ColList<double>& Y, int k,
+                 int n, cudaStream_t st);
+
+// G[i + j*ldg] = V_i . W_j  (i < k1, j < k2).  sym: k1 == k2 and only the
+// upper triangle is formed, then mirrored.  partial: scratch of
+// kRowBlocks*k1*k2 doubles.
+void gram_f64(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
+              double* G, int ldg, bool sym, double* partial, cudaStream_t st);
+// Y_j = beta*Y_j + sum_i X_i C[i + j*ldc]; Y must not alias X.
+void lincomb_f64(const ColList<double>& X, int k1, const double* C, int ldc,
+                 const ColList<double>& Y, int k2, double beta, int n, cudaStream_t st);
+// The same product with FP64 accuracy on the bf16 tensor cores (Ozaki
+// scheme, gcge_cuda_ozaki.cu); scratch of lincomb_oz_scratch_bytes(k1, k2).
+size_t lincomb_oz_scratch_bytes(int k1, int k2);
+void lincomb_oz(const ColList<double>& X, int k1, const double* C, int ldc,
+                const ColList<double>& Y, int k2, double beta, int n, void* scratch,
+                cudaStream_t st);
+// G = V^T W with FP64 accuracy on the bf16 tensor cores; partial holds
+// gram_oz_partial_doubles(k1, k2) doubles.
+size_t gram_oz_partial_doubles(int k1, int k2);
+void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n, double* G,
+             int ldg, bool sym, double* partial, cudaStream_t st);
+// G[i + j*ldg] = sum_b partial[b*k1*k2 + i + j*k1] (fixed order); sym mirrors
+// the upper triangle.
+void gram_reduce_partials(int k1, int k2, int nblk, bool sym, const double* partial, double* G,
+                          int ldg, cudaStream_t st);
+// Y_j = a X_j + b Y_j
+void axpby_f64(double a, const ColList<double>& X, double b, const ColList<double>& Y, int k, int n,
+               cudaStream_t st);
+// Y_j = s_j * Y_j with device scalars s (s_j == 0 allowed)
+void scale_cols_f64(const ColList<double>& Y, const double* s, int k, int n, cudaStream_t st);
+// per-column squared norms into out[j] (device), via partial.
+void colnorm2_f64(const ColList<double>& X, int k, int n, double* out, double* partial,
+                  cudaStream_t st);
+// res_j = ||A x_j - lam_j B x_j||^2 and xn_j = ||x_j||^2 (device outputs).
+void residual_f64(const GcgeDevCsr& A, const GcgeDevCsr* B, const ColList<double>& X,
+                  const double* lam, int k, double* rnorm2, double* xnorm2, double* partial,
+                  cudaStream_t st);
+void convert_f64_to_f32(const ColList<double>& X, const ColList<float>& Y, int k, int n,
+                        cudaStream_t st);
+void convert_f32_to_f64(const ColList<float>& X, const ColList<double>& Y, int k, int n,
+                        cudaStream_t st);
+// Y_j += (double)X_j
+void add_f32_to_f64(const ColList<float>& X, const ColList<double>& Y, int k, int n,
+                    cudaStream_t st);
+
+}  // namespace gcge

@@ -1,0 +1,501 @@
+// Small dense kernels of the GCG iteration (projected matrices of order
+// ldm <= nev + 20 + 2*block_size, Gram blocks of order <= block_size):
+//   * dgemm_small: thread-per-entry C = alpha op(A) op(B) + beta C, with an
+//     option to read A as a symmetric matrix from its upper triangle (dsymm);
+//   * the subspace eigensolver: cyclic two-sided Jacobi with a parallel
+//     round-robin pair ordering, one CTA, matrix staged in shared memory;
+//   * in-subspace Gram-Schmidt with zero-column dropping (P coefficients);
+//   * Cholesky of a Gram block with zero-column dropping and the inverse
+//     factor (the CholQR step of the W orthonormalisation).
+// All arithmetic is FP64.
+#include <math.h>
+
+#include "gcge_cuda_common.cuh"
+#include "gcge_cuda_dense.cuh"
+
+namespace gcge {
+namespace {
+
+__global__ void k_dgemm_small(int ta, int tb, int symA, int m, int n, int k, double alpha,
+                              const double* __restrict__ A, int lda, const double* __restrict__ B,
+                              int ldb, double beta, double* __restrict__ C, int ldc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * n) return;
+  const int i = e % m, j = e / m;
+  double s = 0.0;
+  for (int l = 0; l < k; l++) {
+    double a;
+    if (symA) a = (i <= l) ? A[i + (size_t)l * lda] : A[l + (size_t)i * lda];
+    else a = ta ? A[l + (size_t)i * lda] : A[i + (size_t)l * lda];
+    const double b = tb ? B[j + (size_t)l * ldb] : B[l + (size_t)j * ldb];
+    s = fma(a, b, s);
+  }
+  double* c = C + i + (size_t)j * ldc;
+  *c = (beta == 0.0) ? alpha * s : fma(beta, *c, alpha * s);
+}
+
+// ------------------------------------------------------------ Jacobi
+// Round-robin (circle method) pair k of round r for m players (m even):
+// (m-1, r) and ((r+k) mod (m-1), (r-k) mod (m-1)).
+__device__ inline void rr_pair(int m, int r, int k, int* p, int* q) {
+  int a, b;
+  if (k == 0) {
+    a = m - 1;
+    b = r;
+  } else {
+    a = (r + k) % (m - 1);
+    b = (r - k + (m - 1)) % (m - 1);
+  }
+  *p = a < b ? a : b;
+  *q = a < b ? b : a;
+}
+
+__device__ inline double block_sum1024(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += sh[w];
+  __syncthreads();
+  return s;  // every thread gets the sum
+}
+
+// a: nrows x nrows (lda), upper triangle read.  Cyclic two-sided Jacobi in
+// precision T with a parallel round-robin ordering (npairs disjoint rotations
+// per round), stopping when a whole sweep finds every off-diagonal entry
+// below tol * sqrt(|a_pp a_qq|); rotated entries are set to exactly 0.
+// mode 0: eigenvalues il..iu (1-based, ascending) to eval[0..] and their
+//         eigenvectors to evec (lde), sign fixed so the largest-magnitude
+//         entry is positive;
+// mode 1: all nrows eigenvectors, unsorted, to evec (lde) (a preconditioning
+//         basis for the FP64 pass).
+// work: global scratch of 2*mp*mp T when the matrix does not fit in shared
+// memory.  status[0] = sweeps used (or -1 if not converged).
+template <typename T>
+__global__ void __launch_bounds__(1024) k_jacobi(int nrows, const double* __restrict__ a, int lda,
+                                                 double* __restrict__ eval,
+                                                 double* __restrict__ evec, int lde, int il,
+                                                 int iu, T* __restrict__ work, int use_smem,
+                                                 int* __restrict__ status, int mode, double tol,
+                                                 int max_sweeps) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  __shared__ double red[32];
+  __shared__ T cs[128], sn[128];
+  __shared__ int rank_of[256];
+  __shared__ int nrot;
+  __shared__ unsigned char rot[128];
+  const int m = nrows;
+  const int mp = (m % 2) ? m + 1 : m;  // padded player count
+  T* M = use_smem ? reinterpret_cast<T*>(dyn_raw) : work;
+  T* Q = M + (size_t)mp * mp;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < mp * mp; e += nt) {
+    const int i = e % mp, j = e / mp;
+    double v = 0.0;
+    if (i < m && j < m) v = (i <= j) ? a[i + (size_t)j * lda] : a[j + (size_t)i * lda];
+    M[e] = (T)v;
+    Q[e] = (i == j) ? T(1) : T(0);
+  }
+  __syncthreads();
+  double tot = 0.0;
+  for (int e = tid; e < m * m; e += nt) {
+    const int i = e % m, j = e / m;
+    const double v = (double)M[i + (size_t)j * mp];
+    tot += v * v;
+  }
+  tot = block_sum1024(tot, red);
+  int sweep = 0;
+  bool converged = false;
+  const int npairs = mp / 2;
+  for (; sweep < max_sweeps; sweep++) {
+    if (tid == 0) nrot = 0;
+    __syncthreads();
+    for (int r = 0; r < mp - 1; r++) {
+      for (int k = tid; k < npairs; k += nt) {
+        int p, q;
+        rr_pair(mp, r, k, &p, &q);
+        T c = T(1), s = T(0);
+        unsigned char doit = 0;
+        if (q < m) {
+          const T apq = M[p + (size_t)q * mp];
+          const T app = M[p + (size_t)p * mp], aqq = M[q + (size_t)q * mp];
+          if (fabs((double)apq) > 1e-300 &&
+              fabs((double)apq) > tol * sqrt(fabs((double)app) * fabs((double)aqq))) {
+            const T theta = (aqq - app) / (T(2) * apq);
+            const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+            c = T(1) / sqrt(t * t + T(1));
+            s = t * c;
+            doit = 1;
+            atomicAdd(&nrot, 1);
+          }
+        }
+        cs[k] = c;
+        sn[k] = s;
+        rot[k] = doit;
+      }
+      __syncthreads();
+      // rows p, q of M  (M <- J^T M)
+      for (int e = tid; e < npairs * m; e += nt) {
+        const int k = e % npairs, j = e / npairs;
+        if (!rot[k]) continue;
+        int p, q;
+        rr_pair(mp, r, k, &p, &q);
+        const T c = cs[k], s = sn[k];
+        const T mp_ = M[p + (size_t)j * mp], mq = M[q + (size_t)j * mp];
+        M[p + (size_t)j * mp] = c * mp_ - s * mq;
+        M[q + (size_t)j * mp] = s * mp_ + c * mq;
+      }
+      __syncthreads();
+      // columns p, q of M and Q  (M <- M J, Q <- Q J)
+      for (int e = tid; e < npairs * m; e += nt) {
+        const int k = e % npairs, i = e / npairs;
+        if (!rot[k]) continue;
+        int p, q;
+        rr_pair(mp, r, k, &p, &q);
+        const T c = cs[k], s = sn[k];
+        const T mp_ = M[i + (size_t)p * mp], mq = M[i + (size_t)q * mp];
+        M[i + (size_t)p * mp] = c * mp_ - s * mq;
+        M[i + (size_t)q * mp] = s * mp_ + c * mq;
+        const T qp = Q[i + (size_t)p * mp], qq = Q[i + (size_t)q * mp];
+        Q[i + (size_t)p * mp] = c * qp - s * qq;
+        Q[i + (size_t)q * mp] = s * qp + c * qq;
+      }
+      __syncthreads();
+      for (int k = tid; k < npairs; k += nt) {
+        if (!rot[k]) continue;
+        int p, q;
+        rr_pair(mp, r, k, &p, &q);
+        M[p + (size_t)q * mp] = T(0);
+        M[q + (size_t)p * mp] = T(0);
+      }
+      __syncthreads();
+    }
+    if (nrot == 0) {
+      converged = true;
+      break;
+    }
+    __syncthreads();
+  }
+  if (!converged) {
+    // accept a result whose off-diagonal part is negligible anyway
+    double off = 0.0;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e % m, j = e / m;
+      if (i != j) {
+        const double v = (double)M[i + (size_t)j * mp];
+        off += v * v;
+      }
+    }
+    off = block_sum1024(off, red);
+    converged = off <= (mode == 1 ? 1e-10 : 1e-28) * tot;
+  }
+  if (mode == 1) {
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e % m, j = e / m;
+      evec[i + (size_t)j * lde] = (double)Q[i + (size_t)j * mp];
+    }
+    if (tid == 0) status[0] = converged ? sweep : -1;
+    return;
+  }
+  // ascending order by rank (ties broken by index)
+  for (int i = tid; i < m; i += nt) {
+    const double di = (double)M[i + (size_t)i * mp];
+    int rk = 0;
+    for (int j = 0; j < m; j++) {
+      const double dj = (double)M[j + (size_t)j * mp];
+      if (dj < di || (dj == di && j < i)) rk++;
+    }
+    rank_of[rk] = i;
+  }
+  __syncthreads();
+  const int nout = iu - il + 1;
+  for (int kk = tid; kk < nout; kk += nt)
+    eval[kk] = (double)M[rank_of[il - 1 + kk] * (size_t)(mp + 1)];
+  // eigenvector columns, sign fixed so the largest-magnitude entry is positive
+  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  for (int kk = warp; kk < nout; kk += nw) {
+    const int c = rank_of[il - 1 + kk];
+    double best = -1.0, bv = 0.0;
+    int bi = m;
+    for (int i = lane; i < m; i += 32) {
+      const double v = (double)Q[i + (size_t)c * mp];
+      if (fabs(v) > best || (fabs(v) == best && i < bi)) {
+        best = fabs(v);
+        bv = v;
+        bi = i;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const double ov = __shfl_down_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bv = ov;
+        bi = oi;
+      }
+    }
+    bv = __shfl_sync(0xffffffffu, bv, 0);
+    const double sg = bv < 0 ? -1.0 : 1.0;
+    for (int i = lane; i < m; i += 32)
+      evec[i + (size_t)kk * lde] = sg * (double)Q[i + (size_t)c * mp];
+  }
+  if (tid == 0) status[0] = converged ? sweep : -1;
+}
+
+// ------------------------------------------------------------ subspace MGS
+// Orthonormalise columns [start, *end) of V (nrows x ldV, Euclidean inner
+// product) against each other, two Gram-Schmidt passes per column; a column
+// whose norm after projection is <= tol is dropped by moving the last
+// column into its place (GCGE_MultiOrthonormalizationInSubspace semantics,
+// src/gcge_orthogonal.c:2278-2352).  Writes the new end to *end_out.
+__global__ void __launch_bounds__(256) k_sub_mgs(double* __restrict__ V, int ldV, int nrows,
+                                                 int start, int end, double tol,
+                                                 int* __restrict__ end_out) {
+  __shared__ double red[32];
+  __shared__ double proj[256];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int cur = start;
+  while (cur < end) {
+    double* v = V + (size_t)cur * ldV;
+    for (int pass = 0; pass < 2; pass++) {
+      // projections onto the kept columns start..cur-1 (classical GS, one warp each)
+      const int warp = tid >> 5, lane = tid & 31;
+      for (int j = start + warp; j < cur; j += nt >> 5) {
+        const double* u = V + (size_t)j * ldV;
+        double s = 0.0;
+        for (int i = lane; i < nrows; i += 32) s = fma(u[i], v[i], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) proj[j - start] = s;
+      }
+      __syncthreads();
+      for (int i = tid; i < nrows; i += nt) {
+        double x = v[i];
+        for (int j = start; j < cur; j++) x = fma(-proj[j - start], V[i + (size_t)j * ldV], x);
+        v[i] = x;
+      }
+      __syncthreads();
+    }
+    double s = 0.0;
+    for (int i = tid; i < nrows; i += nt) s = fma(v[i], v[i], s);
+    s = block_sum1024(s, red);
+    const double nv = sqrt(s);
+    if (nv > tol) {
+      for (int i = tid; i < nrows; i += nt) v[i] *= 1.0 / nv;
+      __syncthreads();
+      cur++;
+    } else {
+      // move the last column into cur and shrink
+      const double* last = V + (size_t)(end - 1) * ldV;
+      if (cur < end - 1)
+        for (int i = tid; i < nrows; i += nt) v[i] = last[i];
+      __syncthreads();
+      end--;
+    }
+  }
+  if (tid == 0) *end_out = end;
+}
+
+// ------------------------------------------------------------ Cholesky
+// G: k x k Gram block (ldg).  Right-looking Cholesky G = R^T R in column
+// order; a pivot <= tol^2 drops that column (MGS zero-vector semantics of
+// GCGE_SubOrthonormalizationSelfBGS, src/gcge_orthogonal.c:2180-2263).
+// Outputs kept[0..nk) (original indices, ascending), *nk_out, and
+// T = R^{-1} restricted to the kept columns (nk x nk, ldt = k).
+__global__ void __launch_bounds__(256) k_chol_drop(int k, const double* __restrict__ G, int ldg,
+                                                   double tol2, double* __restrict__ T,
+                                                   int* __restrict__ kept,
+                                                   int* __restrict__ nk_out) {
+  extern __shared__ double sm[];
+  double* M = sm;              // k x k working copy
+  double* R = sm + k * k;      // k x k upper factor (rows of kept pivots)
+  __shared__ int keep[GCGE_MAXCOLS];
+  __shared__ int pos[GCGE_MAXCOLS];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < k * k; e += nt) {
+    const int i = e % k, j = e / k;
+    M[e] = G[i + (size_t)j * ldg];
+    R[e] = 0.0;
+  }
+  __syncthreads();
+  for (int j = 0; j < k; j++) {
+    const double d = M[j + j * k];
+    const bool ok = d > tol2;  // false for NaN too
+    if (tid == 0) keep[j] = ok ? 1 : 0;
+    if (ok) {
+      const double r = sqrt(d);
+      for (int i = j + tid; i < k; i += nt) R[j + i * k] = (i == j) ? r : M[j + i * k] / r;
+      __syncthreads();
+      for (int e = tid; e < k * k; e += nt) {
+        const int a = e % k, b = e / k;
+        if (a > j && b > j) M[e] -= R[j + a * k] * R[j + b * k];
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    int nk = 0;
+    for (int j = 0; j < k; j++) {
+      pos[j] = keep[j] ? nk : -1;
+      if (keep[j]) kept[nk++] = j;
+    }
+    *nk_out = nk;
+    pos[GCGE_MAXCOLS - 1] = nk;
+  }
+  __syncthreads();
+  const int nk = pos[GCGE_MAXCOLS - 1];
+  // T = R_kept^{-1}: thread per column c solves R x = e_c by back substitution
+  for (int c = tid; c < nk; c += nt) {
+    for (int rI = nk - 1; rI >= 0; rI--) {
+      double x = (rI == c) ? 1.0 : 0.0;
+      const int gr = kept[rI];
+      for (int l = rI + 1; l <= c; l++) x -= R[gr + kept[l] * k] * T[l + (size_t)c * k];
+      T[rI + (size_t)c * k] = (rI > c) ? 0.0 : x / R[gr + gr * k];
+    }
+  }
+}
+
+// dst[:, j] rows [0, rows) <- src column idx[j] rows [r0, r0+rows); used to
+// build the P coefficient block from the unconverged Ritz coefficient
+// columns (GCGE_ComputeP, src/gcge_xpw.c:371-383).
+__global__ void k_gather_cols(const double* __restrict__ src, int lds, int r0, int rows,
+                              IntList idx, int ncols, double* __restrict__ dst, int ldd) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * ncols) return;
+  const int i = e % rows, j = e / rows;
+  dst[i + (size_t)j * ldd] = src[r0 + i + (size_t)idx.v[j] * lds];
+}
+
+__global__ void k_set_diag(double* __restrict__ M, int ld, const double* __restrict__ d, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) M[i + (size_t)i * ld] = d[i];
+}
+
+__global__ void k_add_diag(double* __restrict__ M, int ld, double s, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) M[i + (size_t)i * ld] += s;
+}
+
+__global__ void k_sqrt_div(const double* __restrict__ r2, const double* __restrict__ x2,
+                           double* __restrict__ out, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) out[i] = sqrt(r2[i]) / sqrt(x2[i]);
+}
+
+}  // namespace
+
+void dgemm_small(bool ta, bool tb, bool symA, int m, int n, int k, double alpha, const double* A,
+                 int lda, const double* B, int ldb, double beta, double* C, int ldc,
+                 cudaStream_t st) {
+  if (m <= 0 || n <= 0) return;
+  const int tot = m * n;
+  k_dgemm_small<<<(tot + 127) / 128, 128, 0, st>>>(ta, tb, symA, m, n, k, alpha, A, lda, B, ldb,
+                                                   beta, C, ldc);
+}
+
+size_t jacobi_smem_bytes(int nrows) {
+  const int mp = (nrows % 2) ? nrows + 1 : nrows;
+  return sizeof(double) * 2 * (size_t)mp * mp;
+}
+
+template <typename T>
+static void launch_jacobi(int nrows, const double* a, int lda, double* eval, double* evec, int lde,
+                          int il, int iu, T* work, int* status, int mode, double tol,
+                          int max_sweeps, cudaStream_t st) {
+  const int mp = (nrows % 2) ? nrows + 1 : nrows;
+  const size_t sm = sizeof(T) * 2 * (size_t)mp * mp;
+  const int use_smem = sm <= 200 * 1024 ? 1 : 0;
+  if (use_smem) {
+    cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_jacobi<T><<<1, 1024, sm, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, 1, status, mode,
+                                     tol, max_sweeps);
+  } else {
+    k_jacobi<T><<<1, 1024, 0, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, 0, status, mode,
+                                    tol, max_sweeps);
+  }
+}
+
+// Newton-Schulz step Q <- 1.5 Q - 0.5 Q (Q^T Q), which squares the
+// departure from orthogonality.
+static void orth_newton_schulz(int m, double* Q, double* G, double* Qn, cudaStream_t st) {
+  dgemm_small(true, false, false, m, m, m, 1.0, Q, m, Q, m, 0.0, G, m, st);
+  cudaMemcpyAsync(Qn, Q, sizeof(double) * m * m, cudaMemcpyDeviceToDevice, st);
+  dgemm_small(false, false, false, m, m, m, -0.5, Q, m, G, m, 1.5, Qn, m, st);
+}
+
+void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec, int lde, int il,
+                int iu, double* work, int* status, cudaStream_t st) {
+  if (nrows <= 0) return;
+  const int m = nrows;
+  if (m <= 16) {
+    launch_jacobi<double>(m, a, lda, eval, evec, lde, il, iu, work, status, 0, 1e-15, 60, st);
+    return;
+  }
+  // 1. FP32 Jacobi: an eigenvector basis Q accurate to single precision
+  // 2. two Newton-Schulz steps make Q orthogonal to FP64 rounding
+  // 3. M1 = Q^T A Q is diagonal up to ~1e-7 ||A||; FP64 Jacobi on M1
+  //    converges in two or three sweeps
+  // 4. eigenvectors = Q * (eigenvectors of M1)
+  const size_t mm = (size_t)m * m;
+  const int mp = m + 1;
+  double* Q = work;
+  double* G = Q + mm;
+  double* Qn = G + mm;
+  double* T1 = Qn + mm;
+  double* M1 = T1 + mm;
+  double* Z = M1 + mm;
+  void* jw = Z + mm;  // Jacobi global scratch (2 mp^2 of T)
+  launch_jacobi<float>(m, a, lda, eval, Q, m, 1, m, (float*)jw, status, 1, 1e-6, 30, st);
+  orth_newton_schulz(m, Q, G, Qn, st);
+  orth_newton_schulz(m, Qn, G, Q, st);
+  // T1 = A Q (A symmetric from its upper triangle), M1 = Q^T T1
+  dgemm_small(false, false, true, m, m, m, 1.0, a, lda, Q, m, 0.0, T1, m, st);
+  dgemm_small(true, false, false, m, m, m, 1.0, Q, m, T1, m, 0.0, M1, m, st);
+  launch_jacobi<double>(m, M1, m, eval, Z, m, il, iu, (double*)jw, status, 0, 1e-15, 60, st);
+  const int nout = iu - il + 1;
+  dgemm_small(false, false, false, m, nout, m, 1.0, Q, m, Z, m, 0.0, evec, lde, st);
+  (void)mp;
+}
+
+size_t jacobi_work_doubles(int nrows) {
+  const size_t m = nrows, mp = nrows + 1;
+  return 6 * m * m + 2 * mp * mp + 16;
+}
+
+void sub_mgs(double* V, int ldV, int nrows, int start, int end, double tol, int* end_out,
+             cudaStream_t st) {
+  k_sub_mgs<<<1, 256, 0, st>>>(V, ldV, nrows, start, end, tol, end_out);
+}
+
+void chol_drop(int k, const double* G, int ldg, double tol, double* T, int* kept, int* nk,
+               cudaStream_t st) {
+  const size_t sm = sizeof(double) * 2 * (size_t)k * k;
+  if (sm > 48 * 1024) cudaFuncSetAttribute(k_chol_drop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_chol_drop<<<1, 256, sm, st>>>(k, G, ldg, tol * tol, T, kept, nk);
+}
+
+void gather_cols(const double* src, int lds, int r0, int rows, const IntList& idx, int ncols,
+                 double* dst, int ldd, cudaStream_t st) {
+  const int tot = rows * ncols;
+  if (tot <= 0) return;
+  k_gather_cols<<<(tot + 255) / 256, 256, 0, st>>>(src, lds, r0, rows, idx, ncols, dst, ldd);
+}
+
+void set_diag(double* M, int ld, const double* d, int k, cudaStream_t st) {
+  if (k <= 0) return;
+  k_set_diag<<<(k + 127) / 128, 128, 0, st>>>(M, ld, d, k);
+}
+
+void add_diag(double* M, int ld, double s, int k, cudaStream_t st) {
+  if (k <= 0) return;
+  k_add_diag<<<(k + 127) / 128, 128, 0, st>>>(M, ld, s, k);
+}
+
+void sqrt_div(const double* r2, const double* x2, double* out, int k, cudaStream_t st) {
+  if (k <= 0) return;
+  k_sqrt_div<<<(k + 127) / 128, 128, 0, st>>>(r2, x2, out, k);
+}
+
+}  // namespace gcge

@@ -1,0 +1,295 @@
+// Multivector operations of include/gcge_cuda.h in the shape of the GCGE_OPS
+// callbacks (src/gcge_ops.h:76-137), each a synchronous call over device
+// columns.  They share the kernels of the solver.  Scratch (reduction
+// partials, dense staging) is a per-process device buffer grown on demand;
+// concurrent calls from several host threads are not supported.
+#include <mutex>
+#include <vector>
+
+#include "../../include/gcge_cuda.h"
+#include "gcge_cuda_bcg.cuh"
+#include "gcge_cuda_common.cuh"
+#include "gcge_cuda_dense.cuh"
+
+
+namespace {
+
+std::mutex g_mu;
+double* g_scratch = nullptr;
+size_t g_scratch_len = 0;
+
+int scratch(size_t len, double** out) {
+  if (len > g_scratch_len) {
+    if (g_scratch) cudaFree(g_scratch);
+    g_scratch = nullptr;
+    g_scratch_len = 0;
+    if (cudaMalloc(&g_scratch, sizeof(double) * len) != cudaSuccess) return GCGE_CUDA_ERR_ALLOC;
+    g_scratch_len = len;
+  }
+  *out = g_scratch;
+  return GCGE_CUDA_OK;
+}
+
+int finish() {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
+}
+
+ColList<double> mk(double* const* p, int k) {
+  ColList<double> c;
+  for (int i = 0; i < k; i++) c.p[i] = p[i];
+  return c;
+}
+
+}  // namespace
+
+extern "C" int GCGE_CUDA_MatDotMultiVec(const GCGE_CUDA_MAT* A, double* const* x,
+                                        double* const* y, int k) {
+  if (!A || !x || !y || k < 0 || k > GCGE_MAXCOLS) return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  gcge::spmm_f64(A->m, mk(x, k), mk(y, k), k, 0);
+  return finish();
+}
+
+extern "C" int GCGE_CUDA_MatDotMultiVecAsync(const GCGE_CUDA_MAT* A, double* const* x,
+                                             double* const* y, int k, void* stream) {
+  if (!A || !x || !y || k < 0 || k > GCGE_MAXCOLS) return GCGE_CUDA_ERR_ARG;
+  gcge::spmm_f64(A->m, mk(x, k), mk(y, k), k, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
+}
+
+namespace {
+__global__ void k_val_to_f32(const double* __restrict__ a, float* __restrict__ b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+}  // namespace
+
+extern "C" int GCGE_CUDA_MatDotMultiVecF32Async(GCGE_CUDA_MAT* A, float* const* x,
+                                                float* const* y, int k, void* stream) {
+  if (!A || !x || !y || k < 0 || k > GCGE_MAXCOLS) return GCGE_CUDA_ERR_ARG;
+  if (!A->m.v32) {
+    if (cudaMalloc(&A->m.v32, sizeof(float) * (A->m.nnz > 0 ? A->m.nnz : 1)) != cudaSuccess)
+      return GCGE_CUDA_ERR_ALLOC;
+    if (A->m.nnz > 0)
+      k_val_to_f32<<<(A->m.nnz + 255) / 256, 256, 0, (cudaStream_t)stream>>>(A->m.v, A->m.v32,
+                                                                             A->m.nnz);
+  }
+  ColList<float> X, Y;
+  for (int i = 0; i < k; i++) {
+    X.p[i] = x[i];
+    Y.p[i] = y[i];
+  }
+  gcge::spmm_f32(A->m, X, Y, k, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
+}
+
+extern "C" int GCGE_CUDA_MultiVecInnerProd(double* const* V, int k1, double* const* W, int k2,
+                                           int n, double* a, int lda, int sym) {
+  if (!V || !W || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||
+      lda < k1 || (sym && k1 != k2))
+    return GCGE_CUDA_ERR_ARG;
+  if (k1 == 0 || k2 == 0) return GCGE_CUDA_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int tiles = ((k1 + 63) / 64) * ((k2 + 63) / 64);
+  double* buf;
+  const size_t part = (size_t)gcge::kRowBlocks * tiles * 64 * 64;
+  if (scratch(part + (size_t)k1 * k2, &buf)) return GCGE_CUDA_ERR_ALLOC;
+  double* G = buf + part;
+  gcge::gram_f64(mk(V, k1), k1, mk(W, k2), k2, n, G, k1, sym != 0, buf, 0);
+  std::vector<double> h((size_t)k1 * k2);
+  if (cudaMemcpy(h.data(), G, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  for (int j = 0; j < k2; j++)
+    for (int i = 0; i < k1; i++) a[i + (size_t)j * lda] = h[i + (size_t)j * k1];
+  return finish();
+}
+
+extern "C" int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W,
+                                                int k2, int n, double* a, int lda, int sym) {
+  if (!V || !W || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||
+      lda < k1 || (sym && k1 != k2))
+    return GCGE_CUDA_ERR_ARG;
+  if (k1 == 0 || k2 == 0) return GCGE_CUDA_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const size_t part = gcge::gram_oz_partial_doubles(k1, k2);
+  double* buf;
+  if (scratch(part + (size_t)k1 * k2, &buf)) return GCGE_CUDA_ERR_ALLOC;
+  double* G = buf + part;
+  gcge::gram_oz(mk(V, k1), k1, mk(W, k2), k2, n, G, k1, sym != 0, buf, 0);
+  std::vector<double> h((size_t)k1 * k2);
+  if (cudaMemcpy(h.data(), G, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  for (int j = 0; j < k2; j++)
+    for (int i = 0; i < k1; i++) a[i + (size_t)j * lda] = h[i + (size_t)j * k1];
+  return finish();
+}
+
+extern "C" int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int k2,
+                                            int n, const double* a, int lda, double beta) {
+  if (!x || !y || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||
+      lda < k1)
+    return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  double* C;
+  if (scratch((size_t)(k1 > 0 ? k1 : 1) * (k2 > 0 ? k2 : 1), &C)) return GCGE_CUDA_ERR_ALLOC;
+  std::vector<double> h((size_t)k1 * k2);
+  for (int j = 0; j < k2; j++)
+    for (int i = 0; i < k1; i++) h[i + (size_t)j * k1] = a[i + (size_t)j * lda];
+  if (!h.empty() &&
+      cudaMemcpy(C, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  gcge::lincomb_f64(mk(x, k1), k1, C, k1, mk(y, k2), k2, beta, n, 0);
+  return finish();
+}
+
+extern "C" int GCGE_CUDA_MultiVecLinearCombOzaki(double* const* x, int k1, double* const* y,
+                                                  int k2, int n, const double* a, int lda,
+                                                  double beta) {
+  if (!x || !y || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||
+      lda < k1)
+    return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const size_t cb = (size_t)(k1 > 0 ? k1 : 1) * (k2 > 0 ? k2 : 1);
+  const size_t sb = (gcge::lincomb_oz_scratch_bytes(k1, k2) + 15) / 8 + 2;
+  double* buf;
+  if (scratch(cb + sb, &buf)) return GCGE_CUDA_ERR_ALLOC;
+  double* C = buf;
+  void* sc = reinterpret_cast<void*>(((uintptr_t)(buf + cb) + 15) & ~(uintptr_t)15);
+  std::vector<double> h(cb, 0.0);
+  for (int j = 0; j < k2; j++)
+    for (int i = 0; i < k1; i++) h[i + (size_t)j * k1] = a[i + (size_t)j * lda];
+  if (cudaMemcpy(C, h.data(), sizeof(double) * cb, cudaMemcpyHostToDevice) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  gcge::lincomb_oz(mk(x, k1), k1, C, k1 > 0 ? k1 : 1, mk(y, k2), k2, beta, n, sc, 0);
+  return finish();
+}
+
+extern "C" int GCGE_CUDA_MultiVecAxpby(double alpha, double* const* x, double beta,
+                                       double* const* y, int k, int n) {
+  if (!x || !y || k < 0 || k > GCGE_MAXCOLS || n <= 0) return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  gcge::axpby_f64(alpha, mk(x, k), beta, mk(y, k), k, n, 0);
+  return finish();
+}
+
+extern "C" int GCGE_CUDA_DenseMatEigenSolver(const double* a, int lda, int nrows, double* eval,
+                                             double* evec, int lde, int il, int iu) {
+  if (!a || !eval || !evec || nrows <= 0 || nrows > 256 || lda < nrows || lde < nrows || il < 1 ||
+      iu < il || iu > nrows)
+    return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int m = iu - il + 1;
+  const size_t need = (size_t)nrows * nrows + (size_t)nrows * m + m +
+                      gcge::jacobi_work_doubles(nrows) + 1;
+  double* buf;
+  if (scratch(need, &buf)) return GCGE_CUDA_ERR_ALLOC;
+  double* dA = buf;
+  double* dV = dA + (size_t)nrows * nrows;
+  double* dE = dV + (size_t)nrows * m;
+  double* work = dE + m;
+  int* status = reinterpret_cast<int*>(work + gcge::jacobi_work_doubles(nrows));
+  if (cudaMemcpy2D(dA, sizeof(double) * nrows, a, sizeof(double) * lda, sizeof(double) * nrows,
+                   nrows, cudaMemcpyHostToDevice) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  gcge::jacobi_eig(nrows, dA, nrows, dE, dV, nrows, il, iu, work, status, 0);
+  int st = 0;
+  if (cudaMemcpy(&st, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  if (cudaMemcpy(eval, dE, sizeof(double) * m, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  if (cudaMemcpy2D(evec, sizeof(double) * lde, dV, sizeof(double) * nrows, sizeof(double) * nrows,
+                   m, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  if (st < 0) return GCGE_CUDA_ERR_NUMERIC;
+  return finish();
+}
+
+namespace {
+__global__ void k_cvt_d2f(const double* __restrict__ a, float* __restrict__ b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+__global__ void k_cvt_f2d(const float* __restrict__ a, double* __restrict__ b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+}  // namespace
+
+extern "C" int GCGE_CUDA_BlockCG(const GCGE_CUDA_MAT* A, double* const* rhs, double* const* x,
+                                 int k, int n, int max_it, double rate, int fp32, int* steps) {
+  if (!A || !rhs || !x || k <= 0 || k > GCGE_MAXCOLS || n != A->m.n) return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int nb = gcge::kRowBlocks;
+  const size_t ld = ((size_t)n + 31) / 32 * 32;
+  // scalars: 6 arrays of k doubles, partial k*nb, vectors (P, W, and for FP32
+  // also RHS, X copies) in the precision of the solve
+  const size_t nvec = fp32 ? 4 : 2;
+  const size_t vec_doubles = fp32 ? (nvec * k * ld + 1) / 2 + 1 : nvec * k * ld;
+  double* buf;
+  if (scratch(6 * (size_t)GCGE_MAXCOLS + (size_t)k * nb + vec_doubles + GCGE_MAXCOLS, &buf))
+    return GCGE_CUDA_ERR_ALLOC;
+  int* ints = nullptr;
+  int* pinned = nullptr;
+  if (cudaMalloc(&ints, sizeof(int) * (GCGE_MAXCOLS + 1)) != cudaSuccess) return GCGE_CUDA_ERR_ALLOC;
+  if (cudaHostAlloc(&pinned, sizeof(int) * 4, cudaHostAllocMapped) != cudaSuccess) {
+    cudaFree(ints);
+    return GCGE_CUDA_ERR_ALLOC;
+  }
+  gcge::BcgScalars s;
+  s.rho1 = buf;
+  s.rho2 = buf + GCGE_MAXCOLS;
+  s.err = buf + 2 * GCGE_MAXCOLS;
+  s.lerr = buf + 3 * GCGE_MAXCOLS;
+  s.ptw = buf + 4 * GCGE_MAXCOLS;
+  s.rnew = buf + 5 * GCGE_MAXCOLS;
+  s.unl = ints;
+  s.nu = ints + GCGE_MAXCOLS;
+  s.nu_host = pinned;
+  double* partial = buf + 6 * GCGE_MAXCOLS;
+  double* vecs = partial + (size_t)k * nb;
+  int it = -1;
+  GcgeDevCsr M = A->m;
+  if (!fp32) {
+    ColList<double> R = mk(rhs, k), X = mk(x, k), P, W;
+    for (int j = 0; j < k; j++) {
+      P.p[j] = vecs + (size_t)j * ld;
+      W.p[j] = vecs + (size_t)(k + j) * ld;
+    }
+    it = gcge::bcg_run<double>(M.rp, M.ci, M.v, n, R, X, P, W, k, max_it, rate, s, partial, 0,
+                               nullptr);
+  } else {
+    float* f = reinterpret_cast<float*>(vecs);
+    float* v32 = nullptr;
+    if (cudaMalloc(&v32, sizeof(float) * (M.nnz > 0 ? M.nnz : 1)) != cudaSuccess) {
+      cudaFree(ints);
+      cudaFreeHost(pinned);
+      return GCGE_CUDA_ERR_ALLOC;
+    }
+    if (M.nnz > 0) k_cvt_d2f<<<(M.nnz + 255) / 256, 256>>>(M.v, v32, M.nnz);
+    ColList<float> R, X, P, W;
+    for (int j = 0; j < k; j++) {
+      R.p[j] = f + (size_t)j * ld;
+      X.p[j] = f + (size_t)(k + j) * ld;
+      P.p[j] = f + (size_t)(2 * k + j) * ld;
+      W.p[j] = f + (size_t)(3 * k + j) * ld;
+      k_cvt_d2f<<<(n + 255) / 256, 256>>>(rhs[j], R.p[j], n);
+      k_cvt_d2f<<<(n + 255) / 256, 256>>>(x[j], X.p[j], n);
+    }
+    it = gcge::bcg_run<float>(M.rp, M.ci, v32, n, R, X, P, W, k, max_it, rate, s, partial, 0,
+                              nullptr);
+    for (int j = 0; j < k; j++) {
+      k_cvt_f2d<<<(n + 255) / 256, 256>>>(X.p[j], x[j], n);
+      k_cvt_f2d<<<(n + 255) / 256, 256>>>(R.p[j], rhs[j], n);
+    }
+    cudaDeviceSynchronize();
+    cudaFree(v32);
+  }
+  const int rc = finish();
+  cudaFree(ints);
+  cudaFreeHost(pinned);
+  if (steps) *steps = it;
+  if (it < 0) return GCGE_CUDA_ERR_CUDA;
+  return rc;
+}

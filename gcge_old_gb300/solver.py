@@ -1,0 +1,127 @@
+"""Python mirror of the GCGE solver interface over the CUDA C ABI.
+
+``GCGESolver`` follows GCGE_SOLVER (src/gcge_solver.h:42-60): build it from
+CSR matrices, set -gcge_* parameters (names of src/gcge_para.c:128-407),
+give the initial block, ``solve()``, read eigenvalues/eigenvectors.  The
+matrices are copied to the device once (``GCGE_CUDA_MatCreate``); inputs and
+outputs of ``solve`` are host arrays, as for the reference CSR app.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import lib as L
+from .matrices import CSRMatrix
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class DeviceMatrix:
+    """A CSR matrix resident on the GPU (GCGE_CUDA_MAT)."""
+
+    def __init__(self, m: CSRMatrix):
+        self._lib = L.load()
+        self.n = m.n
+        self._h = (np.ascontiguousarray(m.rowptr, dtype=np.int32),
+                   np.ascontiguousarray(m.col, dtype=np.int32),
+                   np.ascontiguousarray(m.val, dtype=np.float64))
+        h = C.c_void_p()
+        L.check(self._lib.GCGE_CUDA_MatCreate(C.byref(h), m.n, _ptr(self._h[0]), _ptr(self._h[1]),
+                                              _ptr(self._h[2]), 0), "MatCreate")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            h = self.handle
+            self._lib.GCGE_CUDA_MatDestroy(C.byref(h))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GCGESolver:
+    """GCG eigensolver for A x = lambda B x on one GPU.
+
+    params: mapping of GCGE_PARA names (``nev``, ``ev_tol``, ``block_size``,
+    ``ev_max_it``, ``cg_max_it``, ``cg_rate``, ...) plus ``precision``
+    ("fp64" or "mixed": FP32 block CG on FP32 copies of A).
+    """
+
+    INT_PARAMS = {"nev", "ev_max_it", "block_size", "num_init_evec", "cg_max_it",
+                  "max_reorth_time", "print_level", "gemm"}
+
+    def __init__(self, A, B=None, nev: int = 1, **params):
+        self._lib = L.load()
+        self.A = A if isinstance(A, DeviceMatrix) else DeviceMatrix(A)
+        self.B = None if B is None else (B if isinstance(B, DeviceMatrix) else DeviceMatrix(B))
+        self.n = self.A.n
+        self.nev = nev
+        h = C.c_void_p()
+        L.check(self._lib.GCGE_CUDA_SOLVER_Create(C.byref(h)), "SOLVER_Create")
+        self.handle = h
+        L.check(self._lib.GCGE_CUDA_SOLVER_SetMatA(h, self.A.handle), "SetMatA")
+        L.check(self._lib.GCGE_CUDA_SOLVER_SetMatB(h, self.B.handle if self.B else None), "SetMatB")
+        L.check(self._lib.GCGE_CUDA_SOLVER_SetNumEigen(h, nev), "SetNumEigen")
+        params.setdefault("num_init_evec", nev)
+        for k, v in params.items():
+            if k == "precision":
+                v = {"fp64": 0, "mixed": 1}.get(v, v)
+                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"precision", int(v)), k)
+            elif k == "gemm":
+                v = {"fp64": 0, "ozaki": 1}.get(v, v)
+                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"gemm", int(v)), k)
+            elif k in self.INT_PARAMS:
+                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, k.encode(), int(v)), k)
+            else:
+                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamDouble(h, k.encode(), float(v)), k)
+        self.eval = np.zeros(nev)
+        self.evec = np.zeros((nev, self.n))  # column j of the n x nev block is evec[j]
+        L.check(self._lib.GCGE_CUDA_SOLVER_SetEigenvalues(h, _ptr(self.eval)), "SetEigenvalues")
+        L.check(self._lib.GCGE_CUDA_SOLVER_SetEigenvectors(h, _ptr(self.evec)), "SetEigenvectors")
+        L.check(self._lib.GCGE_CUDA_SOLVER_Setup(h), "Setup")
+
+    def solve(self, x0: np.ndarray):
+        """x0: initial block, shape (nev, n) (= column-major n x nev)."""
+        self.evec[...] = np.asarray(x0, dtype=np.float64).reshape(self.nev, self.n)
+        L.check(self._lib.GCGE_CUDA_SOLVER_Solve(self.handle), "Solve")
+        return self.eval.copy(), self.evec.copy()
+
+    def residuals(self) -> np.ndarray:
+        r = np.zeros(self.nev)
+        L.check(self._lib.GCGE_CUDA_SOLVER_GetResiduals(self.handle, _ptr(r)), "GetResiduals")
+        return r
+
+    def stats(self) -> dict:
+        st = L.Stats()
+        L.check(self._lib.GCGE_CUDA_SOLVER_GetStats(self.handle, C.byref(st)), "GetStats")
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            h = self.handle
+            self._lib.GCGE_CUDA_SOLVER_Free(C.byref(h))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve(A, B, nev, x0, **params):
+    """One-shot solve: returns (eigenvalues, eigenvectors (nev x n), stats)."""
+    s = GCGESolver(A, B, nev, **params)
+    try:
+        ev, vec = s.solve(x0)
+        return ev, vec, s.stats()
+    finally:
+        s.close()

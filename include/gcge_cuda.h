@@ -1,0 +1,161 @@
+/*
+ * gcge_cuda.h — C ABI of the GB300-native GCG eigensolver.
+ *
+ * A CUDA-backed app that sits beside the reference's CSR app (app/csr/):
+ * it solves A x = lambda B x for the nev smallest eigenpairs of sparse
+ * symmetric A and SPD B (B = NULL means the identity) with the GCG
+ * iteration, entirely on one GPU.  Every entry point returns an int status
+ * (0 = success, see GCGE_CUDA_ERR_*); the reference's callbacks return void
+ * and exit() on fatal errors (src/gcge_eigsol.c:904-905), which a library
+ * must not do.
+ *
+ * Plain C types only: host arrays are host pointers, "device" arrays are
+ * CUDA device pointers, multivectors are arrays of column pointers (the
+ * shape of the reference's default "void**" multivector, src/gcge_ops.c).
+ */
+#ifndef GCGE_CUDA_H_
+#define GCGE_CUDA_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCGE_CUDA_OK 0
+#define GCGE_CUDA_ERR_ARG 1
+#define GCGE_CUDA_ERR_CUDA 2
+#define GCGE_CUDA_ERR_ALLOC 3
+#define GCGE_CUDA_ERR_STATE 4
+#define GCGE_CUDA_ERR_NUMERIC 5
+
+/* Layout-compatible with the reference's CSR_MAT (app/csr/gcge_app_csr.h:27-41):
+ * 0-based int32 row pointers and column indices, double entries, so a
+ * CSR_MAT* can be passed where a GCGE_CUDA_CSR_HOST* is expected. */
+typedef struct GCGE_CUDA_CSR_HOST_ {
+  int N_Rows;
+  int N_Columns;
+  int N_Entries;
+  int* KCol;
+  int* RowPtr;
+  double* Entries;
+} GCGE_CUDA_CSR_HOST;
+
+typedef struct GCGE_CUDA_MAT_ GCGE_CUDA_MAT;       /* device CSR matrix */
+typedef struct GCGE_CUDA_SOLVER_ GCGE_CUDA_SOLVER; /* solver state */
+
+/* Counters of the last Solve (see GCGE_CUDA_SOLVER_GetStats). */
+typedef struct GCGE_CUDA_STATS_ {
+  int num_iter;            /* GCG iterations, as para->num_iter counts them */
+  int num_conv_continuous; /* leading converged pairs */
+  int bcg_steps;           /* block-CG steps over all W computations */
+  long long kernel_launches;
+  double seconds;          /* wall time of Solve, host clock */
+  double t_x_orth, t_rr_mat, t_rr_eig, t_x_axpy, t_p, t_w_line, t_w_orth, t_conv;
+} GCGE_CUDA_STATS;
+
+/* ---------------------------------------------------------------- errors */
+const char* GCGE_CUDA_GetErrorString(int code);
+/* Message of the last failing call in this thread. */
+const char* GCGE_CUDA_GetLastErrorMessage(void);
+
+/* ---------------------------------------------------------------- matrices */
+/* Copy a host CSR matrix to the device (replaces CSR_MAT for the solver;
+ * the reference's equivalents are CSR_ReadMatFile + the CSR_MAT struct). */
+int GCGE_CUDA_MatCreateFromCSR(GCGE_CUDA_MAT** mat, const GCGE_CUDA_CSR_HOST* csr);
+/* rowptr/col/val are host arrays when on_device == 0, device arrays otherwise
+ * (then they are copied too, the caller keeps ownership). */
+int GCGE_CUDA_MatCreate(GCGE_CUDA_MAT** mat, int n, const int* rowptr, const int* col,
+                        const double* val, int on_device);
+int GCGE_CUDA_MatDestroy(GCGE_CUDA_MAT** mat);
+
+/* ---------------------------------------------------------------- solver
+ * Mirrors GCGE_SOLVER (src/gcge_solver.h:42-60): Create, Set*, Setup,
+ * Solve, Get*, Free.  Parameter names and defaults follow GCGE_PARA
+ * (src/gcge_para.c:25-113) and its -gcge_* command-line flags
+ * (src/gcge_para.c:128-407).  Extra flag: -gcge_precision fp64|mixed. */
+int GCGE_CUDA_SOLVER_Create(GCGE_CUDA_SOLVER** solver);
+int GCGE_CUDA_SOLVER_SetMatA(GCGE_CUDA_SOLVER* solver, GCGE_CUDA_MAT* A);
+int GCGE_CUDA_SOLVER_SetMatB(GCGE_CUDA_SOLVER* solver, GCGE_CUDA_MAT* B);
+int GCGE_CUDA_SOLVER_SetNumEigen(GCGE_CUDA_SOLVER* solver, int nev);
+/* Host arrays of nev doubles / n*nev doubles (column-major) that receive the
+ * result; evec also carries the initial block when num_init_evec >= nev
+ * (src/gcge_eigsol.c:134,219-242). */
+int GCGE_CUDA_SOLVER_SetEigenvalues(GCGE_CUDA_SOLVER* solver, double* eval);
+int GCGE_CUDA_SOLVER_SetEigenvectors(GCGE_CUDA_SOLVER* solver, double* evec);
+/* Same as SetEigenvectors with a DEVICE array of n*nev doubles (column j at
+ * evec + j*n): the initial block is read from and the result written to
+ * device memory, so a caller that keeps its data in HBM pays no transfer. */
+int GCGE_CUDA_SOLVER_SetEigenvectorsDevice(GCGE_CUDA_SOLVER* solver, double* evec);
+/* The CUDA stream (cudaStream_t) the solver runs on, for event timing. */
+int GCGE_CUDA_SOLVER_GetStream(GCGE_CUDA_SOLVER* solver, void** stream);
+int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* solver, int argc, char** argv);
+int GCGE_CUDA_SOLVER_SetParamInt(GCGE_CUDA_SOLVER* solver, const char* name, int value);
+int GCGE_CUDA_SOLVER_SetParamDouble(GCGE_CUDA_SOLVER* solver, const char* name, double value);
+int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* solver);
+int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* solver);
+int GCGE_CUDA_SOLVER_GetEigenvalues(GCGE_CUDA_SOLVER* solver, double** eval);
+int GCGE_CUDA_SOLVER_GetEigenvectors(GCGE_CUDA_SOLVER* solver, double** evec);
+/* para->res: the convergence criterion value per pair (src/gcge_eigsol.c:722). */
+int GCGE_CUDA_SOLVER_GetResiduals(GCGE_CUDA_SOLVER* solver, double* res);
+int GCGE_CUDA_SOLVER_GetStats(GCGE_CUDA_SOLVER* solver, GCGE_CUDA_STATS* stats);
+int GCGE_CUDA_SOLVER_Free(GCGE_CUDA_SOLVER** solver);
+
+/* Mirrors GCGE_CSR_Solver_Init (app/csr/gcge_app_csr.c:92-124): creates the
+ * solver for host CSR matrices A and B (B may be NULL), allocates eval/evec,
+ * reads -gcge_* flags and runs Setup.  NULL on failure. */
+GCGE_CUDA_SOLVER* GCGE_CUDA_Solver_Init(const GCGE_CUDA_CSR_HOST* A, const GCGE_CUDA_CSR_HOST* B,
+                                        int num_eigenvalues, int argc, char* argv[]);
+/* Frees the solver and the eval/evec arrays Solver_Init allocated
+ * (GCGE_SOLVER_Free_All, src/gcge_solver.c:75-82). */
+int GCGE_CUDA_SOLVER_Free_All(GCGE_CUDA_SOLVER** solver);
+
+/* ---------------------------------------------------------------- multivector ops
+ * Device kernels in the shape of the GCGE_OPS multivector callbacks
+ * (src/gcge_ops.h:76-127).  Columns are device pointers of length n; the
+ * column-pointer arrays themselves are host arrays.  Synchronous. */
+/* y[j] = A x[j], j < k   (MatDotMultiVec, src/gcge_ops.h:95) */
+int GCGE_CUDA_MatDotMultiVec(const GCGE_CUDA_MAT* A, double* const* x, double* const* y, int k);
+/* Asynchronous y[j] = A x[j] on the given cudaStream_t (NULL = legacy
+ * default stream); no synchronisation, for pipelines and timing. */
+int GCGE_CUDA_MatDotMultiVecAsync(const GCGE_CUDA_MAT* A, double* const* x, double* const* y,
+                                  int k, void* stream);
+/* FP32 variant on the FP32 copy of A (made on first use), float columns;
+ * the SpMM of the mixed-precision inner solve. */
+int GCGE_CUDA_MatDotMultiVecF32Async(GCGE_CUDA_MAT* A, float* const* x, float* const* y, int k,
+                                     void* stream);
+/* a[i + j*lda] = V[i] . W[j] into a HOST array; sym != 0 forms the upper
+ * triangle and mirrors it (MultiVecInnerProd, src/gcge_ops.h:113-114). */
+int GCGE_CUDA_MultiVecInnerProd(double* const* V, int k1, double* const* W, int k2, int n,
+                                double* a, int lda, int sym);
+/* The same inner products with FP64 accuracy on the bf16 tensor cores
+ * (per-32-row column scaling, 8 slices of 7 bits, exact level sums). */
+int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W, int k2, int n,
+                                     double* a, int lda, int sym);
+/* y[j] = sum_i x[i] a[i + j*lda] + beta y[j], a a HOST array
+ * (MultiVecLinearComb, src/gcge_ops.h:109-111). */
+int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int k2, int n,
+                                 const double* a, int lda, double beta);
+/* The same linear combination with FP64 accuracy computed on the bf16
+ * tensor cores (error-free splitting into 8 slices of 7 bits, exact FP32
+ * level sums, 64-bit fixed-point combination); the solver's default for
+ * its X, P and W updates on GB300, where FP64 FMA is ~600x slower than
+ * bf16 MMA. */
+int GCGE_CUDA_MultiVecLinearCombOzaki(double* const* x, int k1, double* const* y, int k2, int n,
+                                      const double* a, int lda, double beta);
+/* y[j] = alpha x[j] + beta y[j] (MultiVecAxpby, src/gcge_ops.h:98-99) */
+int GCGE_CUDA_MultiVecAxpby(double alpha, double* const* x, double beta, double* const* y, int k,
+                            int n);
+/* Eigenpairs il..iu (1-based, ascending) of the symmetric nrows x nrows HOST
+ * matrix a (upper triangle), computed on the device
+ * (DenseMatEigenSolver, src/gcge_ops.h:134-137). */
+int GCGE_CUDA_DenseMatEigenSolver(const double* a, int lda, int nrows, double* eval,
+                                  double* evec, int lde, int il, int iu);
+/* Block CG (GCGE_BCG, src/gcge_cg.c:302-501) on A x_j = rhs_j for k device
+ * columns; rhs is overwritten with the residual.  fp32 != 0 runs it in
+ * single precision on FP32 copies.  *steps receives the final niter. */
+int GCGE_CUDA_BlockCG(const GCGE_CUDA_MAT* A, double* const* rhs, double* const* x, int k, int n,
+                      int max_it, double rate, int fp32, int* steps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GCGE_CUDA_H_ */

@@ -52,7 +52,7 @@ typedef struct {
 static void spmv(const port_csr* M, const double* x, double* y, port_ws* w) {
   const int n = M->n;
   w->spmv_count++;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n > 32768)
   for (int i = 0; i < n; i++) {
     double s = 0.0;
     for (int k = M->rp[i]; k < M->rp[i + 1]; k++) s += M->v[k] * x[M->ci[k]];
@@ -61,19 +61,19 @@ static void spmv(const port_csr* M, const double* x, double* y, port_ws* w) {
 }
 static void axpby(int n, double a, const double* x, double b, double* y) {
   if (a == 0.0) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n > 32768)
     for (int i = 0; i < n; i++) y[i] = b * y[i];
   } else if (b == 0.0) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n > 32768)
     for (int i = 0; i < n; i++) y[i] = a * x[i];
   } else {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n > 32768)
     for (int i = 0; i < n; i++) y[i] = a * x[i] + b * y[i];
   }
 }
 static double dot(int n, const double* x, const double* y) {
   double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
+#pragma omp parallel for reduction(+ : s) schedule(static) if (n > 32768)
   for (int i = 0; i < n; i++) s += x[i] * y[i];
   return s;
 }
@@ -95,7 +95,7 @@ static void mv_lincomb(port_ws* w, double** x, double** y, int s0, int e0, int s
   for (int j = s1; j < e1; j++) {
     const double* aj = a + (size_t)(j - s1) * lda;
     double* yj = y[j];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n > 32768)
     for (int r = 0; r < n; r++) {
       double s = beta == 0.0 ? 0.0 : beta * yj[r];
       for (int i = 0; i < nx; i++) s += aj[i] * x[s0 + i][r];
@@ -646,7 +646,8 @@ void gcge_port_default_para(port_para* p, int nev) {
 int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, const int* b_rp,
                     const int* b_ci, const double* b_v, const port_para* para_in, const double* x0,
                     int max_outer, double* eval_out, double* evec_out, double* res_out,
-                    int* num_iter_out, double* seconds_out, long long* spmv_out) {
+                    int* num_iter_out, double* seconds_out, long long* spmv_out,
+                    double* phase_out) {
   port_csr A = {n, a_rp, a_ci, a_v}, Bm = {n, b_rp, b_ci, b_v};
   port_ws W;
   port_ws* w = &W;
@@ -714,6 +715,7 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
     compute_x(w, nev, w->dim_xpw);
     check_convergence(w);
   }
+  double t_loop = wall();
   int outer = 0;
   while (w->num_conv_continuous < nev && w->num_iter < w->p.ev_max_it) {
     if (max_outer >= 0 && outer >= max_outer) break;
@@ -737,6 +739,12 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
     for (int j = 0; j < s; j++) memcpy(w->evec[j], w->V[j], sizeof(double) * n);
   }
   double t1 = wall();
+  /* phase_out: [time before the loop, time in the loop, loop iterations] */
+  if (phase_out) {
+    phase_out[0] = t_loop - t0;
+    phase_out[1] = t1 - t_loop;
+    phase_out[2] = outer;
+  }
   for (int j = 0; j < nev; j++) {
     eval_out[j] = w->eval[j];
     if (evec_out) memcpy(evec_out + (size_t)j * n, w->evec[j], sizeof(double) * n);
@@ -757,6 +765,25 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
   free(w->unlock);
   free(w->res);
   return 0;
+}
+
+/* Thread count of the OpenMP loops (1 = the reference's single thread). */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+void gcge_port_set_threads(int t) {
+#ifdef _OPENMP
+  if (t > 0) omp_set_num_threads(t);
+#else
+  (void)t;
+#endif
+}
+int gcge_port_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
 }
 
 /* The size of port_para, so callers can check their struct mirror. */

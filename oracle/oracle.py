@@ -84,11 +84,11 @@ def default_para(nev: int, **kw) -> PortPara:
 
 def port_solve(A, B, nev, x0, para: PortPara | None = None, max_outer: int = -1,
                threads: int | None = None):
-    """Run the oracle port.  Returns dict(eval, evec (nev x n rows = columns),
-    res, iters, seconds, spmv)."""
+    """Run the oracle port (threads: OpenMP threads, default 1 like the
+    single-threaded reference).  Returns dict(eval, evec (nev x n rows =
+    columns), res, iters, seconds, spmv)."""
     lib = port_lib()
-    if threads is not None:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
+    lib.gcge_port_set_threads(int(threads) if threads is not None else 1)
     para = para or default_para(nev)
     n = A.n
     x0 = np.ascontiguousarray(x0, dtype=np.float64).reshape(nev, n)
@@ -98,14 +98,16 @@ def port_solve(A, B, nev, x0, para: PortPara | None = None, max_outer: int = -1,
     it = C.c_int(0)
     sec = C.c_double(0)
     nsp = C.c_longlong(0)
+    ph = np.zeros(3)
     rc = lib.gcge_port_solve(
         C.c_int(n), _iptr(A.rowptr), _iptr(A.col), _dptr(A.val),
         _iptr(B.rowptr) if B is not None else None, _iptr(B.col) if B is not None else None,
         _dptr(B.val) if B is not None else None, C.byref(para), _dptr(x0), C.c_int(max_outer),
-        _dptr(ev), _dptr(vec), _dptr(res), C.byref(it), C.byref(sec), C.byref(nsp))
+        _dptr(ev), _dptr(vec), _dptr(res), C.byref(it), C.byref(sec), C.byref(nsp), _dptr(ph))
     if rc != 0:
         raise RuntimeError("oracle port failed: %d" % rc)
-    return dict(eval=ev, evec=vec, res=res, iters=it.value, seconds=sec.value, spmv=nsp.value)
+    return dict(eval=ev, evec=vec, res=res, iters=it.value, seconds=sec.value, spmv=nsp.value,
+                t_init=ph[0], t_loop=ph[1], loop_iters=int(ph[2]))
 
 
 def ref_available() -> bool:

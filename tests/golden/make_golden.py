@@ -1,0 +1,72 @@
+"""Generates the golden fixtures of tests/golden/ from the REAL reference.
+
+Run in a checkout where the reference is present (oracle/build_ref.sh builds
+it into oracle/_ref/).  Each fixture stores the exact inputs (CSR arrays,
+initial block) and the reference's outputs (eigenvalues, eigenvectors for
+small cases, iteration count, convergence residuals) so the tests can check
+the oracle port and the CUDA solver without the reference on the machine.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from gcge_old_gb300 import matrices as M  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+REF_DATA = os.environ.get("GCGE_REFERENCE_DIR", "/root/reference") + "/test/data"
+
+
+def save(name, A, B, nev, x0, flags, keep_vecs=True):
+    r = O.ref_solve(A, B, nev, x0, flags)
+    d = dict(a_rowptr=A.rowptr, a_col=A.col, a_val=A.val, nev=nev, x0=x0,
+             eval=r["eval"], res=r["res"], iters=r["iters"],
+             flags=np.array([f"{k}={v}" for k, v in flags.items()]))
+    if B is not None:
+        d.update(b_rowptr=B.rowptr, b_col=B.col, b_val=B.val)
+    if keep_vecs:
+        d["evec"] = r["evec"]
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **d)
+    tr = O.true_residuals(A, B, r["eval"], r["evec"])
+    print(f"{name}: n={A.n} nev={nev} iters={r['iters']} seconds={r['seconds']:.2f} "
+          f"max true residual {tr.max():.2e}")
+
+
+def main():
+    if not O.ref_available():
+        O.build_ref()
+    # 3x3 SPD pair of the reference's test data (test/data/testA, testB)
+    A3 = M.read_csr_text(REF_DATA + "/testA")
+    B3 = M.read_csr_text(REF_DATA + "/testB")
+    save("ref_testAB_3x3", A3, B3, 1, M.initial_block(3, 1, seed=5),
+         {"-gcge_ev_tol": 1e-12, "-gcge_ev_max_it": 50})
+    # (the 81x81 FE data A_3.txt/M_3.txt is not used: M_3 is singular, and
+    # A_3's eigenvalue 1 from its 32 Dirichlet rows has multiplicity above
+    # nev + 20, where the reference itself returns no valid pair)
+    # 27-point Q1 diffusion with log-normal coefficients and Q1 mass, 10^3
+    A, B = M.diffusion27(10, seed=2)
+    save("ref_diff27_m10_nev10", A, B, 10, M.initial_block(A.n, 10, seed=4),
+         {"-gcge_ev_tol": 1e-11, "-gcge_ev_max_it": 100})
+    # 2D 5-point Laplacian, 32 x 32, B = I
+    A = M.laplace2d(32)
+    save("ref_lap2d_m32_nev10", A, None, 10, M.initial_block(A.n, 10, seed=3),
+         {"-gcge_ev_tol": 1e-12, "-gcge_ev_max_it": 100})
+    # 3D 7-point Laplacian with diagonal mass, 12^3
+    A, B = M.laplace3d_mass(12, seed=1)
+    save("ref_lap3d_m12_nev12", A, B, 12, M.initial_block(A.n, 12, seed=3),
+         {"-gcge_ev_tol": 1e-10, "-gcge_ev_max_it": 100})
+    # the CPU-runnable headline case: 128 x 128 Laplacian, nev 20, block 20
+    A = M.laplace2d(128)
+    save("ref_lap2d_m128_nev20", A, None, 20, M.initial_block(A.n, 20, seed=0),
+         {"-gcge_ev_tol": 1e-13, "-gcge_block_size": 20, "-gcge_ev_max_it": 100},
+         keep_vecs=False)
+
+
+if __name__ == "__main__":
+    main()

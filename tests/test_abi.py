@@ -1,0 +1,71 @@
+"""CPU tests of the C ABI: the library builds, loads and exports every
+function include/gcge_cuda.h declares; host-side argument checking works
+without touching a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "gcge_cuda.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(GCGE_CUDA_\w+)\s*\(", txt)))
+
+
+def test_library_builds_and_exports_header(tmp_path):
+    from gcge_old_gb300 import build as B
+    from gcge_old_gb300 import lib as L
+    path = B.build()
+    assert os.path.exists(path)
+    lib = C.CDLL(path)
+    names = header_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # the Python binding declares every exported function
+    assert set(names) <= set(L.SIGNATURES), set(names) - set(L.SIGNATURES)
+
+
+def test_error_strings_and_host_side_checks():
+    from gcge_old_gb300 import lib as L
+    lib = L.load(build_if_missing=True)
+    assert lib.GCGE_CUDA_GetErrorString(0) == b"ok"
+    assert lib.GCGE_CUDA_GetErrorString(1) == b"invalid argument"
+    # malformed CSR is rejected before any device allocation
+    rp = np.array([0, 2, 1], dtype=np.int32)
+    ci = np.array([0, 1], dtype=np.int32)
+    v = np.ones(2)
+    h = C.c_void_p()
+    p = lambda a: C.c_void_p(a.ctypes.data)
+    assert lib.GCGE_CUDA_MatCreate(C.byref(h), 2, p(rp), p(ci), p(v), 0) == 1
+    assert b"RowPtr" in lib.GCGE_CUDA_GetLastErrorMessage()
+    rp = np.array([1, 1, 2], dtype=np.int32)
+    assert lib.GCGE_CUDA_MatCreate(C.byref(h), 2, p(rp), p(ci), p(v), 0) == 1
+    assert lib.GCGE_CUDA_MatCreate(C.byref(h), 0, p(rp), p(ci), p(v), 0) == 1
+
+
+def test_solver_parameter_surface_without_gpu():
+    from gcge_old_gb300 import lib as L
+    lib = L.load(build_if_missing=True)
+    s = C.c_void_p()
+    assert lib.GCGE_CUDA_SOLVER_Create(C.byref(s)) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"block_size", 10) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamDouble(s, b"-gcge_ev_tol", 1e-10) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"no_such_flag", 1) == 1
+    args = [b"prog", b"-gcge_nev", b"7", b"-gcge_cg_rate", b"0.05", b"-unknown", b"-gcge_precision",
+            b"mixed"]
+    argv = (C.c_char_p * len(args))(*args)
+    assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, len(args), argv) == 0
+    bad = [b"-gcge_precision", b"half"]
+    argv = (C.c_char_p * 2)(*bad)
+    assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, 2, argv) == 1
+    # Solve before Setup is a state error, not a crash
+    assert lib.GCGE_CUDA_SOLVER_Solve(s) == 4
+    stream = C.c_void_p()
+    assert lib.GCGE_CUDA_SOLVER_GetStream(s, C.byref(stream)) == 4
+    assert lib.GCGE_CUDA_SOLVER_Free(C.byref(s)) == 0
+    assert not s.value
