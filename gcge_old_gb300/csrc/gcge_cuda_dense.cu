@@ -199,12 +199,15 @@ __global__ void __launch_bounds__(1024) k_jacobi(int nrows, const double* __rest
     if (tid == 0) status[0] = converged ? sweep : -1;
     return;
   }
-  // ascending order by rank (ties broken by index)
+  // ascending order by rank under a strict total order: NaN sorts as +inf
+  // and ties break by index, so rank_of is always a permutation of 0..m-1
   for (int i = tid; i < m; i += nt) {
-    const double di = (double)M[i + (size_t)i * mp];
+    double di = (double)M[i + (size_t)i * mp];
+    if (di != di) di = INFINITY;
     int rk = 0;
     for (int j = 0; j < m; j++) {
-      const double dj = (double)M[j + (size_t)j * mp];
+      double dj = (double)M[j + (size_t)j * mp];
+      if (dj != dj) dj = INFINITY;
       if (dj < di || (dj == di && j < i)) rk++;
     }
     rank_of[rk] = i;

@@ -13,8 +13,8 @@
 // slice is exactly a bf16.  The products P_ab = X_a C_b of slices are
 // integers bounded by k * 127^2; for k <= 128 a level L = a + b (up to 8
 // pairs) sums below 2^24, so one FP32 MMA accumulator per level is exact.
-// Pairs with a + b >= 10 are dropped (their total is below 2^{-55} of the
-// scale).  The levels are combined exactly in a 64-bit fixed-point integer
+// Levels L = 2..10 are kept (43 of the 64 slice products); the first dropped
+// level contributes below 6 * 127^2 * 2^{-77} < 2^{-60} of the scale.  The levels are combined exactly in a 64-bit fixed-point integer
 // T = sum_L acc_L 2^{54-7L}, and Y = T 2^{e_r + t_j - 54}.  The error is
 // about k * 2^{-55} relative to sum_i |x_ri| |c_ij|, the bound of an FP64
 // dot product.  k1 > 128 is processed in blocks of 128 that add into T.
@@ -31,7 +31,7 @@ constexpr int OZ_KC = 32;         // k columns per shared-memory stage
 constexpr int OZ_KB = 128;        // k columns per exact accumulation block
 constexpr int OZ_LD = OZ_KC + 8;  // bf16 stride of a staged row (20 words: conflict-free)
 constexpr int OZ_T = 256;         // 8 warps per CTA
-constexpr int OZ_NL = 8;          // levels L = 2..9
+constexpr int OZ_NL = 9;          // levels L = 2..10
 
 // Scaled 56-bit magnitude of x for the group exponent e (|x| < 2^e).
 __device__ __forceinline__ uint64_t oz_m56(double x, int e, bool* neg) {
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(OZ_T, 1)
             const uint32_t b1 = *reinterpret_cast<const uint32_t*>(bb + tq * 2 + 8);
 #pragma unroll
             for (int a = 0; a < OZ_S; a++)
-              if (a + b <= 7)  // slices a+1, b+1: level (a+1)+(b+1) <= 9
+              if (a + b <= OZ_NL - 1)  // slices a+1, b+1: level (a+1)+(b+1) <= 10
                 mma_bf16(acc[a + b][nt], af[a], b0, b1);
           }
         }
@@ -265,81 +265,68 @@ void launch_oz(const ColList<double>& X, int k1, int k1p, const __nv_bfloat16* C
 // power-of-two scale, the 8 x 8 slice products of a level are summed exactly
 // in FP32 by the MMAs (32 * 8 * 127^2 < 2^24), the levels are combined in a
 // 64-bit fixed-point integer and the chunk's exact value is added to an FP64
-// per-CTA partial sum.  A CTA owns a group of up to 8 x 4 output tiles
-// (128 columns of V x 32 columns of W); warp w owns m-tile w of its group.
+// per-CTA partial sum.  A CTA owns a group of GM columns of V x GN columns of
+// W; warp w owns m-tile w of its group.  A warp reads one column's 32 rows of
+// a chunk with one coalesced load (lane = row), finds the column's scale by
+// a warp max and writes the 8 slices, so each value is read from HBM once.
 constexpr int OG_R = 32;
 constexpr int OG_LD = OG_R + 8;  // 20 words per staged column: conflict-free fragments
-constexpr int OG_GM = 128, OG_GN = 32;
 
+template <int GM, int GN>
 struct OgSmem {
-  __nv_bfloat16 vs[OZ_S][OG_GM][OG_LD];  // [slice][col of V][row]
-  __nv_bfloat16 ws[OZ_S][OG_GN][OG_LD];  // [slice][col of W][row]
-  double stage[OG_GM + OG_GN][OG_R + 1];  // the chunk's doubles, [col][row] (padded)
-  int cexp[OG_GM + OG_GN];
-  double gsum[OG_GM][OG_GN];             // FP64 partial sums of this CTA
+  __nv_bfloat16 vs[OZ_S][GM][OG_LD];  // [slice][col of V][row]
+  __nv_bfloat16 ws[OZ_S][GN][OG_LD];  // [slice][col of W][row]
+  int cexp[GM + GN];
+  double gsum[GM][GN];  // FP64 partial sums of this CTA
 };
 
-__global__ void __launch_bounds__(OZ_T, 1)
+template <int GM, int GN>
+__global__ void __launch_bounds__(OZ_T, (GM <= 96 ? 2 : 1))
     k_gram_oz(ColList<double> V, int k1, ColList<double> W, int k2, int n, int groups_n,
               double* __restrict__ partial) {
+  constexpr int MT = GM / 16, NTN = GN / 8;
   extern __shared__ __align__(16) unsigned char smraw[];
-  OgSmem& sm = *reinterpret_cast<OgSmem*>(smraw);
+  OgSmem<GM, GN>& sm = *reinterpret_cast<OgSmem<GM, GN>*>(smraw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, tq = lane & 3;
   const int gi = blockIdx.y / groups_n, gj = blockIdx.y % groups_n;
-  const int i0 = gi * OG_GM, j0 = gj * OG_GN;
-  const int mi = min(OG_GM, k1 - i0), nj = min(OG_GN, k2 - j0);
-  const int ncol = mi + nj;
-  for (int e = tid; e < OG_GM * OG_GN; e += OZ_T) (&sm.gsum[0][0])[e] = 0.0;
+  const int i0 = gi * GM, j0 = gj * GN;
+  const int mi = min(GM, k1 - i0), nj = min(GN, k2 - j0);
+  for (int e = tid; e < GM * GN; e += OZ_T) (&sm.gsum[0][0])[e] = 0.0;
   const int nchunks = (n + OG_R - 1) / OG_R;
-  const int mt = warp;                         // this warp's m-tile in the group
-  const bool active = mt * 16 < mi;
+  const int mt = warp;
+  const bool active = mt < MT && mt * 16 < mi;
   const int ntiles = (nj + 7) / 8;
   for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    const int r0 = ch * OG_R;
+    const int r = ch * OG_R + lane;
     __syncthreads();
-    // stage the chunk (coalesced along rows)
-    for (int e = tid; e < OG_R * ncol; e += OZ_T) {
-      const int rr = e % OG_R, c = e / OG_R;
-      const int r = r0 + rr;
-      double v = 0.0;
-      if (r < n) v = (c < mi) ? V.p[i0 + c][r] : W.p[j0 + c - mi][r];
-      sm.stage[c][rr] = v;
-    }
-    __syncthreads();
-    for (int c = tid; c < ncol; c += OZ_T) {
-      int e = -2000;
-      for (int rr = 0; rr < OG_R; rr++) e = max(e, oz_exp(sm.stage[c][rr]));
-      sm.cexp[c] = e;
-    }
-    __syncthreads();
-    // split into slices; padding columns become zero slices
-    for (int e = tid; e < OG_R * (OG_GM + OG_GN); e += OZ_T) {
-      const int rr = e % OG_R, c = e / OG_R;
-      const bool isv = c < OG_GM;
-      const int cc = isv ? c : c - OG_GM;
-      const int sc = isv ? cc : mi + cc;  // staged column index
+    // one warp per column: load, scale by the column's chunk maximum, slice
+    for (int c = warp; c < GM + GN; c += OZ_T / 32) {
+      const bool isv = c < GM;
+      const int cc = isv ? c : c - GM;
       const bool valid = isv ? (cc < mi) : (cc < nj);
-      uint64_t m = 0;
+      double v = 0.0;
+      if (valid && r < n) v = isv ? V.p[i0 + cc][r] : W.p[j0 + cc][r];
+      int e = oz_exp(v);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+      if (lane == 0) sm.cexp[c] = e;
       bool neg = false;
-      if (valid) {
-        const int ex = sm.cexp[sc];
-        if (ex < 4096) m = oz_m56(sm.stage[sc][rr], ex, &neg);
-      }
+      const uint64_t m = (e >= 4096) ? 0 : oz_m56(v, e, &neg);
 #pragma unroll
       for (int a = 1; a <= OZ_S; a++) {
-        const __nv_bfloat16 v = oz_slice(m, a, neg);
-        if (isv) sm.vs[a - 1][cc][rr] = v;
-        else sm.ws[a - 1][cc][rr] = v;
+        const __nv_bfloat16 sv = oz_slice(m, a, neg);
+        if (isv) sm.vs[a - 1][cc][lane] = sv;
+        else sm.ws[a - 1][cc][lane] = sv;
       }
     }
     __syncthreads();
     if (active) {
-      float acc[OZ_NL][4][4];
+      float acc[OZ_NL][NTN][4];
 #pragma unroll
       for (int l = 0; l < OZ_NL; l++)
 #pragma unroll
-        for (int a = 0; a < 4; a++)
+        for (int a = 0; a < NTN; a++)
 #pragma unroll
           for (int b = 0; b < 4; b++) acc[l][a][b] = 0.f;
 #pragma unroll
@@ -357,21 +344,21 @@ __global__ void __launch_bounds__(OZ_T, 1)
 #pragma unroll
         for (int b = 0; b < OZ_S; b++) {
 #pragma unroll
-          for (int nt = 0; nt < 4; nt++) {
+          for (int nt = 0; nt < NTN; nt++) {
             if (nt < ntiles) {
               const __nv_bfloat16* bb = &sm.ws[b][nt * 8 + g][ks];
               const uint32_t b0 = *reinterpret_cast<const uint32_t*>(bb + tq * 2);
               const uint32_t b1 = *reinterpret_cast<const uint32_t*>(bb + tq * 2 + 8);
 #pragma unroll
               for (int a = 0; a < OZ_S; a++)
-                if (a + b <= 7) mma_bf16(acc[a + b][nt], af[a], b0, b1);
+                if (a + b <= OZ_NL - 1) mma_bf16(acc[a + b][nt], af[a], b0, b1);
             }
           }
         }
       }
       // exact chunk value -> FP64 partial sums
 #pragma unroll
-      for (int nt = 0; nt < 4; nt++) {
+      for (int nt = 0; nt < NTN; nt++) {
         if (nt >= ntiles) continue;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
@@ -385,7 +372,7 @@ __global__ void __launch_bounds__(OZ_T, 1)
           const int ii = mt * 16 + g + ((q >= 2) ? 8 : 0);
           const int jj = nt * 8 + tq * 2 + (q & 1);
           if (ii < mi && jj < nj) {
-            const int ea = sm.cexp[ii], eb = sm.cexp[mi + jj];
+            const int ea = sm.cexp[ii], eb = sm.cexp[GM + jj];
             double v;
             if (ea >= 4096 || eb >= 4096) v = __longlong_as_double(0x7ff8000000000000ll);
             else if (ea <= -2000 || eb <= -2000) v = 0.0;
@@ -403,6 +390,24 @@ __global__ void __launch_bounds__(OZ_T, 1)
     const int ii = e % mi, jj = e / mi;
     out[(i0 + ii) + (size_t)(j0 + jj) * k1] = sm.gsum[ii][jj];
   }
+}
+
+template <int GM, int GN>
+int launch_gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
+                   double* partial, cudaStream_t st) {
+  const int groups_m = (k1 + GM - 1) / GM, groups_n = (k2 + GN - 1) / GN;
+  const int nchunks = (n + OG_R - 1) / OG_R;
+  const int per_sm = GM <= 96 ? 2 : 1;
+  const int nblk = nchunks < 152 * per_sm ? nchunks : 152 * per_sm;
+  const size_t sm = sizeof(OgSmem<GM, GN>);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gram_oz<GM, GN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  k_gram_oz<GM, GN><<<dim3(nblk, groups_m * groups_n), OZ_T, sm, st>>>(V, k1, W, k2, n, groups_n,
+                                                                       partial);
+  return nblk;
 }
 
 }  // namespace
@@ -430,7 +435,7 @@ void lincomb_oz(const ColList<double>& X, int k1, const double* C, int ldc,
 }
 
 size_t gram_oz_partial_doubles(int k1, int k2) {
-  return (size_t)152 * k1 * k2;
+  return (size_t)304 * k1 * k2;
 }
 
 // G = V^T W (k1 x k2) into partial (gram_oz_partial_doubles) then G (ldg);
@@ -438,16 +443,9 @@ size_t gram_oz_partial_doubles(int k1, int k2) {
 void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n, double* G,
              int ldg, bool sym, double* partial, cudaStream_t st) {
   if (k1 <= 0 || k2 <= 0 || n <= 0) return;
-  const int groups_m = (k1 + OG_GM - 1) / OG_GM, groups_n = (k2 + OG_GN - 1) / OG_GN;
-  const int nchunks = (n + OG_R - 1) / OG_R;
-  const int nblk = nchunks < 152 ? nchunks : 152;
-  const size_t sm = sizeof(OgSmem);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_gram_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    attr = true;
-  }
-  k_gram_oz<<<dim3(nblk, groups_m * groups_n), OZ_T, sm, st>>>(V, k1, W, k2, n, groups_n, partial);
+  int nblk;
+  if (k1 <= 96 && k2 <= 16) nblk = launch_gram_oz<96, 16>(V, k1, W, k2, n, partial, st);
+  else nblk = launch_gram_oz<128, 32>(V, k1, W, k2, n, partial, st);
   gram_reduce_partials(k1, k2, nblk, sym, partial, G, ldg, st);
 }
 

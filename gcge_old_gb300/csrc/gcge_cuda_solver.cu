@@ -202,7 +202,9 @@ struct Para {
   double scbgs_reorth_tol = 1e-16;
   double multi_tol_for_lock = 1e-6;
   int precision = 0;  // 0: all FP64, 1: FP32 block CG
-  int gemm = 1;       // tall-skinny products: 0 FP64 FMA, 1 Ozaki on bf16 tensor cores
+  // tall-skinny products: 0 FP64 FMA, 1 Ozaki on bf16 tensor cores; 2 / 3:
+  // Ozaki only for the linear combinations / only for the Gram blocks
+  int gemm = 1;
   int print_level = 0;
 };
 
@@ -530,19 +532,59 @@ static int sync(Solver* s) {
 
 static const GcgeDevCsr* Bptr(Solver* s) { return s->B ? &s->B->m : nullptr; }
 
-// Tall-skinny Y = X C (+ beta Y) with the configured arithmetic.
+// max |a - b| and max |b| over k columns (debug comparison of two products)
+static __global__ void k_maxdiff(ColList<double> A, ColList<double> B, int k, int n,
+                                 unsigned long long* out) {
+  const int row = blockIdx.x * 256 + threadIdx.x;
+  const int c = blockIdx.y;
+  if (row >= n || c >= k) return;
+  const double d = fabs(A.p[c][row] - B.p[c][row]);
+  const double v = fabs(B.p[c][row]);
+  atomicMax(out, (unsigned long long)__double_as_longlong(d));
+  atomicMax(out + 1, (unsigned long long)__double_as_longlong(v));
+}
+
+// Tall-skinny Y = X C (+ beta Y) with the configured arithmetic.  With the
+// environment variable GCGE_CUDA_CHECK_GEMM set, every tensor-core product is
+// recomputed in FP64 and the largest difference is printed (diagnostics).
 static void lincomb(Solver* s, const ColList<double>& X, int k1, const double* C, int ldc,
                     const ColList<double>& Y, int k2, double beta) {
-  if (s->para.gemm == 1 && k1 > 0)
+  if ((s->para.gemm == 1 || s->para.gemm == 2) && k1 > 0) {
+    static const bool check = getenv("GCGE_CUDA_CHECK_GEMM") != nullptr;
+    if (check && beta == 0.0 && k2 <= (int)s->evec.size()) {
+      // FP64 result into evec-sized debug columns
+      static double* dbg = nullptr;
+      static unsigned long long* dmx = nullptr;
+      if (!dbg) {
+        cudaMalloc(&dbg, sizeof(double) * (size_t)s->ldn * GCGE_MAXCOLS);
+        cudaMalloc(&dmx, 16);
+      }
+      ColList<double> D;
+      for (int j = 0; j < k2; j++) D.p[j] = dbg + (size_t)j * s->ldn;
+      gcge::lincomb_f64(X, k1, C, ldc, D, k2, 0.0, s->n, s->st);
+      gcge::lincomb_oz(X, k1, C, ldc, Y, k2, beta, s->n, s->oz_scratch, s->st);
+      cudaMemsetAsync(dmx, 0, 16, s->st);
+      k_maxdiff<<<dim3((s->n + 255) / 256, k2), 256, 0, s->st>>>(Y, D, k2, s->n, dmx);
+      unsigned long long h[2];
+      cudaMemcpyAsync(h, dmx, 16, cudaMemcpyDeviceToHost, s->st);
+      cudaStreamSynchronize(s->st);
+      double d, v;
+      memcpy(&d, &h[0], 8);
+      memcpy(&v, &h[1], 8);
+      fprintf(stderr, "[gemm-check] iter %d k1 %d k2 %d ldc %d maxdiff %.3e maxval %.3e\n",
+              s->num_iter, k1, k2, ldc, d, v);
+      return;
+    }
     gcge::lincomb_oz(X, k1, C, ldc, Y, k2, beta, s->n, s->oz_scratch, s->st);
-  else
+  } else {
     gcge::lincomb_f64(X, k1, C, ldc, Y, k2, beta, s->n, s->st);
+  }
 }
 
 // Tall-skinny G = V^T W with the configured arithmetic.
 static void gram(Solver* s, const ColList<double>& V, int k1, const ColList<double>& W, int k2,
                  double* G, int ldg, bool sym) {
-  if (s->para.gemm == 1)
+  if (s->para.gemm == 1 || s->para.gemm == 3)
     gcge::gram_oz(V, k1, W, k2, s->n, G, ldg, sym, s->partial, s->st);
   else
     gcge::gram_f64(V, k1, W, k2, s->n, G, ldg, sym, s->partial, s->st);
