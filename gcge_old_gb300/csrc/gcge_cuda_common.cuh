@@ -64,12 +64,14 @@ void lincomb_f64(const ColList<double>& X, int k1, const double* C, int ldc,
 size_t lincomb_oz_scratch_bytes(int k1, int k2);
 void lincomb_oz(const ColList<double>& X, int k1, const double* C, int ldc,
                 const ColList<double>& Y, int k2, double beta, int n, void* scratch,
-                cudaStream_t st);
+                cudaStream_t st, bool balance = false, bool negate = false);
 // G = V^T W with FP64 accuracy on the bf16 tensor cores; partial holds
 // gram_oz_partial_doubles(k1, k2) doubles.
 size_t gram_oz_partial_doubles(int k1, int k2);
+// wdiag (optional): W's rows are scaled by wdiag[r] first (G = V^T diag(d) W,
+// the B-Gram of a diagonal B).
 void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n, double* G,
-             int ldg, bool sym, double* partial, cudaStream_t st);
+             int ldg, bool sym, double* partial, cudaStream_t st, const double* wdiag = nullptr);
 // G[i + j*ldg] = sum_b partial[b*k1*k2 + i + j*k1] (fixed order); sym mirrors
 // the upper triangle.
 void gram_reduce_partials(int k1, int k2, int nblk, bool sym, const double* partial, double* G,

@@ -74,17 +74,15 @@ __device__ inline double block_sum1024(double v, double* sh) {
 // work: global scratch of 2*mp*mp T when the matrix does not fit in shared
 // memory.  status[0] = sweeps used (or -1 if not converged).
 template <typename T>
-__global__ void __launch_bounds__(1024) k_jacobi(int nrows, const double* __restrict__ a, int lda,
-                                                 double* __restrict__ eval,
-                                                 double* __restrict__ evec, int lde, int il,
-                                                 int iu, T* __restrict__ work, int use_smem,
-                                                 int* __restrict__ status, int mode, double tol,
-                                                 int max_sweeps) {
+__global__ void __launch_bounds__(1024, 1)
+    k_jacobi(int nrows, const double* __restrict__ a, int lda, double* __restrict__ eval,
+             double* __restrict__ evec, int lde, int il, int iu, T* __restrict__ work,
+             int use_smem, int* __restrict__ status, int mode, double tol, int max_sweeps,
+             const unsigned char* __restrict__ mask, const double* __restrict__ norm_ptr) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   __shared__ double red[32];
   __shared__ T cs[128], sn[128];
   __shared__ int rank_of[256];
-  __shared__ int nrot;
   __shared__ unsigned char rot[128];
   const int m = nrows;
   const int mp = (m % 2) ? m + 1 : m;  // padded player count
@@ -106,13 +104,16 @@ __global__ void __launch_bounds__(1024) k_jacobi(int nrows, const double* __rest
     tot += v * v;
   }
   tot = block_sum1024(tot, red);
+  // pair table of the current round, rotation parameters and flags
+  __shared__ short pp_[128], qq_[128];
   int sweep = 0;
   bool converged = false;
   const int npairs = mp / 2;
+  const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
   for (; sweep < max_sweeps; sweep++) {
-    if (tid == 0) nrot = 0;
-    __syncthreads();
+    int did = 0;
     for (int r = 0; r < mp - 1; r++) {
+      // parameters of the npairs disjoint rotations of this round
       for (int k = tid; k < npairs; k += nt) {
         int p, q;
         rr_pair(mp, r, k, &p, &q);
@@ -121,62 +122,69 @@ __global__ void __launch_bounds__(1024) k_jacobi(int nrows, const double* __rest
         if (q < m) {
           const T apq = M[p + (size_t)q * mp];
           const T app = M[p + (size_t)p * mp], aqq = M[q + (size_t)q * mp];
-          if (fabs((double)apq) > 1e-300 &&
-              fabs((double)apq) > tol * sqrt(fabs((double)app) * fabs((double)aqq))) {
+          // with a mask (the refinement's clustered pairs) the other pairs
+          // rotate only if a coupling above 1e-14 ||A||_F is left
+          bool big;
+          if (!mask || mask[p + (size_t)q * m])
+            big = fabs((double)apq) > tol * sqrt(fabs((double)app) * fabs((double)aqq));
+          else
+            big = fabs((double)apq) > 1e-14 * norm_ptr[0];
+          if (fabs((double)apq) > 1e-300 && big) {
             const T theta = (aqq - app) / (T(2) * apq);
             const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
             c = T(1) / sqrt(t * t + T(1));
             s = t * c;
             doit = 1;
-            atomicAdd(&nrot, 1);
+            did = 1;
           }
         }
+        pp_[k] = (short)p;
+        qq_[k] = (short)q;
         cs[k] = c;
         sn[k] = s;
         rot[k] = doit;
       }
       __syncthreads();
-      // rows p, q of M  (M <- J^T M)
-      for (int e = tid; e < npairs * m; e += nt) {
-        const int k = e % npairs, j = e / npairs;
+      // rows p, q of M (M <- J^T M): a warp per pair, lanes along the row
+      for (int k = warp; k < npairs; k += nwarps) {
         if (!rot[k]) continue;
-        int p, q;
-        rr_pair(mp, r, k, &p, &q);
+        const int p = pp_[k], q = qq_[k];
         const T c = cs[k], s = sn[k];
-        const T mp_ = M[p + (size_t)j * mp], mq = M[q + (size_t)j * mp];
-        M[p + (size_t)j * mp] = c * mp_ - s * mq;
-        M[q + (size_t)j * mp] = s * mp_ + c * mq;
+        for (int j = lane; j < m; j += 32) {
+          const T mp_ = M[p + (size_t)j * mp], mq = M[q + (size_t)j * mp];
+          M[p + (size_t)j * mp] = c * mp_ - s * mq;
+          M[q + (size_t)j * mp] = s * mp_ + c * mq;
+        }
       }
       __syncthreads();
-      // columns p, q of M and Q  (M <- M J, Q <- Q J)
-      for (int e = tid; e < npairs * m; e += nt) {
-        const int k = e % npairs, i = e / npairs;
+      // columns p, q of M and Q (M <- M J, Q <- Q J)
+      for (int k = warp; k < npairs; k += nwarps) {
         if (!rot[k]) continue;
-        int p, q;
-        rr_pair(mp, r, k, &p, &q);
+        const int p = pp_[k], q = qq_[k];
         const T c = cs[k], s = sn[k];
-        const T mp_ = M[i + (size_t)p * mp], mq = M[i + (size_t)q * mp];
-        M[i + (size_t)p * mp] = c * mp_ - s * mq;
-        M[i + (size_t)q * mp] = s * mp_ + c * mq;
-        const T qp = Q[i + (size_t)p * mp], qq = Q[i + (size_t)q * mp];
-        Q[i + (size_t)p * mp] = c * qp - s * qq;
-        Q[i + (size_t)q * mp] = s * qp + c * qq;
-      }
-      __syncthreads();
-      for (int k = tid; k < npairs; k += nt) {
-        if (!rot[k]) continue;
-        int p, q;
-        rr_pair(mp, r, k, &p, &q);
-        M[p + (size_t)q * mp] = T(0);
-        M[q + (size_t)p * mp] = T(0);
+        T* Mp = M + (size_t)p * mp;
+        T* Mq = M + (size_t)q * mp;
+        T* Qp = Q + (size_t)p * mp;
+        T* Qq = Q + (size_t)q * mp;
+        for (int i = lane; i < m; i += 32) {
+          const T a1 = Mp[i], a2 = Mq[i];
+          Mp[i] = c * a1 - s * a2;
+          Mq[i] = s * a1 + c * a2;
+          const T q1 = Qp[i], q2 = Qq[i];
+          Qp[i] = c * q1 - s * q2;
+          Qq[i] = s * q1 + c * q2;
+        }
+        if (lane == 0) {  // the annihilated entries are exactly zero
+          Mp[q] = T(0);
+          Mq[p] = T(0);
+        }
       }
       __syncthreads();
     }
-    if (nrot == 0) {
+    if (!__syncthreads_or(did)) {
       converged = true;
       break;
     }
-    __syncthreads();
   }
   if (!converged) {
     // accept a result whose off-diagonal part is negligible anyway
@@ -217,7 +225,7 @@ __global__ void __launch_bounds__(1024) k_jacobi(int nrows, const double* __rest
   for (int kk = tid; kk < nout; kk += nt)
     eval[kk] = (double)M[rank_of[il - 1 + kk] * (size_t)(mp + 1)];
   // eigenvector columns, sign fixed so the largest-magnitude entry is positive
-  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  const int nw = nwarps;
   for (int kk = warp; kk < nout; kk += nw) {
     const int c = rank_of[il - 1 + kk];
     double best = -1.0, bv = 0.0;
@@ -406,26 +414,97 @@ size_t jacobi_smem_bytes(int nrows) {
 template <typename T>
 static void launch_jacobi(int nrows, const double* a, int lda, double* eval, double* evec, int lde,
                           int il, int iu, T* work, int* status, int mode, double tol,
-                          int max_sweeps, cudaStream_t st) {
+                          int max_sweeps, cudaStream_t st, const unsigned char* mask = nullptr,
+                          const double* norm_ptr = nullptr) {
   const int mp = (nrows % 2) ? nrows + 1 : nrows;
   const size_t sm = sizeof(T) * 2 * (size_t)mp * mp;
   const int use_smem = sm <= 200 * 1024 ? 1 : 0;
   if (use_smem) {
     cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_jacobi<T><<<1, 1024, sm, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, 1, status, mode,
-                                     tol, max_sweeps);
+                                     tol, max_sweeps, mask, norm_ptr);
   } else {
     k_jacobi<T><<<1, 1024, 0, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, 0, status, mode,
-                                    tol, max_sweeps);
+                                    tol, max_sweeps, mask, norm_ptr);
   }
 }
 
-// Newton-Schulz step Q <- 1.5 Q - 0.5 Q (Q^T Q), which squares the
-// departure from orthogonality.
-static void orth_newton_schulz(int m, double* Q, double* G, double* Qn, cudaStream_t st) {
-  dgemm_small(true, false, false, m, m, m, 1.0, Q, m, Q, m, 0.0, G, m, st);
-  cudaMemcpyAsync(Qn, Q, sizeof(double) * m * m, cudaMemcpyDeviceToDevice, st);
-  dgemm_small(false, false, false, m, m, m, -0.5, Q, m, G, m, 1.5, Qn, m, st);
+// One step of the Ogita-Aishima refinement of an approximate eigenvector
+// basis X of a symmetric A (Japan J. Indust. Appl. Math. 35 (2018)
+// 1007-1035, Algorithm 1), given S = X^T A X and R = I - X^T X:
+//   l_i = s_ii / (1 - r_ii),  delta = 2 (||S - diag(l)|| + ||A|| ||R||),
+//   E_ij = (s_ij + l_j r_ij) / (l_j - l_i)  if |l_i - l_j| > delta
+//        = r_ij / 2                          otherwise (and on the diagonal),
+// after which X <- X + X E.  Frobenius norms stand in for 2-norms (larger
+// delta: safe); ||A|| is read from device memory.  Pairs within delta are
+// "clustered": on the first step the mask records them and later steps keep
+// treating them as clustered; the final FP64 Jacobi rotates exactly those
+// pairs.  One CTA.
+__global__ void __launch_bounds__(1024) k_oa_step_dev(int m, const double* __restrict__ S,
+                                                      const double* __restrict__ R,
+                                                      const double* __restrict__ normA, int first,
+                                                      unsigned char* __restrict__ mask,
+                                                      double* __restrict__ E);
+
+__global__ void k_eye_minus(double* __restrict__ R, int m) {
+  // R <- I - R  (R holds X^T X on entry)
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * m) return;
+  const int i = e % m, j = e / m;
+  R[e] = (i == j ? 1.0 : 0.0) - R[e];
+}
+
+__global__ void __launch_bounds__(1024) k_frob_sym(int m, const double* __restrict__ a, int lda,
+                                                   double* __restrict__ out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    const int i = e % m, j = e / m;
+    const double v = (i <= j) ? a[i + (size_t)j * lda] : a[j + (size_t)i * lda];
+    s += v * v;
+  }
+  s = block_sum1024(s, red);
+  if (threadIdx.x == 0) out[0] = sqrt(s);
+}
+
+__global__ void __launch_bounds__(1024) k_oa_step_dev(int m, const double* __restrict__ S,
+                                                      const double* __restrict__ R,
+                                                      const double* __restrict__ normA, int first,
+                                                      unsigned char* __restrict__ mask,
+                                                      double* __restrict__ E) {
+  __shared__ double lam[256];
+  __shared__ double red[32];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const double nA = normA[0];
+  for (int i = tid; i < m; i += nt) lam[i] = S[i + (size_t)i * m] / (1.0 - R[i + (size_t)i * m]);
+  __syncthreads();
+  double s2 = 0.0, r2 = 0.0;
+  for (int e = tid; e < m * m; e += nt) {
+    const int i = e % m, j = e / m;
+    const double sv = S[e] - (i == j ? lam[i] : 0.0);
+    s2 += sv * sv;
+    r2 += R[e] * R[e];
+  }
+  s2 = block_sum1024(s2, red);
+  r2 = block_sum1024(r2, red);
+  const double delta = 2.0 * (sqrt(s2) + nA * sqrt(r2));
+  for (int e = tid; e < m * m; e += nt) {
+    const int i = e % m, j = e / m;
+    double v;
+    if (i == j) {
+      v = 0.5 * R[e];
+    } else {
+      bool clustered;
+      if (first) {
+        clustered = !(fabs(lam[i] - lam[j]) > delta);  // NaN -> clustered
+        mask[e] = clustered ? 1 : 0;
+      } else {
+        clustered = mask[e] != 0;
+      }
+      v = clustered ? 0.5 * R[e] : (S[e] + lam[j] * R[e]) / (lam[j] - lam[i]);
+    }
+    E[e] = v;
+  }
 }
 
 void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec, int lde, int il,
@@ -436,35 +515,45 @@ void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec,
     launch_jacobi<double>(m, a, lda, eval, evec, lde, il, iu, work, status, 0, 1e-15, 60, st);
     return;
   }
-  // 1. FP32 Jacobi: an eigenvector basis Q accurate to single precision
-  // 2. two Newton-Schulz steps make Q orthogonal to FP64 rounding
-  // 3. M1 = Q^T A Q is diagonal up to ~1e-7 ||A||; FP64 Jacobi on M1
-  //    converges in two or three sweeps
-  // 4. eigenvectors = Q * (eigenvectors of M1)
+  // 1. FP32 Jacobi: a basis X of eigenvectors to single precision
+  // 2. three Ogita-Aishima refinement steps in FP64 (matrix products only)
+  // 3. S = X^T A X is diagonal to rounding except inside clusters of close
+  //    eigenvalues; an FP64 Jacobi restricted to the clustered pairs
+  //    finishes it and sorts; eigenvectors = X * (its eigenvectors)
   const size_t mm = (size_t)m * m;
-  const int mp = m + 1;
-  double* Q = work;
-  double* G = Q + mm;
-  double* Qn = G + mm;
-  double* T1 = Qn + mm;
-  double* M1 = T1 + mm;
-  double* Z = M1 + mm;
-  void* jw = Z + mm;  // Jacobi global scratch (2 mp^2 of T)
-  launch_jacobi<float>(m, a, lda, eval, Q, m, 1, m, (float*)jw, status, 1, 1e-6, 30, st);
-  orth_newton_schulz(m, Q, G, Qn, st);
-  orth_newton_schulz(m, Qn, G, Q, st);
-  // T1 = A Q (A symmetric from its upper triangle), M1 = Q^T T1
-  dgemm_small(false, false, true, m, m, m, 1.0, a, lda, Q, m, 0.0, T1, m, st);
-  dgemm_small(true, false, false, m, m, m, 1.0, Q, m, T1, m, 0.0, M1, m, st);
-  launch_jacobi<double>(m, M1, m, eval, Z, m, il, iu, (double*)jw, status, 0, 1e-15, 60, st);
+  double* X = work;
+  double* AX = X + mm;
+  double* S = AX + mm;
+  double* R = S + mm;
+  double* E = R + mm;
+  double* Z = E + mm;
+  double* nrm = Z + mm;                                         // 8 doubles
+  unsigned char* mask = reinterpret_cast<unsigned char*>(nrm + 8);  // m*m bytes
+  void* jw = nrm + 8 + (mm + 7) / 8;                            // Jacobi scratch
+  launch_jacobi<float>(m, a, lda, eval, X, m, 1, m, (float*)jw, status, 1, 2e-7, 20, st);
+  k_frob_sym<<<1, 1024, 0, st>>>(m, a, lda, nrm);
+  double* normA_dev = nrm;
+  for (int it = 0; it < 3; it++) {
+    dgemm_small(false, false, true, m, m, m, 1.0, a, lda, X, m, 0.0, AX, m, st);
+    dgemm_small(true, false, false, m, m, m, 1.0, X, m, AX, m, 0.0, S, m, st);
+    dgemm_small(true, false, false, m, m, m, 1.0, X, m, X, m, 0.0, R, m, st);
+    k_eye_minus<<<(int)((mm + 255) / 256), 256, 0, st>>>(R, m);
+    k_oa_step_dev<<<1, 1024, 0, st>>>(m, S, R, normA_dev, it == 0 ? 1 : 0, mask, E);
+    // X <- X + X E
+    cudaMemcpyAsync(AX, X, sizeof(double) * mm, cudaMemcpyDeviceToDevice, st);
+    dgemm_small(false, false, false, m, m, m, 1.0, AX, m, E, m, 1.0, X, m, st);
+  }
+  dgemm_small(false, false, true, m, m, m, 1.0, a, lda, X, m, 0.0, AX, m, st);
+  dgemm_small(true, false, false, m, m, m, 1.0, X, m, AX, m, 0.0, S, m, st);
+  launch_jacobi<double>(m, S, m, eval, Z, m, il, iu, (double*)jw, status, 0, 1e-15, 60, st, mask,
+                        normA_dev);
   const int nout = iu - il + 1;
-  dgemm_small(false, false, false, m, nout, m, 1.0, Q, m, Z, m, 0.0, evec, lde, st);
-  (void)mp;
+  dgemm_small(false, false, false, m, nout, m, 1.0, X, m, Z, m, 0.0, evec, lde, st);
 }
 
 size_t jacobi_work_doubles(int nrows) {
   const size_t m = nrows, mp = nrows + 1;
-  return 6 * m * m + 2 * mp * mp + 16;
+  return 6 * m * m + 8 + (m * m + 7) / 8 + 2 * mp * mp + 16;
 }
 
 void sub_mgs(double* V, int ldV, int nrows, int start, int end, double tol, int* end_out,

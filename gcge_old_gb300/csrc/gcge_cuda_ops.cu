@@ -162,7 +162,7 @@ extern "C" int GCGE_CUDA_MultiVecLinearCombOzaki(double* const* x, int k1, doubl
     for (int i = 0; i < k1; i++) h[i + (size_t)j * k1] = a[i + (size_t)j * lda];
   if (cudaMemcpy(C, h.data(), sizeof(double) * cb, cudaMemcpyHostToDevice) != cudaSuccess)
     return GCGE_CUDA_ERR_CUDA;
-  gcge::lincomb_oz(mk(x, k1), k1, C, k1 > 0 ? k1 : 1, mk(y, k2), k2, beta, n, sc, 0);
+  gcge::lincomb_oz(mk(x, k1), k1, C, k1 > 0 ? k1 : 1, mk(y, k2), k2, beta, n, sc, 0, true);
   return finish();
 }
 

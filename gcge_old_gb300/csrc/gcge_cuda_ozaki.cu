@@ -60,16 +60,54 @@ __device__ __forceinline__ __nv_bfloat16 oz_slice(uint64_t m, int a, bool neg) {
   return __float2bfloat16_rn(neg ? -(float)v : (float)v);
 }
 
+// exponent of x scaled by 2^d (sentinels kept)
+__device__ __forceinline__ int oz_exp_shift(double x, int d) {
+  const int e = oz_exp(x);
+  return (e >= 4096 || e <= -2000) ? e : e + d;
+}
+
+// Column balancing of X: xe[i] = max exponent of the finite entries of
+// column i (-2000 for a zero column; consumers read that as 0).  Grid:
+// (row blocks, k1); xe must be preset to -2000.
+__global__ void k_oz_colexp(ColList<double> X, int k1, int n, int* __restrict__ xe) {
+  __shared__ int emax;
+  const int i = blockIdx.y;
+  if (threadIdx.x == 0) emax = -2000;
+  __syncthreads();
+  int e = -2000;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const int ex = oz_exp(X.p[i][r]);
+    if (ex < 4096) e = max(e, ex);  // non-finite rows are flagged by the row exponent
+  }
+  atomicMax(&emax, e);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(xe + i, emax);
+}
+
+__global__ void k_fill_int(int* __restrict__ a, int v, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) a[i] = v;
+}
+
+__device__ __forceinline__ int oz_bal(const int* xe, int i) {
+  if (!xe) return 0;
+  const int d = xe[i];
+  return d <= -2000 ? 0 : d;
+}
+
 // C (k1 x k2, ldc) -> slices Cg[s][j][i] (k2p x k1p, zero padded), texp[j].
+// With balancing, row i of C is taken as C[i][j] * 2^{xe[i]} (exactly).
 __global__ void k_oz_split_c(const double* __restrict__ C, int ldc, int k1, int k2, int k1p,
-                             int k2p, __nv_bfloat16* __restrict__ Cg, int* __restrict__ texp) {
+                             int k2p, const int* __restrict__ xe, int negate,
+                             __nv_bfloat16* __restrict__ Cg, int* __restrict__ texp) {
   __shared__ int emax;
   const int j = blockIdx.x;
   if (threadIdx.x == 0) emax = -2000;
   __syncthreads();
   int e = -2000;
   if (j < k2)
-    for (int i = threadIdx.x; i < k1; i += blockDim.x) e = max(e, oz_exp(C[i + (size_t)j * ldc]));
+    for (int i = threadIdx.x; i < k1; i += blockDim.x)
+      e = max(e, oz_exp_shift(C[i + (size_t)j * ldc], oz_bal(xe, i)));
   atomicMax(&emax, e);
   __syncthreads();
   const int t = emax;
@@ -77,7 +115,9 @@ __global__ void k_oz_split_c(const double* __restrict__ C, int ldc, int k1, int 
   for (int i = threadIdx.x; i < k1p; i += blockDim.x) {
     const double c = (j < k2 && i < k1) ? C[i + (size_t)j * ldc] : 0.0;
     bool neg = false;
-    const uint64_t m = (t >= 4096) ? 0 : oz_m56(c, t, &neg);
+    const int d = (i < k1) ? oz_bal(xe, i) : 0;
+    const uint64_t m = (t >= 4096) ? 0 : oz_m56(c, t - d, &neg);
+    if (negate) neg = !neg;
 #pragma unroll
     for (int a = 1; a <= OZ_S; a++)
       Cg[((size_t)(a - 1) * k2p + j) * k1p + i] = oz_slice(m, a, neg);
@@ -105,7 +145,7 @@ template <int WM, int WN, int NT>
 __global__ void __launch_bounds__(OZ_T, 1)
     k_lincomb_oz(ColList<double> X, int k1, int k1p, const __nv_bfloat16* __restrict__ Cg,
                  const int* __restrict__ texp, int k2, int k2p, ColList<double> Y, double beta,
-                 int n) {
+                 int n, const int* __restrict__ xe) {
   constexpr int TM = 16 * WM, TN = 8 * NT * WN;
   static_assert(WM * WN * 32 == OZ_T, "8 warps");
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -116,14 +156,27 @@ __global__ void __launch_bounds__(OZ_T, 1)
   const int r0 = blockIdx.x * TM;
   const int j0 = blockIdx.y * TN;
 
-  // row exponents (OZ_T / TM threads per row)
+  // row exponents (OZ_T / TM threads per row), loads issued in batches of 8
   {
     constexpr int PARTS = OZ_T / TM;
     const int rr = tid % TM, part = tid / TM;
     int e = -2000;
     const int r = r0 + rr;
-    if (r < n)
-      for (int i = part; i < k1; i += PARTS) e = max(e, oz_exp(X.p[i][r]));
+    if (r < n) {
+      for (int i0 = part; i0 < k1; i0 += 8 * PARTS) {
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int i = i0 + q * PARTS;
+          v[q] = (i < k1) ? __ldg(X.p[i] + r) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int i = i0 + q * PARTS;
+          if (i < k1) e = max(e, oz_exp_shift(v[q], -oz_bal(xe, i)));
+        }
+      }
+    }
     if (part == 0) sm.rexp[rr] = -2000;
     __syncthreads();
     atomicMax(&sm.rexp[rr], e);
@@ -147,16 +200,30 @@ __global__ void __launch_bounds__(OZ_T, 1)
     const int kend = min(kb + OZ_KB, k1p);
     for (int kc = kb; kc < kend; kc += OZ_KC) {
       __syncthreads();
-      // split the X chunk rows [r0, r0+TM) x cols [kc, kc+32) into slices
-      for (int e = tid; e < TM * OZ_KC; e += OZ_T) {
-        const int rr = e % TM, cc = e / TM;
-        const int r = r0 + rr, i = kc + cc;
-        const double x = (r < n && i < k1) ? X.p[i][r] : 0.0;
-        const int ex = sm.rexp[rr];
-        bool neg = false;
-        const uint64_t m = (ex >= 4096) ? 0 : oz_m56(x, ex, &neg);
+      // split the X chunk rows [r0, r0+TM) x cols [kc, kc+32) into slices;
+      // all of a thread's loads are issued before any is used
+      {
+        constexpr int PER = TM * OZ_KC / OZ_T;
+        double xv[PER];
 #pragma unroll
-        for (int a = 1; a <= OZ_S; a++) sm.xs[a - 1][rr][cc] = oz_slice(m, a, neg);
+        for (int q = 0; q < PER; q++) {
+          const int e = tid + q * OZ_T;
+          const int rr = e % TM, cc = e / TM;
+          const int r = r0 + rr, i = kc + cc;
+          xv[q] = (r < n && i < k1) ? __ldg(X.p[i] + r) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+          const int e = tid + q * OZ_T;
+          const int rr = e % TM, cc = e / TM;
+          const int i = kc + cc;
+          const int ex = sm.rexp[rr];
+          bool neg = false;
+          const int d = (i < k1) ? oz_bal(xe, i) : 0;  // column i is taken as X * 2^{-d}
+          const uint64_t m = (ex >= 4096) ? 0 : oz_m56(xv[q], ex + d, &neg);
+#pragma unroll
+          for (int a = 1; a <= OZ_S; a++) sm.xs[a - 1][rr][cc] = oz_slice(m, a, neg);
+        }
       }
       // stage the C slices [slice][j0..j0+TN)[kc..kc+32) (16-byte copies)
       for (int e = tid; e < OZ_S * TN * (OZ_KC / 8); e += OZ_T) {
@@ -245,7 +312,7 @@ __global__ void __launch_bounds__(OZ_T, 1)
 template <int WM, int WN, int NT>
 void launch_oz(const ColList<double>& X, int k1, int k1p, const __nv_bfloat16* Cg,
                const int* texp, const ColList<double>& Y, int k2, int k2p, double beta, int n,
-               cudaStream_t st) {
+               const int* xe, cudaStream_t st) {
   constexpr int TM = 16 * WM, TN = 8 * NT * WN;
   const size_t sm = sizeof(OzSmem<TM, TN>) > (size_t)TN * TM * 8 ? sizeof(OzSmem<TM, TN>)
                                                                   : (size_t)TN * TM * 8;
@@ -256,7 +323,7 @@ void launch_oz(const ColList<double>& X, int k1, int k1p, const __nv_bfloat16* C
     attr = true;
   }
   dim3 grid((n + TM - 1) / TM, (k2 + TN - 1) / TN);
-  k_lincomb_oz<WM, WN, NT><<<grid, OZ_T, sm, st>>>(X, k1, k1p, Cg, texp, k2, k2p, Y, beta, n);
+  k_lincomb_oz<WM, WN, NT><<<grid, OZ_T, sm, st>>>(X, k1, k1p, Cg, texp, k2, k2p, Y, beta, n, xe);
 }
 
 // ---------------------------------------------------------------- Gram
@@ -283,7 +350,7 @@ struct OgSmem {
 template <int GM, int GN>
 __global__ void __launch_bounds__(OZ_T, (GM <= 96 ? 2 : 1))
     k_gram_oz(ColList<double> V, int k1, ColList<double> W, int k2, int n, int groups_n,
-              double* __restrict__ partial) {
+              const double* __restrict__ wdiag, double* __restrict__ partial) {
   constexpr int MT = GM / 16, NTN = GN / 8;
   extern __shared__ __align__(16) unsigned char smraw[];
   OgSmem<GM, GN>& sm = *reinterpret_cast<OgSmem<GM, GN>*>(smraw);
@@ -300,13 +367,30 @@ __global__ void __launch_bounds__(OZ_T, (GM <= 96 ? 2 : 1))
   for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
     const int r = ch * OG_R + lane;
     __syncthreads();
-    // one warp per column: load, scale by the column's chunk maximum, slice
-    for (int c = warp; c < GM + GN; c += OZ_T / 32) {
+    // one warp per column (lane = row): all of the warp's loads are issued
+    // first, then each column is scaled by its chunk maximum and sliced
+    constexpr int CPW = (GM + GN + 7) / 8;  // columns per warp
+    double cv[CPW];
+#pragma unroll
+    for (int q = 0; q < CPW; q++) {
+      const int c = warp + 8 * q;
       const bool isv = c < GM;
       const int cc = isv ? c : c - GM;
-      const bool valid = isv ? (cc < mi) : (cc < nj);
+      const bool valid = c < GM + GN && (isv ? (cc < mi) : (cc < nj));
       double v = 0.0;
-      if (valid && r < n) v = isv ? V.p[i0 + cc][r] : W.p[j0 + cc][r];
+      if (valid && r < n) {
+        if (isv) v = __ldg(V.p[i0 + cc] + r);
+        else v = wdiag ? __ldg(wdiag + r) * __ldg(W.p[j0 + cc] + r) : __ldg(W.p[j0 + cc] + r);
+      }
+      cv[q] = v;
+    }
+#pragma unroll
+    for (int q = 0; q < CPW; q++) {
+      const int c = warp + 8 * q;
+      if (c >= GM + GN) break;
+      const bool isv = c < GM;
+      const int cc = isv ? c : c - GM;
+      const double v = cv[q];
       int e = oz_exp(v);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
@@ -394,7 +478,7 @@ __global__ void __launch_bounds__(OZ_T, (GM <= 96 ? 2 : 1))
 
 template <int GM, int GN>
 int launch_gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
-                   double* partial, cudaStream_t st) {
+                   const double* wdiag, double* partial, cudaStream_t st) {
   const int groups_m = (k1 + GM - 1) / GM, groups_n = (k2 + GN - 1) / GN;
   const int nchunks = (n + OG_R - 1) / OG_R;
   const int per_sm = GM <= 96 ? 2 : 1;
@@ -406,7 +490,7 @@ int launch_gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, i
     attr = true;
   }
   k_gram_oz<GM, GN><<<dim3(nblk, groups_m * groups_n), OZ_T, sm, st>>>(V, k1, W, k2, n, groups_n,
-                                                                       partial);
+                                                                       wdiag, partial);
   return nblk;
 }
 
@@ -415,23 +499,33 @@ int launch_gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, i
 size_t lincomb_oz_scratch_bytes(int k1, int k2) {
   const int k1p = (k1 + OZ_KC - 1) / OZ_KC * OZ_KC;
   const int k2p = (k2 + 63) / 64 * 64;
-  return sizeof(__nv_bfloat16) * (size_t)OZ_S * k1p * k2p + sizeof(int) * (size_t)k2p + 256;
+  return sizeof(__nv_bfloat16) * (size_t)OZ_S * k1p * k2p + sizeof(int) * (size_t)(k2p + k1p) +
+         256;
 }
 
 // Y_j = beta Y_j + sum_i X_i C[i + j*ldc], FP64 accuracy on bf16 tensor cores.
-// scratch: lincomb_oz_scratch_bytes(k1, k2) bytes, 16-byte aligned.
+// scratch: lincomb_oz_scratch_bytes(k1, k2) bytes, 16-byte aligned.  balance:
+// scale the columns of X by powers of two (and the rows of C inversely)
+// first, for blocks whose columns differ widely in magnitude (the product is
+// unchanged: the scaling is exact).
 void lincomb_oz(const ColList<double>& X, int k1, const double* C, int ldc,
                 const ColList<double>& Y, int k2, double beta, int n, void* scratch,
-                cudaStream_t st) {
+                cudaStream_t st, bool balance, bool negate) {
   if (k2 <= 0 || n <= 0) return;
   const int k1p = (k1 + OZ_KC - 1) / OZ_KC * OZ_KC;
   const int k2p = (k2 + 63) / 64 * 64;  // C slices padded to the widest CTA tile
   __nv_bfloat16* Cg = reinterpret_cast<__nv_bfloat16*>(scratch);
   int* texp = reinterpret_cast<int*>(Cg + (size_t)OZ_S * k1p * k2p);
-  k_oz_split_c<<<k2p, 128, 0, st>>>(C, ldc, k1, k2, k1p, k2p, Cg, texp);
-  if (k2 <= 16) launch_oz<8, 1, 2>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, st);
-  else if (k2 <= 32) launch_oz<8, 1, 4>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, st);
-  else launch_oz<4, 2, 4>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, st);
+  int* xe = balance ? texp + k2p : nullptr;
+  if (balance) {
+    k_fill_int<<<(k1 + 127) / 128, 128, 0, st>>>(xe, -2000, k1);
+    const int nb = (n + 255) / 256 < 64 ? (n + 255) / 256 : 64;
+    k_oz_colexp<<<dim3(nb, k1), 256, 0, st>>>(X, k1, n, xe);
+  }
+  k_oz_split_c<<<k2p, 128, 0, st>>>(C, ldc, k1, k2, k1p, k2p, xe, negate ? 1 : 0, Cg, texp);
+  if (k2 <= 16) launch_oz<8, 1, 2>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, xe, st);
+  else if (k2 <= 32) launch_oz<8, 1, 4>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, xe, st);
+  else launch_oz<4, 2, 4>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, xe, st);
 }
 
 size_t gram_oz_partial_doubles(int k1, int k2) {
@@ -441,11 +535,11 @@ size_t gram_oz_partial_doubles(int k1, int k2) {
 // G = V^T W (k1 x k2) into partial (gram_oz_partial_doubles) then G (ldg);
 // sym: only the upper triangle is kept and mirrored.
 void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n, double* G,
-             int ldg, bool sym, double* partial, cudaStream_t st) {
+             int ldg, bool sym, double* partial, cudaStream_t st, const double* wdiag) {
   if (k1 <= 0 || k2 <= 0 || n <= 0) return;
   int nblk;
-  if (k1 <= 96 && k2 <= 16) nblk = launch_gram_oz<96, 16>(V, k1, W, k2, n, partial, st);
-  else nblk = launch_gram_oz<128, 32>(V, k1, W, k2, n, partial, st);
+  if (k1 <= 96 && k2 <= 16) nblk = launch_gram_oz<96, 16>(V, k1, W, k2, n, wdiag, partial, st);
+  else nblk = launch_gram_oz<128, 32>(V, k1, W, k2, n, wdiag, partial, st);
   gram_reduce_partials(k1, k2, nblk, sym, partial, G, ldg, st);
 }
 

@@ -548,7 +548,7 @@ static __global__ void k_maxdiff(ColList<double> A, ColList<double> B, int k, in
 // environment variable GCGE_CUDA_CHECK_GEMM set, every tensor-core product is
 // recomputed in FP64 and the largest difference is printed (diagnostics).
 static void lincomb(Solver* s, const ColList<double>& X, int k1, const double* C, int ldc,
-                    const ColList<double>& Y, int k2, double beta) {
+                    const ColList<double>& Y, int k2, double beta, bool balance = false) {
   if ((s->para.gemm == 1 || s->para.gemm == 2) && k1 > 0) {
     static const bool check = getenv("GCGE_CUDA_CHECK_GEMM") != nullptr;
     if (check && beta == 0.0 && k2 <= (int)s->evec.size()) {
@@ -562,7 +562,7 @@ static void lincomb(Solver* s, const ColList<double>& X, int k1, const double* C
       ColList<double> D;
       for (int j = 0; j < k2; j++) D.p[j] = dbg + (size_t)j * s->ldn;
       gcge::lincomb_f64(X, k1, C, ldc, D, k2, 0.0, s->n, s->st);
-      gcge::lincomb_oz(X, k1, C, ldc, Y, k2, beta, s->n, s->oz_scratch, s->st);
+      gcge::lincomb_oz(X, k1, C, ldc, Y, k2, beta, s->n, s->oz_scratch, s->st, balance);
       cudaMemsetAsync(dmx, 0, 16, s->st);
       k_maxdiff<<<dim3((s->n + 255) / 256, k2), 256, 0, s->st>>>(Y, D, k2, s->n, dmx);
       unsigned long long h[2];
@@ -575,7 +575,7 @@ static void lincomb(Solver* s, const ColList<double>& X, int k1, const double* C
               s->num_iter, k1, k2, ldc, d, v);
       return;
     }
-    gcge::lincomb_oz(X, k1, C, ldc, Y, k2, beta, s->n, s->oz_scratch, s->st);
+    gcge::lincomb_oz(X, k1, C, ldc, Y, k2, beta, s->n, s->oz_scratch, s->st, balance);
   } else {
     gcge::lincomb_f64(X, k1, C, ldc, Y, k2, beta, s->n, s->st);
   }
@@ -641,7 +641,9 @@ static int cholqr2(Solver* s, std::vector<double*>& V, int start, int* end,
     ColList<double> Wk;
     for (int j = 0; j < m; j++) Wk.p[j] = V[start + h[j]];
     ColList<double> out = cols(T, 0, m);
-    KL(lincomb(s, Wk, m, s->sub_tmp, k, out, m, 0.0));
+    // the columns of W can differ by orders of magnitude (R^{-1} undoes it):
+    // balance them before the fixed-point splitting
+    KL(lincomb(s, Wk, m, s->sub_tmp, k, out, m, 0.0, true));
     // W <- V_tmp[0:m]; the kept old W buffers become V_tmp[0:m] and the
     // dropped ones are parked beyond the new end, so the pool stays a
     // permutation of the same buffers
@@ -662,8 +664,13 @@ static int cholqr2(Solver* s, std::vector<double*>& V, int start, int* end,
 // GCGE_StableMultiOrthonormalization (src/gcge_orthogonal.c:1909-2019):
 // block CGS of V[start:*end] against V[0:start] with re-orthogonalisation
 // until ||V1^T B V2||_F <= scbgs_reorth_tol, then self-orthonormalisation.
+// On the tensor-core path a diagonal B is folded into the Gram and the update
+// W <- W - V1 G is one product with beta = 1.
 static int w_orth(Solver* s, int start, int* end) {
   const Para& p = s->para;
+  const bool oz = (p.gemm == 1 || p.gemm == 3);
+  const bool ozl = (p.gemm == 1 || p.gemm == 2);
+  const double* bdiag = s->B ? s->B->m.diag : nullptr;
   if (start > 0) {
     double vi = 1.0;
     int it = 0;
@@ -674,10 +681,21 @@ static int w_orth(Solver* s, int start, int* end) {
       ColList<double> W = cols(s->V, start, *end);
       ColList<double> T = cols(s->V_tmp, 0, l2);
       ColList<double> V1 = cols(s->V, 0, start);
-      KL(gcge::apply_b_f64(Bptr(s), W, T, l2, s->n, s->st));
-      KL(gram(s, V1, start, T, l2, s->sub_tmp2, start, false));
-      KL(lincomb(s, V1, start, s->sub_tmp2, start, T, l2, 0.0));
-      KL(gcge::axpby_f64(-1.0, T, 1.0, W, l2, s->n, s->st));
+      if (oz && (bdiag || !s->B)) {
+        KL(gcge::gram_oz(V1, start, W, l2, s->n, s->sub_tmp2, start, false, s->partial, s->st,
+                         bdiag));
+      } else {
+        KL(gcge::apply_b_f64(Bptr(s), W, T, l2, s->n, s->st));
+        KL(gram(s, V1, start, T, l2, s->sub_tmp2, start, false));
+      }
+      if (ozl) {
+        // W <- W - V1 G
+        KL(gcge::lincomb_oz(V1, start, s->sub_tmp2, start, W, l2, 1.0, s->n, s->oz_scratch, s->st,
+                            false, true));
+      } else {
+        KL(lincomb(s, V1, start, s->sub_tmp2, start, T, l2, 0.0));
+        KL(gcge::axpby_f64(-1.0, T, 1.0, W, l2, s->n, s->st));
+      }
       KL((k_frob<<<1, 256, 0, s->st>>>(s->sub_tmp2, start, l2, s->d_small)));
       double h = 0.0;
       CU(cudaMemcpyAsync(&h, s->d_small, sizeof(double), cudaMemcpyDeviceToHost, s->st));
@@ -691,17 +709,24 @@ static int w_orth(Solver* s, int start, int* end) {
 
 // GCGE_ComputeSubspaceMatrixVTAW (src/gcge_rayleighritz.c:40-90); A W goes
 // to evec[0:w_length] as scratch, as in the reference.
+static __global__ void k_mirror_upper(double* __restrict__ G, int ld, int k) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= k * k) return;
+  const int i = e % k, j = e / k;
+  if (i > j) G[i + (size_t)j * ld] = G[j + (size_t)i * ld];
+}
+
 static int vtaw(Solver* s, int start_W, int start_V, int end_V, double* smat) {
   const int wl = end_V - start_W, xpl = end_V - wl;
   ColList<double> W = cols(s->V, start_W, end_V);
   ColList<double> AW = cols(s->evec, 0, wl);
   KL(gcge::spmm_f64(s->A->m, W, AW, wl, s->st));
   CU(cudaMemsetAsync(smat, 0, sizeof(double) * (size_t)end_V * wl, s->st));
-  if (xpl - start_V > 0) {
-    ColList<double> VX = cols(s->V, start_V, xpl);
-    KL(gram(s, VX, xpl - start_V, AW, wl, smat + start_V, end_V, false));
-  }
-  KL(gram(s, W, wl, AW, wl, smat + xpl, end_V, true));
+  // one Gram [V[start_V:xpl], W]^T (A W), then the W^T A W block is made
+  // symmetric from its upper triangle (the "sym" product of the reference)
+  ColList<double> VV = cols(s->V, start_V, end_V);
+  KL(gram(s, VV, end_V - start_V, AW, wl, smat + start_V, end_V, false));
+  KL((k_mirror_upper<<<(wl * wl + 127) / 128, 128, 0, s->st>>>(smat + xpl, end_V, wl)));
   return GCGE_CUDA_OK;
 }
 

@@ -138,7 +138,8 @@ int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int
  * tensor cores (error-free splitting into 8 slices of 7 bits, exact FP32
  * level sums, 64-bit fixed-point combination); the solver's default for
  * its X, P and W updates on GB300, where FP64 FMA is ~600x slower than
- * bf16 MMA. */
+ * bf16 MMA.  The columns of x are balanced by powers of two first, so
+ * columns of very different magnitude keep their accuracy. */
 int GCGE_CUDA_MultiVecLinearCombOzaki(double* const* x, int k1, double* const* y, int k2, int n,
                                       const double* a, int lda, double beta);
 /* y[j] = alpha x[j] + beta y[j] (MultiVecAxpby, src/gcge_ops.h:98-99) */

@@ -70,3 +70,21 @@ def main():
 
 if __name__ == "__main__":
     main()
+
+
+def make_cfg2_summary(out_path=os.path.join(OUT, "cfg2_reference_summary.json")):
+    """Full-size headline workload (about 40 minutes on one core): writes the
+    reference's eigenvalues, criterion values, iteration count and time."""
+    import json
+    import platform
+    A, B = M.laplace3d_mass(128, seed=0)
+    x0 = M.initial_block(A.n, 50, seed=0)
+    flags = {"-gcge_ev_tol": 1e-10, "-gcge_ev_max_it": 1000}
+    r = O.ref_solve(A, B, 50, x0, flags)
+    tr = O.true_residuals(A, B, r["eval"], r["evec"])
+    json.dump({"workload": "laplace3d_7pt_128^3_diagmass_nev50_tol1e-10 (seed 0 matrix, seed 0 initial block)",
+               "generator": "gcge_old_gb300.matrices.laplace3d_mass(128, seed=0), initial_block(n, 50, seed=0)",
+               "flags": dict(flags, **{"-gcge_num_init_evec": 50}), "iters": r["iters"],
+               "seconds": r["seconds"], "host": "1 core, %s" % platform.machine(),
+               "max_true_residual": float(tr.max()), "eval": [float(x) for x in r["eval"]],
+               "res": [float(x) for x in r["res"]]}, open(out_path, "w"), indent=1)

@@ -135,3 +135,23 @@ def test_solver_nonfinite_input_returns(cuda_lib):
         assert st["num_iter"] <= 5
     except Exception as e:  # an error status is an acceptable outcome
         assert "Solve" in str(e)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solver_headline_workload_matches_reference(cuda_lib, precision):
+    """The full-size workload (128^3 7-point Laplacian with diagonal mass,
+    nev 50, 1e-10): eigenvalues against the reference's own run
+    (tests/golden/cfg2_reference_summary.json) to 1e-10 relative, every pair
+    at relative residual <= 1e-10 (FP64 post-check), B-orthonormal vectors."""
+    import json
+    import os
+    from conftest import GOLDEN
+    ref = json.load(open(os.path.join(GOLDEN, "cfg2_reference_summary.json")))
+    A, B = M.laplace3d_mass(128, seed=0)
+    x0 = M.initial_block(A.n, 50, seed=0)
+    ev, vec, st = S.solve(A, B, 50, x0, ev_tol=1e-10, ev_max_it=1000, precision=precision)
+    rel = np.abs(ev - np.array(ref["eval"])) / np.abs(np.array(ref["eval"]))
+    assert rel.max() < EV_RTOL, rel.max()
+    assert O.true_residuals(A, B, ev, vec).max() <= 1e-10
+    assert b_orthonormality(B, vec) < 1e-9
+    assert abs(st["num_iter"] - ref["iters"]) <= 5
