@@ -79,6 +79,10 @@ extern "C" const char* GCGE_CUDA_GetErrorString(int code) {
 }
 extern "C" const char* GCGE_CUDA_GetLastErrorMessage(void) { return g_errmsg; }
 
+// Records a message for GCGE_CUDA_GetLastErrorMessage from the library's
+// other translation units; returns code.
+int gcge_record_error(int code, const char* msg) { return set_err(code, "%s", msg); }
+
 // ------------------------------------------------------------------ matrices
 
 // Rejects malformed CSR input before any kernel reads it: row pointers must

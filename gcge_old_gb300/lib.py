@@ -73,6 +73,8 @@ SIGNATURES = {
                                               C.c_int, C.c_int]),
     "GCGE_CUDA_MultiVecInnerProdOzaki": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,
                                                    C.c_void_p, C.c_int, C.c_int]),
+    "GCGE_CUDA_MultiVecInnerProdNoAlloc": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,
+                                                     C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MultiVecLinearComb": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int, C.c_void_p,
                                                C.c_int, C.c_double]),
     "GCGE_CUDA_MultiVecLinearCombOzaki": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,

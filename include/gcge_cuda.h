@@ -130,6 +130,21 @@ int GCGE_CUDA_MultiVecInnerProd(double* const* V, int k1, double* const* W, int 
  * (per-32-row column scaling, 8 slices of 7 bits, exact level sums). */
 int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W, int k2, int n,
                                      double* a, int lda, int sym);
+/* Allocation-free FP64 inner products (no counterpart in the reference):
+ * the same a[i + j*lda] = V[i] . W[j] as GCGE_CUDA_MultiVecInnerProd, for
+ * callers that must not allocate device memory (a fixed memory budget owned
+ * by the host application, or loops where an allocation could stall or fail
+ * mid-solve).  It calls no cudaMalloc/cudaFree: its reduction scratch is a
+ * fixed device array of GCGE_CUDA_NOALLOC_MAX_OUTPUTS x 304 doubles
+ * (9.5 MiB), so k1 * k2 above GCGE_CUDA_NOALLOC_MAX_OUTPUTS is rejected with
+ * GCGE_CUDA_ERR_ARG.  `a` is a DEVICE array; the call is asynchronous on the
+ * given cudaStream_t (NULL = legacy default stream).  The first call on each
+ * device looks up the scratch array's address; make that first call before
+ * any stream capture begins.  All calls share the one scratch array (each
+ * overwrites what it reads), so calls that overlap on the GPU race. */
+#define GCGE_CUDA_NOALLOC_MAX_OUTPUTS 4096
+int GCGE_CUDA_MultiVecInnerProdNoAlloc(double* const* V, int k1, double* const* W, int k2, int n,
+                                       double* a, int lda, int sym, void* stream);
 /* y[j] = sum_i x[i] a[i + j*lda] + beta y[j], a a HOST array
  * (MultiVecLinearComb, src/gcge_ops.h:109-111). */
 int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int k2, int n,
