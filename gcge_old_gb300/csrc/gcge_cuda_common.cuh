@@ -59,9 +59,13 @@ void gram_f64(const ColList<double>& V, int k1, const ColList<double>& W, int k2
 // Y_j = beta*Y_j + sum_i X_i C[i + j*ldc]; Y must not alias X.
 void lincomb_f64(const ColList<double>& X, int k1, const double* C, int ldc,
                  const ColList<double>& Y, int k2, double beta, int n, cudaStream_t st);
-// The same product with FP64 accuracy on the bf16 tensor cores (Ozaki
-// scheme, gcge_cuda_ozaki.cu); scratch of lincomb_oz_scratch_bytes(k1, k2).
+// The same product with FP64 accuracy on the tcgen05 bf16 tensor cores
+// (error-free digit splitting, gcge_cuda_ozaki.cu); scratch of
+// lincomb_oz_scratch_bytes(k1, k2).
 size_t lincomb_oz_scratch_bytes(int k1, int k2);
+// 1 when a tensor-core kernel gave up waiting on its MMAs (its outputs were
+// set to NaN); reset clears the flag.  -1 when the flag cannot be read.
+int oz_tc_status(bool reset);
 void lincomb_oz(const ColList<double>& X, int k1, const double* C, int ldc,
                 const ColList<double>& Y, int k2, double beta, int n, void* scratch,
                 cudaStream_t st, bool balance = false, bool negate = false);

@@ -22,14 +22,12 @@
 #include <stdint.h>
 
 #include "gcge_cuda_common.cuh"
+#include "gcge_cuda_tc.cuh"
 
 namespace gcge {
 namespace {
 
 constexpr int OZ_S = 8;           // slices per value
-constexpr int OZ_KC = 32;         // k columns per shared-memory stage
-constexpr int OZ_KB = 128;        // k columns per exact accumulation block
-constexpr int OZ_LD = OZ_KC + 8;  // bf16 stride of a staged row (20 words: conflict-free)
 constexpr int OZ_T = 256;         // 8 warps per CTA
 constexpr int OZ_NL = 9;          // levels L = 2..10
 
@@ -95,11 +93,117 @@ __device__ __forceinline__ int oz_bal(const int* xe, int i) {
   return d <= -2000 ? 0 : d;
 }
 
-// C (k1 x k2, ldc) -> slices Cg[s][j][i] (k2p x k1p, zero padded), texp[j].
-// With balancing, row i of C is taken as C[i][j] * 2^{xe[i]} (exactly).
-__global__ void k_oz_split_c(const double* __restrict__ C, int ldc, int k1, int k2, int k1p,
-                             int k2p, const int* __restrict__ xe, int negate,
-                             __nv_bfloat16* __restrict__ Cg, int* __restrict__ texp) {
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ---------------------------------------------------------------- tcgen05 linear combination
+// Y = X C on the 5th-generation tensor cores.  Digits: every value, scaled by
+// its group's power of two into (-1, 1), is cut into D8_S = 7 balanced
+// base-256 digits (m = trunc(x 2^{55-E}) = sum_a d_a 256^{7-a}, the top digit
+// in [-128, 128], the others in [-128, 127]); each digit is exactly a bf16.
+// A product of two digits is an integer of magnitude <= 2^14; a level
+// L = a + b holds at most 7 of them, so a level summed over K <= 128 stays
+// below 7 * 2^21 < 2^24 and its FP32 tensor-memory accumulator is exact.
+// Levels L = 2..9 (34 digit products) are kept; the first dropped level is
+// below 5 * 2^14 * 2^{2-80} < 2^{-61} of the scale, the digit truncation
+// 2^{-55}.  Levels combine in a 64-bit integer T = sum_L acc_L 2^{57-8L}
+// (|T| < 2^62; levels 8 and 9 rounded to the integer unit), and
+// y = T 2^{e_r + t_j - 55}.
+//
+// One CTA: 128 rows (MMA M, TMEM lane = row) x up to 64 output columns (MMA
+// N).  Per k step of 16: all 256 threads slice their 8 values into shared
+// memory (K-major core-matrix layout, no swizzle), one thread issues the 34
+// MMAs (kind::f16, bf16 x bf16 -> FP32) into the 8 level accumulators in
+// tensor memory and commits them to the stage's mbarrier; stages rotate
+// through TC_STAGES buffers.  The epilogue reads the levels with
+// tcgen05.ld, combines them in registers and writes Y column-coalesced.
+constexpr int D8_S = 7;
+constexpr int D8_NL = 8;
+constexpr int TC_M = 128;
+constexpr int TC_KS = 16;
+constexpr int TC_NMAX = 64;
+constexpr int TC_STAGES = 3;
+constexpr int TC_T = 256;
+constexpr int TC_ABYTES = D8_S * TC_M * TC_KS * 2;  // 28672
+constexpr int TC_WAIT = 1 << 26;                    // mbarrier polls before giving up
+
+__device__ int g_oz_tc_status = 0;  // 1: an mbarrier wait gave up (outputs set to NaN)
+
+__device__ __forceinline__ uint32_t d8_pack(float lo, float hi) {
+  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+// The 7 digits of x / 2^E (|x| < 2^E) as exact FP32 values, most significant
+// first.  Zero, subnormal and non-finite x give zero digits.
+__device__ __forceinline__ void d8_digits(double x, int E, float* f) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  long long m = 0;
+  if (ex != 0 && ex != 0x7FF) {
+    const unsigned long long mant = ((unsigned long long)b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1020 - E;  // <= 2 because |x| < 2^E
+    const unsigned long long mm =
+        sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
+    m = b < 0 ? -(long long)mm : (long long)mm;
+  }
+  const long long u = m + 0x808080808080ll;  // bytes 0..5 of u are the low digits + 128
+  const int hi = (int)(u >> 32);
+  const unsigned lo = (unsigned)u;
+  f[0] = __int_as_float(0x4B000000 + (hi >> 16) + 256) - 8388864.0f;
+  f[1] = __int_as_float(__byte_perm((unsigned)hi, 0x4B000000u, 0x7651)) - 8388736.0f;
+  f[2] = __int_as_float(__byte_perm((unsigned)hi, 0x4B000000u, 0x7650)) - 8388736.0f;
+  f[3] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7653)) - 8388736.0f;
+  f[4] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7652)) - 8388736.0f;
+  f[5] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7651)) - 8388736.0f;
+  f[6] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7650)) - 8388736.0f;
+}
+
+// T 2^s rounded to the nearest double (ties to even), by integer operations.
+__device__ __forceinline__ double d8_to_double(long long T, int s) {
+  if (T == 0) return 0.0;
+  const unsigned long long sgn = T < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long mag = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
+  const int lz = __clzll((long long)mag);
+  const unsigned long long nrm = mag << lz;  // top bit at 63
+  unsigned long long mant = nrm >> 11;       // 53 bits
+  const unsigned long long rem = nrm & 0x7FFull;
+  int e2 = 63 - lz;  // value = nrm 2^{e2 - 63} 2^s
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) {
+    mant += 1ull;
+    if (mant == (1ull << 53)) {
+      mant >>= 1;
+      e2 += 1;
+    }
+  }
+  const int be = e2 + s + 1023;
+  if (be >= 1 && be <= 2046)
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) |
+                                            (mant & ((1ull << 52) - 1))));
+  return scalbn(T < 0 ? -(double)mag : (double)mag, s);  // out of the normal range
+}
+
+__host__ __device__ __forceinline__ int tc_round16(int v) { return (v + 15) / 16 * 16; }
+
+// width (MMA N) of output-column tile nt
+__host__ __device__ __forceinline__ int tc_tile_n(int k2, int nt) {
+  const int rem = k2 - nt * TC_NMAX;
+  return rem >= TC_NMAX ? TC_NMAX : tc_round16(rem);
+}
+
+// C (k1 x k2, ldc; k1 <= 128) -> B operand images Cg and column exponents
+// texp.  Layout: tile nt (TC_NMAX columns) at byte nt*TC_NMAX*k1p*14, inside it
+// stage ks (16 values of i) and digit a at (ks*7 + a) * N*32, then the
+// K-major core-matrix image of N columns x 16 values.  Grid: one CTA per
+// padded column.  Row i of C is taken as C[i][j] 2^{xe[i]} (balancing), and
+// negated when negate is set.
+__global__ void k_d8_split_c(const double* __restrict__ C, int ldc, int k1, int k2, int k1p,
+                             const int* __restrict__ xe, int negate, uint8_t* __restrict__ Cg,
+                             int* __restrict__ texp) {
   __shared__ int emax;
   const int j = blockIdx.x;
   if (threadIdx.x == 0) emax = -2000;
@@ -111,221 +215,222 @@ __global__ void k_oz_split_c(const double* __restrict__ C, int ldc, int k1, int 
   atomicMax(&emax, e);
   __syncthreads();
   const int t = emax;
-  if (threadIdx.x == 0) texp[j] = t;
+  if (threadIdx.x == 0 && j < k2) texp[j] = t;
+  const int nt = j / TC_NMAX, jj = j % TC_NMAX;
+  const int N = tc_tile_n(k2, nt);
+  uint8_t* tile = Cg + (size_t)nt * TC_NMAX * k1p * (D8_S * 2);
   for (int i = threadIdx.x; i < k1p; i += blockDim.x) {
-    const double c = (j < k2 && i < k1) ? C[i + (size_t)j * ldc] : 0.0;
-    bool neg = false;
+    double c = (j < k2 && i < k1 && t < 4096) ? C[i + (size_t)j * ldc] : 0.0;
+    if (negate) c = -c;
     const int d = (i < k1) ? oz_bal(xe, i) : 0;
-    const uint64_t m = (t >= 4096) ? 0 : oz_m56(c, t - d, &neg);
-    if (negate) neg = !neg;
+    float f[D8_S];
+    d8_digits(c, t - d, f);
+    const int ks = i / TC_KS, kk = i % TC_KS;
+    const size_t off = (size_t)(kk >> 3) * (N * 16) + (size_t)(jj >> 3) * 128 + (jj & 7) * 16 +
+                       (kk & 7) * 2;
 #pragma unroll
-    for (int a = 1; a <= OZ_S; a++)
-      Cg[((size_t)(a - 1) * k2p + j) * k1p + i] = oz_slice(m, a, neg);
+    for (int a = 0; a < D8_S; a++) {
+      const unsigned short h = (unsigned short)(__float_as_uint(f[a]) >> 16);
+      *reinterpret_cast<unsigned short*>(tile + (size_t)(ks * D8_S + a) * (N * 32) + off) = h;
+    }
   }
 }
 
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+__device__ __forceinline__ void d8_fill_nan(ColList<double> Y, int j0, int N, int k2, int n,
+                                            int r0) {
+  for (int e = threadIdx.x; e < N * TC_M; e += TC_T) {
+    const int rr = e % TC_M, jj = e / TC_M;
+    if (r0 + rr < n && j0 + jj < k2)
+      Y.p[j0 + jj][r0 + rr] = __longlong_as_double(0x7ff8000000000000ll);
+  }
 }
 
-template <int TM, int TN>
-struct OzSmem {
-  __nv_bfloat16 xs[OZ_S][TM][OZ_LD];  // X slices, [slice][row][k]
-  __nv_bfloat16 cs[OZ_S][TN][OZ_LD];  // C slices, [slice][col][k]
-  int rexp[TM];
-};
-
-// CTA: WM x WN warps, warp tile 16 rows x (8*NT) columns;
-// CTA tile TM = 16*WM rows x TN = 8*NT*WN columns.
-template <int WM, int WN, int NT>
-__global__ void __launch_bounds__(OZ_T, 1)
-    k_lincomb_oz(ColList<double> X, int k1, int k1p, const __nv_bfloat16* __restrict__ Cg,
-                 const int* __restrict__ texp, int k2, int k2p, ColList<double> Y, double beta,
-                 int n, const int* __restrict__ xe) {
-  constexpr int TM = 16 * WM, TN = 8 * NT * WN;
-  static_assert(WM * WN * 32 == OZ_T, "8 warps");
-  extern __shared__ __align__(16) unsigned char smraw[];
-  OzSmem<TM, TN>& sm = *reinterpret_cast<OzSmem<TM, TN>*>(smraw);
+// Y[:, j] = beta Y[:, j] + sum_i X[:, i] C[i][j] for k1 <= 128.  Grid:
+// (row tiles of 128, output-column tiles of 64).  Dynamic shared memory:
+// tc_lincomb_smem(N).
+__global__ void __launch_bounds__(TC_T, 1)
+    k_lincomb_tc(ColList<double> X, int k1, int k1p, const uint8_t* __restrict__ Cg,
+                 const int* __restrict__ texp, int k2, ColList<double> Y, double beta, int n,
+                 const int* __restrict__ xe) {
+  extern __shared__ __align__(1024) uint8_t smtc[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp % WM, wn = warp / WM;
-  const int g = lane >> 2, tq = lane & 3;
-  const int r0 = blockIdx.x * TM;
-  const int j0 = blockIdx.y * TN;
+  const int nt = blockIdx.y, j0 = nt * TC_NMAX;
+  const int N = tc_tile_n(k2, nt);
+  const int BB = D8_S * N * 32;                           // B bytes per stage
+  const int SB = (TC_ABYTES + BB + 1023) / 1024 * 1024;   // stage stride
+  uint8_t* base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smtc) + 1023) & ~(uintptr_t)1023);
+  int* rexp = reinterpret_cast<int*>(base + TC_STAGES * SB);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(rexp + TC_M);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + TC_STAGES);
+  const int r0 = blockIdx.x * TC_M;
+  const uint8_t* Ct = Cg + (size_t)j0 * k1p * (D8_S * 2);
+  const uint32_t ncols = N <= 16 ? 128u : (N <= 32 ? 256u : 512u);
 
-  // row exponents (OZ_T / TM threads per row), loads issued in batches of 8
+  if (warp == 0) gcge::tc::tmem_alloc(tslot, ncols);
+  if (tid == 0)
+    for (int s = 0; s < TC_STAGES; s++) gcge::tc::mbar_init(&mbar[s], 1);
+  if (tid < TC_M) rexp[tid] = -2000;
+  gcge::tc::fence_before();
+  __syncthreads();
+  gcge::tc::fence_after();
+  // row exponents: two threads per row, loads issued 16 at a time
   {
-    constexpr int PARTS = OZ_T / TM;
-    const int rr = tid % TM, part = tid / TM;
-    int e = -2000;
+    const int rr = tid & (TC_M - 1), part = tid >> 7;
     const int r = r0 + rr;
+    int e = -2000;
     if (r < n) {
-      for (int i0 = part; i0 < k1; i0 += 8 * PARTS) {
-        double v[8];
+      for (int i0 = part; i0 < k1; i0 += 32) {
+        double v[16];
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-          const int i = i0 + q * PARTS;
+        for (int q = 0; q < 16; q++) {
+          const int i = i0 + 2 * q;
           v[q] = (i < k1) ? __ldg(X.p[i] + r) : 0.0;
         }
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-          const int i = i0 + q * PARTS;
+        for (int q = 0; q < 16; q++) {
+          const int i = i0 + 2 * q;
           if (i < k1) e = max(e, oz_exp_shift(v[q], -oz_bal(xe, i)));
         }
       }
     }
-    if (part == 0) sm.rexp[rr] = -2000;
-    __syncthreads();
-    atomicMax(&sm.rexp[rr], e);
-    __syncthreads();
-  }
-
-  int64_t T[NT][4];  // [n-tile][fragment element] fixed-point accumulators
-#pragma unroll
-  for (int a = 0; a < NT; a++)
-#pragma unroll
-    for (int b = 0; b < 4; b++) T[a][b] = 0;
-
-  for (int kb = 0; kb < k1p; kb += OZ_KB) {
-    float acc[OZ_NL][NT][4];
-#pragma unroll
-    for (int l = 0; l < OZ_NL; l++)
-#pragma unroll
-      for (int a = 0; a < NT; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) acc[l][a][b] = 0.f;
-    const int kend = min(kb + OZ_KB, k1p);
-    for (int kc = kb; kc < kend; kc += OZ_KC) {
-      __syncthreads();
-      // split the X chunk rows [r0, r0+TM) x cols [kc, kc+32) into slices;
-      // all of a thread's loads are issued before any is used
-      {
-        constexpr int PER = TM * OZ_KC / OZ_T;
-        double xv[PER];
-#pragma unroll
-        for (int q = 0; q < PER; q++) {
-          const int e = tid + q * OZ_T;
-          const int rr = e % TM, cc = e / TM;
-          const int r = r0 + rr, i = kc + cc;
-          xv[q] = (r < n && i < k1) ? __ldg(X.p[i] + r) : 0.0;
-        }
-#pragma unroll
-        for (int q = 0; q < PER; q++) {
-          const int e = tid + q * OZ_T;
-          const int rr = e % TM, cc = e / TM;
-          const int i = kc + cc;
-          const int ex = sm.rexp[rr];
-          bool neg = false;
-          const int d = (i < k1) ? oz_bal(xe, i) : 0;  // column i is taken as X * 2^{-d}
-          const uint64_t m = (ex >= 4096) ? 0 : oz_m56(xv[q], ex + d, &neg);
-#pragma unroll
-          for (int a = 1; a <= OZ_S; a++) sm.xs[a - 1][rr][cc] = oz_slice(m, a, neg);
-        }
-      }
-      // stage the C slices [slice][j0..j0+TN)[kc..kc+32) (16-byte copies)
-      for (int e = tid; e < OZ_S * TN * (OZ_KC / 8); e += OZ_T) {
-        const int q = e % (OZ_KC / 8);
-        const int jj = (e / (OZ_KC / 8)) % TN;
-        const int s = e / ((OZ_KC / 8) * TN);
-        const uint4 v = *reinterpret_cast<const uint4*>(Cg + ((size_t)s * k2p + j0 + jj) * k1p +
-                                                        kc + q * 8);
-        *reinterpret_cast<uint4*>(&sm.cs[s][jj][q * 8]) = v;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int ks = 0; ks < OZ_KC; ks += 16) {
-        uint32_t af[OZ_S][4];
-#pragma unroll
-        for (int a = 0; a < OZ_S; a++) {
-          const __nv_bfloat16* base = &sm.xs[a][wm * 16][ks];
-          af[a][0] = *reinterpret_cast<const uint32_t*>(base + g * OZ_LD + tq * 2);
-          af[a][1] = *reinterpret_cast<const uint32_t*>(base + (g + 8) * OZ_LD + tq * 2);
-          af[a][2] = *reinterpret_cast<const uint32_t*>(base + g * OZ_LD + tq * 2 + 8);
-          af[a][3] = *reinterpret_cast<const uint32_t*>(base + (g + 8) * OZ_LD + tq * 2 + 8);
-        }
-#pragma unroll
-        for (int b = 0; b < OZ_S; b++) {
-#pragma unroll
-          for (int nt = 0; nt < NT; nt++) {
-            const __nv_bfloat16* bb = &sm.cs[b][wn * (8 * NT) + nt * 8 + g][ks];
-            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(bb + tq * 2);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(bb + tq * 2 + 8);
-#pragma unroll
-            for (int a = 0; a < OZ_S; a++)
-              if (a + b <= OZ_NL - 1)  // slices a+1, b+1: level (a+1)+(b+1) <= 10
-                mma_bf16(acc[a + b][nt], af[a], b0, b1);
-          }
-        }
-      }
-    }
-    // fold the exact level sums into the fixed-point accumulators
-#pragma unroll
-    for (int l = 0; l < OZ_NL; l++) {
-      const int L = l + 2;
-      const int sh = 54 - 7 * L;
-#pragma unroll
-      for (int nt = 0; nt < NT; nt++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const int64_t v = (int64_t)__float2int_rn(acc[l][nt][q]);
-          T[nt][q] += (sh >= 0) ? v * ((int64_t)1 << sh) : (v >> (-sh));
-        }
-    }
+    atomicMax(&rexp[rr], e);
   }
   __syncthreads();
-  // stage the results as doubles [col][row] for coalesced column writes
-  double* ys = reinterpret_cast<double*>(smraw);  // TN x TM doubles
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = gcge::tc::idesc_bf16(TC_M, N);
+
+  // slicing role of this thread: row rr, 8 values k = 16 s + 8 kg + q
+  const int rr = tid & (TC_M - 1), kg = tid >> 7;
+  const int r = r0 + rr;
+  const int myexp = rexp[rr];
+  const int nks = k1p / TC_KS;
+  bool ok = true;
+  double vn[8];
 #pragma unroll
-  for (int nt = 0; nt < NT; nt++)
+  for (int q = 0; q < 8; q++) {
+    const int i = 8 * kg + q;
+    vn[q] = (r < n && i < k1) ? __ldg(X.p[i] + r) : 0.0;
+  }
+  for (int s = 0; s < nks; s++) {
+    const int buf = s % TC_STAGES;
+    double v[8];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int rr = wm * 16 + g + ((q >= 2) ? 8 : 0);
-      const int jj = wn * (8 * NT) + nt * 8 + tq * 2 + (q & 1);
-      const int j = j0 + jj;
-      const int re = sm.rexp[rr];
-      double y;
-      if (j >= k2) {
-        y = 0.0;
-      } else {
-        const int te = texp[j];
-        if (re >= 4096 || te >= 4096) y = __longlong_as_double(0x7ff8000000000000ll);  // NaN in
+    for (int q = 0; q < 8; q++) v[q] = vn[q];
+    if (s + 1 < nks) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int i = (s + 1) * TC_KS + 8 * kg + q;
+        vn[q] = (r < n && i < k1) ? __ldg(X.p[i] + r) : 0.0;
+      }
+    }
+    uint8_t* As = base + buf * SB;
+    uint8_t* Bs = As + TC_ABYTES;
+    if (s >= TC_STAGES) {
+      // the MMAs of stage s - TC_STAGES read this buffer
+      if (!gcge::tc::mbar_wait(&mbar[buf], ((s / TC_STAGES) - 1) & 1, TC_WAIT)) ok = false;
+    }
+    // digits of this thread's 8 values -> 7 x 16 bytes
+    {
+      float f[8][D8_S];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int i = s * TC_KS + 8 * kg + q;
+        const int E = (myexp >= 4096) ? 4096 : myexp + ((i < k1) ? oz_bal(xe, i) : 0);
+        d8_digits(myexp >= 4096 ? 0.0 : v[q], E, f[q]);
+      }
+      uint8_t* dst = As + kg * 2048 + (rr >> 3) * 128 + (rr & 7) * 16;
+#pragma unroll
+      for (int a = 0; a < D8_S; a++) {
+        uint4 w;
+        w.x = d8_pack(f[0][a], f[1][a]);
+        w.y = d8_pack(f[2][a], f[3][a]);
+        w.z = d8_pack(f[4][a], f[5][a]);
+        w.w = d8_pack(f[6][a], f[7][a]);
+        *reinterpret_cast<uint4*>(dst + a * (TC_M * TC_KS * 2)) = w;
+      }
+    }
+    // B operand of this stage: one contiguous block of BB bytes
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(Ct + (size_t)s * BB);
+      uint4* dst = reinterpret_cast<uint4*>(Bs);
+      for (int e = tid; e < BB / 16; e += TC_T) dst[e] = __ldg(src + e);
+    }
+    gcge::tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      gcge::tc::fence_after();
+      const uint32_t abase = gcge::tc::smem_u32(As), bbase = gcge::tc::smem_u32(Bs);
+#pragma unroll
+      for (int L = 2; L <= D8_NL + 1; L++) {
+#pragma unroll
+        for (int a = 1; a <= D8_S; a++) {
+          const int b = L - a;
+          if (b < 1 || b > D8_S) continue;
+          const uint64_t ad = gcge::tc::smem_desc(abase + (a - 1) * (TC_M * TC_KS * 2), 2048, 128);
+          const uint64_t bd = gcge::tc::smem_desc(bbase + (b - 1) * (N * 32), N * 16, 128);
+          const uint32_t accum = (s > 0 || a != (L - D8_S > 1 ? L - D8_S : 1)) ? 1u : 0u;
+          gcge::tc::mma_bf16(tmem + (uint32_t)((L - 2) * N), ad, bd, idesc, accum);
+        }
+      }
+      gcge::tc::commit(&mbar[buf]);
+    }
+  }
+  // wait for the last stage (its commit covers every earlier MMA)
+  {
+    const int s = nks - 1;
+    if (!gcge::tc::mbar_wait(&mbar[s % TC_STAGES], (s / TC_STAGES) & 1, TC_WAIT)) ok = false;
+  }
+  gcge::tc::fence_after();
+  const int anybad = __syncthreads_or(ok ? 0 : 1);
+  if (anybad) {
+    if (tid == 0) atomicExch(&g_oz_tc_status, 1);
+    d8_fill_nan(Y, j0, N, k2, n, r0);
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, column half w / 4
+    const int q4 = warp & 3, h = warp >> 2;
+    const int row = r0 + 32 * q4 + lane;
+    const int re = rexp[32 * q4 + lane];
+    const int half = N / 2;
+    for (int c0 = h * half; c0 < (h + 1) * half; c0 += 8) {
+      uint32_t acc[D8_NL][8];
+#pragma unroll
+      for (int l = 0; l < D8_NL; l++)
+        gcge::tc::tmem_ld8(tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(l * N + c0), acc[l]);
+      gcge::tc::tmem_wait_ld();
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++) {
+        const int j = j0 + c0 + jj;
+        if (j >= k2 || row >= n) continue;
+        long long T = 0;
+#pragma unroll
+        for (int l = 0; l < D8_NL; l++) {
+          const long long v = (long long)__float2int_rn(__uint_as_float(acc[l][jj]));
+          const int sh = 57 - 8 * (l + 2);  // levels 8, 9 rounded to the nearest unit
+          T += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+        }
+        const int te = __ldg(texp + j);
+        double y;
+        if (re >= 4096 || te >= 4096) y = __longlong_as_double(0x7ff8000000000000ll);
         else if (re <= -2000 || te <= -2000) y = 0.0;
-        else y = scalbn((double)T[nt][q], re + te - 54);
+        else y = d8_to_double(T, re + te - 55);
+        double* yp = Y.p[j] + row;
+        *yp = (beta == 0.0) ? y : fma(beta, *yp, y);
       }
-      ys[jj * TM + rr] = y;
     }
+  }
+  gcge::tc::fence_before();
   __syncthreads();
-  for (int e = tid; e < TN * TM; e += OZ_T) {
-    const int rr = e % TM, jj = e / TM;
-    const int r = r0 + rr, j = j0 + jj;
-    if (r < n && j < k2) {
-      double* yp = Y.p[j] + r;
-      const double v = ys[jj * TM + rr];
-      *yp = (beta == 0.0) ? v : fma(beta, *yp, v);
-    }
+  if (warp == 0) {
+    gcge::tc::fence_after();
+    gcge::tc::tmem_dealloc(tmem, ncols);
   }
 }
 
-template <int WM, int WN, int NT>
-void launch_oz(const ColList<double>& X, int k1, int k1p, const __nv_bfloat16* Cg,
-               const int* texp, const ColList<double>& Y, int k2, int k2p, double beta, int n,
-               const int* xe, cudaStream_t st) {
-  constexpr int TM = 16 * WM, TN = 8 * NT * WN;
-  const size_t sm = sizeof(OzSmem<TM, TN>) > (size_t)TN * TM * 8 ? sizeof(OzSmem<TM, TN>)
-                                                                  : (size_t)TN * TM * 8;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_lincomb_oz<WM, WN, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    attr = true;
-  }
-  dim3 grid((n + TM - 1) / TM, (k2 + TN - 1) / TN);
-  k_lincomb_oz<WM, WN, NT><<<grid, OZ_T, sm, st>>>(X, k1, k1p, Cg, texp, k2, k2p, Y, beta, n, xe);
+size_t tc_lincomb_smem(int N) {
+  const int SB = (TC_ABYTES + D8_S * N * 32 + 1023) / 1024 * 1024;
+  return (size_t)TC_STAGES * SB + 1024 /* alignment */ + TC_M * 4 + TC_STAGES * 8 + 16;
 }
-
 // ---------------------------------------------------------------- Gram
 // G = V^T W (k1 x k2) over n rows with FP64 accuracy.  Rows are processed in
 // chunks of OG_R = 32; within a chunk every column of V and of W gets its own
@@ -497,35 +602,66 @@ int launch_gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, i
 }  // namespace
 
 size_t lincomb_oz_scratch_bytes(int k1, int k2) {
-  const int k1p = (k1 + OZ_KC - 1) / OZ_KC * OZ_KC;
-  const int k2p = (k2 + 63) / 64 * 64;
-  return sizeof(__nv_bfloat16) * (size_t)OZ_S * k1p * k2p + sizeof(int) * (size_t)(k2p + k1p) +
-         256;
+  const int kb = k1 < 128 ? (k1 > 0 ? k1 : 1) : 128;
+  const int k1p = tc_round16(kb);
+  const int k2p = (k2 + TC_NMAX - 1) / TC_NMAX * TC_NMAX;
+  return (size_t)k2p * k1p * (D8_S * 2) + sizeof(int) * (size_t)(k2p + (k1 > 0 ? k1 : 1)) + 512;
 }
 
-// Y_j = beta Y_j + sum_i X_i C[i + j*ldc], FP64 accuracy on bf16 tensor cores.
-// scratch: lincomb_oz_scratch_bytes(k1, k2) bytes, 16-byte aligned.  balance:
-// scale the columns of X by powers of two (and the rows of C inversely)
-// first, for blocks whose columns differ widely in magnitude (the product is
-// unchanged: the scaling is exact).
+// Y_j = beta Y_j + sum_i X_i C[i + j*ldc], FP64 accuracy on the tcgen05
+// tensor cores.  scratch: lincomb_oz_scratch_bytes(k1, k2) bytes, 16-byte
+// aligned.  balance: scale the columns of X by powers of two (and the rows of
+// C inversely) first, for blocks whose columns differ widely in magnitude
+// (the product is unchanged: the scaling is exact).  negate: use -C.  k1 >
+// 128 runs in blocks of 128 rows of C, each added to Y in FP64.  Y must not
+// alias X.
 void lincomb_oz(const ColList<double>& X, int k1, const double* C, int ldc,
                 const ColList<double>& Y, int k2, double beta, int n, void* scratch,
                 cudaStream_t st, bool balance, bool negate) {
   if (k2 <= 0 || n <= 0) return;
-  const int k1p = (k1 + OZ_KC - 1) / OZ_KC * OZ_KC;
-  const int k2p = (k2 + 63) / 64 * 64;  // C slices padded to the widest CTA tile
-  __nv_bfloat16* Cg = reinterpret_cast<__nv_bfloat16*>(scratch);
-  int* texp = reinterpret_cast<int*>(Cg + (size_t)OZ_S * k1p * k2p);
-  int* xe = balance ? texp + k2p : nullptr;
+  if (k1 <= 0) {
+    lincomb_f64(X, 0, C, ldc, Y, k2, beta, n, st);
+    return;
+  }
+  const int ntile = (k2 + TC_NMAX - 1) / TC_NMAX;
+  const int k2pad = (ntile - 1) * TC_NMAX + tc_tile_n(k2, ntile - 1);
+  const int kbmax = k1 < 128 ? k1 : 128;
+  uint8_t* Cg = reinterpret_cast<uint8_t*>(scratch);
+  int* texp = reinterpret_cast<int*>(
+      Cg + (size_t)ntile * TC_NMAX * tc_round16(kbmax) * (D8_S * 2));
+  int* xe = balance ? texp + ntile * TC_NMAX : nullptr;
   if (balance) {
     k_fill_int<<<(k1 + 127) / 128, 128, 0, st>>>(xe, -2000, k1);
     const int nb = (n + 255) / 256 < 64 ? (n + 255) / 256 : 64;
     k_oz_colexp<<<dim3(nb, k1), 256, 0, st>>>(X, k1, n, xe);
   }
-  k_oz_split_c<<<k2p, 128, 0, st>>>(C, ldc, k1, k2, k1p, k2p, xe, negate ? 1 : 0, Cg, texp);
-  if (k2 <= 16) launch_oz<8, 1, 2>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, xe, st);
-  else if (k2 <= 32) launch_oz<8, 1, 4>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, xe, st);
-  else launch_oz<4, 2, 4>(X, k1, k1p, Cg, texp, Y, k2, k2p, beta, n, xe, st);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_lincomb_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc_lincomb_smem(TC_NMAX));
+    attr = true;
+  }
+  const size_t smem = tc_lincomb_smem(tc_tile_n(k2, 0));
+  for (int kb = 0; kb < k1; kb += 128) {
+    const int kc = (k1 - kb) < 128 ? (k1 - kb) : 128;
+    const int k1p = tc_round16(kc);
+    ColList<double> Xb;
+    for (int i = 0; i < kc; i++) Xb.p[i] = X.p[kb + i];
+    const int* xeb = xe ? xe + kb : nullptr;
+    k_d8_split_c<<<k2pad, 128, 0, st>>>(C + kb, ldc, kc, k2, k1p, xeb, negate ? 1 : 0, Cg, texp);
+    k_lincomb_tc<<<dim3((n + TC_M - 1) / TC_M, ntile), TC_T, smem, st>>>(
+        Xb, kc, k1p, Cg, texp, k2, Y, kb == 0 ? beta : 1.0, n, xeb);
+  }
+}
+
+int oz_tc_status(bool reset) {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_oz_tc_status, sizeof(int)) != cudaSuccess) return -1;
+  if (reset && v) {
+    const int z = 0;
+    cudaMemcpyToSymbol(g_oz_tc_status, &z, sizeof(int));
+  }
+  return v;
 }
 
 size_t gram_oz_partial_doubles(int k1, int k2) {
