@@ -1,23 +1,15 @@
-// FP64-accurate tall-skinny linear combination Y = X C (+ beta Y) on the
-// bf16 tensor cores (mma.sync.m16n8k16, FP32 accumulate), by error-free
-// splitting (the Ozaki scheme).
+// FP64-accurate tall-skinny products on the GB300 tensor cores (tcgen05,
+// bf16 operands in shared memory, FP32 accumulators in tensor memory) by
+// error-free splitting into integer digits (the Ozaki scheme):
+//   * k_lincomb_tc: Y = X C (+ beta Y), the X/P/W updates of GCG
+//     (n x k1 times k1 x k2, k1 <= 256, k2 <= 256);
+//   * k_gram_tc: G = V^T diag(d) W, the inner products of the orthogonalisation
+//     and of the Rayleigh-Ritz projection.
 //
-// Why: on GB300 FP64 FMA runs at ~1 TFLOP/s while bf16 MMA runs at ~600
-// TFLOP/s (measured), so the X/P/W updates of GCG (n x k1 times k1 x k2,
-// k1 <= 200) are the solve's bottleneck in FP64.
+// Why: on GB300 FP64 FMA runs at ~1 TFLOP/s while the bf16 tensor cores run
+// at ~2 PFLOP/s (measured), so in FP64 these products, not the memory
+// traffic, bound the GCG iteration.
 //
-// Scheme.  Each row r of X is scaled by 2^{e_r} (e_r: smallest power of two
-// above the row's largest |x|) and each column j of C by 2^{t_j}; the scaled
-// values in (-1, 1) are cut into S = 8 signed 7-bit integer slices
-// (x / 2^e = sum_a s_a 2^{-7a}, 56 bits, truncation error < 2^{-56}).  Every
-// slice is exactly a bf16.  The products P_ab = X_a C_b of slices are
-// integers bounded by k * 127^2; for k <= 128 a level L = a + b (up to 8
-// pairs) sums below 2^24, so one FP32 MMA accumulator per level is exact.
-// Levels L = 2..10 are kept (43 of the 64 slice products); the first dropped
-// level contributes below 6 * 127^2 * 2^{-77} < 2^{-60} of the scale.  The levels are combined exactly in a 64-bit fixed-point integer
-// T = sum_L acc_L 2^{54-7L}, and Y = T 2^{e_r + t_j - 54}.  The error is
-// about k * 2^{-55} relative to sum_i |x_ri| |c_ij|, the bound of an FP64
-// dot product.  k1 > 128 is processed in blocks of 128 that add into T.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -27,23 +19,6 @@
 namespace gcge {
 namespace {
 
-constexpr int OZ_S = 8;           // slices per value
-constexpr int OZ_T = 256;         // 8 warps per CTA
-constexpr int OZ_NL = 9;          // levels L = 2..10
-
-// Scaled 56-bit magnitude of x for the group exponent e (|x| < 2^e).
-__device__ __forceinline__ uint64_t oz_m56(double x, int e, bool* neg) {
-  const uint64_t b = (uint64_t)__double_as_longlong(x);
-  *neg = (b >> 63) != 0;
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0 || ex == 0x7FF) return 0;  // zero/subnormal (negligible) or non-finite (flagged)
-  const uint64_t mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
-  const int sh = (ex - 1023) + 4 - e;
-  if (sh >= 0) return mant << sh;  // sh <= 3 since |x| < 2^e
-  if (sh <= -64) return 0;
-  return mant >> (-sh);
-}
-
 // exponent e with |x| < 2^e (0 for zero/subnormal); non-finite -> 4096
 __device__ __forceinline__ int oz_exp(double x) {
   const uint64_t b = (uint64_t)__double_as_longlong(x);
@@ -51,11 +26,6 @@ __device__ __forceinline__ int oz_exp(double x) {
   if (ex == 0x7FF) return 4096;
   if (ex == 0) return -2000;
   return ex - 1023 + 1;
-}
-
-__device__ __forceinline__ __nv_bfloat16 oz_slice(uint64_t m, int a, bool neg) {
-  const int v = (int)((m >> (56 - 7 * a)) & 127u);
-  return __float2bfloat16_rn(neg ? -(float)v : (float)v);
 }
 
 // exponent of x scaled by 2^d (sentinels kept)
@@ -93,14 +63,6 @@ __device__ __forceinline__ int oz_bal(const int* xe, int i) {
   return d <= -2000 ? 0 : d;
 }
 
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
 // ---------------------------------------------------------------- tcgen05 linear combination
 // Y = X C on the 5th-generation tensor cores.  Digits: every value, scaled by
 // its group's power of two into (-1, 1), is cut into D8_S = 7 balanced
@@ -128,7 +90,7 @@ constexpr int TC_M = 128;
 constexpr int TC_KS = 16;
 constexpr int TC_NMAX = 64;
 constexpr int TC_STAGES = 3;
-constexpr int TC_T = 256;
+constexpr int TC_T = 512;
 constexpr int TC_ABYTES = D8_S * TC_M * TC_KS * 2;  // 28672
 constexpr int TC_WAIT = 1 << 26;                    // mbarrier polls before giving up
 
@@ -161,6 +123,35 @@ __device__ __forceinline__ void d8_digits(double x, int E, float* f) {
   f[4] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7652)) - 8388736.0f;
   f[5] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7651)) - 8388736.0f;
   f[6] = __int_as_float(__byte_perm(lo, 0x4B000000u, 0x7650)) - 8388736.0f;
+}
+
+// exponent e with |x| < 2^e from the high 32 bits of x (sentinels as oz_exp)
+__device__ __forceinline__ int oz_exp_hi(int hi) {
+  const int ex = (hi >> 20) & 0x7FF;
+  if (ex == 0x7FF) return 4096;
+  if (ex == 0) return -2000;
+  return ex - 1023 + 1;
+}
+
+// high 32 bits of p[i] (the sign, exponent and top of the mantissa)
+__device__ __forceinline__ int ld_hi(const double* p) {
+  return __ldg(reinterpret_cast<const int*>(p) + 1);
+}
+
+// 4 values -> 7 digit rows of 8 bytes at dst + a*dstride (half of a
+// core-matrix row), value q scaled by 2^{-E[q]}
+__device__ __forceinline__ void d8_slice4(const double* v, const int* E, uint8_t* dst,
+                                          int dstride) {
+  float f[4][D8_S];
+#pragma unroll
+  for (int q = 0; q < 4; q++) d8_digits(v[q], E[q], f[q]);
+#pragma unroll
+  for (int a = 0; a < D8_S; a++) {
+    uint2 w;
+    w.x = d8_pack(f[0][a], f[1][a]);
+    w.y = d8_pack(f[2][a], f[3][a]);
+    *reinterpret_cast<uint2*>(dst + a * dstride) = w;
+  }
 }
 
 // T 2^s rounded to the nearest double (ties to even), by integer operations.
@@ -197,8 +188,9 @@ __host__ __device__ __forceinline__ int tc_tile_n(int k2, int nt) {
 
 // C (k1 x k2, ldc; k1 <= 128) -> B operand images Cg and column exponents
 // texp.  Layout: tile nt (TC_NMAX columns) at byte nt*TC_NMAX*k1p*14, inside it
-// stage ks (16 values of i) and digit a at (ks*7 + a) * N*32, then the
-// K-major core-matrix image of N columns x 16 values.  Grid: one CTA per
+// stage ks (16 values of i) at ks*7*N*32: the K-major core-matrix image of a
+// 7N x 16 matrix whose row (a, j) = a*N + j is digit a of column j (so one
+// descriptor spans several digits of the tile).  Grid: one CTA per
 // padded column.  Row i of C is taken as C[i][j] 2^{xe[i]} (balancing), and
 // negated when negate is set.
 __global__ void k_d8_split_c(const double* __restrict__ C, int ldc, int k1, int k2, int k1p,
@@ -226,12 +218,12 @@ __global__ void k_d8_split_c(const double* __restrict__ C, int ldc, int k1, int 
     float f[D8_S];
     d8_digits(c, t - d, f);
     const int ks = i / TC_KS, kk = i % TC_KS;
-    const size_t off = (size_t)(kk >> 3) * (N * 16) + (size_t)(jj >> 3) * 128 + (jj & 7) * 16 +
-                       (kk & 7) * 2;
+    const size_t off = (size_t)ks * (D8_S * N * 32) + (size_t)(kk >> 3) * (D8_S * N * 16) +
+                       (size_t)(jj >> 3) * 128 + (jj & 7) * 16 + (kk & 7) * 2;
 #pragma unroll
     for (int a = 0; a < D8_S; a++) {
       const unsigned short h = (unsigned short)(__float_as_uint(f[a]) >> 16);
-      *reinterpret_cast<unsigned short*>(tile + (size_t)(ks * D8_S + a) * (N * 32) + off) = h;
+      *reinterpret_cast<unsigned short*>(tile + off + (size_t)a * (N * 16)) = h;
     }
   }
 }
@@ -245,10 +237,39 @@ __device__ __forceinline__ void d8_fill_nan(ColList<double> Y, int j0, int N, in
   }
 }
 
+// Issues the 34 digit products of one K step of 16.  A digit a (1..7) is
+// multiplied by B digits b = 1..min(7, 9-a) in MMAs whose N spans several
+// digits (at most 256 columns each), with D offset so that product (a, b)
+// accumulates on level a + b, i.e. TMEM columns (a+b-2)*Nw of the 8*Nw level
+// block: 7 MMAs per step for Nw <= 32 instead of one per product.  first: the
+// step opens the accumulation (level blocks 2..8 are first written by a = 1,
+// level 9 by (a, b) = (2, 7), issued on its own then).  A digit a is the
+// 128 x 16 tile at abase + (a-1)*astride (core matrices 2048 bytes apart
+// along K); the B image is the 7Nw x 16 matrix described at k_d8_split_c.
+__device__ __forceinline__ void d8_issue(uint32_t tacc, uint32_t abase, uint32_t astride,
+                                         uint32_t bbase, int Nw, bool first) {
+  const int maxd = 256 / Nw;
+#pragma unroll
+  for (int a = 1; a <= D8_S; a++) {
+    const uint64_t ad = gcge::tc::smem_desc(abase + (a - 1) * astride, TC_M * 16, 128);
+    const int bmax = (9 - a) < D8_S ? (9 - a) : D8_S;
+    int b0 = 1;
+    while (b0 <= bmax) {
+      int cnt = (bmax - b0 + 1) < maxd ? (bmax - b0 + 1) : maxd;
+      if (first && a == 2 && b0 + cnt - 1 == D8_S && cnt > 1) cnt -= 1;
+      const uint32_t accum = (first && (a == 1 || (a == 2 && b0 == D8_S))) ? 0u : 1u;
+      const uint64_t bd = gcge::tc::smem_desc(bbase + (b0 - 1) * Nw * 16, D8_S * Nw * 16, 128);
+      gcge::tc::mma_bf16(tacc + (uint32_t)((a + b0 - 2) * Nw), ad, bd,
+                         gcge::tc::idesc_bf16(TC_M, cnt * Nw), accum);
+      b0 += cnt;
+    }
+  }
+}
+
 // Y[:, j] = beta Y[:, j] + sum_i X[:, i] C[i][j] for k1 <= 128.  Grid:
-// (row tiles of 128, output-column tiles of 64).  Dynamic shared memory:
-// tc_lincomb_smem(N).
-__global__ void __launch_bounds__(TC_T, 1)
+// (row tiles of 128, output-column tiles of 64), 512 threads.  Dynamic
+// shared memory: tc_lincomb_smem(N of tile 0).
+__global__ void __launch_bounds__(TC_T, 2)
     k_lincomb_tc(ColList<double> X, int k1, int k1p, const uint8_t* __restrict__ Cg,
                  const int* __restrict__ texp, int k2, ColList<double> Y, double beta, int n,
                  const int* __restrict__ xe) {
@@ -256,8 +277,8 @@ __global__ void __launch_bounds__(TC_T, 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nt = blockIdx.y, j0 = nt * TC_NMAX;
   const int N = tc_tile_n(k2, nt);
-  const int BB = D8_S * N * 32;                           // B bytes per stage
-  const int SB = (TC_ABYTES + BB + 1023) / 1024 * 1024;   // stage stride
+  const int BB = D8_S * N * 32;                          // B bytes per stage
+  const int SB = (TC_ABYTES + BB + 1023) / 1024 * 1024;  // stage stride
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smtc) + 1023) & ~(uintptr_t)1023);
   int* rexp = reinterpret_cast<int*>(base + TC_STAGES * SB);
@@ -274,23 +295,36 @@ __global__ void __launch_bounds__(TC_T, 1)
   gcge::tc::fence_before();
   __syncthreads();
   gcge::tc::fence_after();
-  // row exponents: two threads per row, loads issued 16 at a time
+  // row exponents: four threads per row, the high words of all (<= 32) of a
+  // thread's values loaded at once
   {
     const int rr = tid & (TC_M - 1), part = tid >> 7;
     const int r = r0 + rr;
     int e = -2000;
     if (r < n) {
-      for (int i0 = part; i0 < k1; i0 += 32) {
-        double v[16];
+      int hv[32];
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int i = i0 + 2 * q;
-          v[q] = (i < k1) ? __ldg(X.p[i] + r) : 0.0;
+      for (int q = 0; q < 32; q++) {
+        const int i = part + 4 * q;
+        hv[q] = (i < k1) ? ld_hi(X.p[i] + r) : 0;
+      }
+      if (!xe) {
+        int fmax = 0, bad = 0;
+#pragma unroll
+        for (int q = 0; q < 32; q++) {
+          const int f = (hv[q] >> 20) & 0x7FF;
+          bad |= f == 0x7FF;
+          fmax = max(fmax, f);
         }
+        e = bad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
+      } else {
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int i = i0 + 2 * q;
-          if (i < k1) e = max(e, oz_exp_shift(v[q], -oz_bal(xe, i)));
+        for (int q = 0; q < 32; q++) {
+          const int i = part + 4 * q;
+          if (i < k1) {
+            const int ex = oz_exp_hi(hv[q]);
+            e = max(e, (ex >= 4096 || ex <= -2000) ? ex : ex - oz_bal(xe, i));
+          }
         }
       }
     }
@@ -298,57 +332,48 @@ __global__ void __launch_bounds__(TC_T, 1)
   }
   __syncthreads();
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = gcge::tc::idesc_bf16(TC_M, N);
 
-  // slicing role of this thread: row rr, 8 values k = 16 s + 8 kg + q
-  const int rr = tid & (TC_M - 1), kg = tid >> 7;
-  const int r = r0 + rr;
-  const int myexp = rexp[rr];
+  // slicing role: row srr, values k = 16 s + 4 kq + q (q < 4); the two
+  // threads of a lane pair fill the two halves of one 16-byte core-matrix row
+  const int srr = (tid >> 1) & (TC_M - 1), kq = ((tid >> 8) << 1) | (tid & 1);
+  const int sr = r0 + srr;
+  const int myexp = rexp[srr];
+  const int doff = (kq >> 1) * 2048 + (srr >> 3) * 128 + (srr & 7) * 16 + (kq & 1) * 8;
   const int nks = k1p / TC_KS;
   bool ok = true;
-  double vn[8];
+  double vn[4];
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    const int i = 8 * kg + q;
-    vn[q] = (r < n && i < k1) ? __ldg(X.p[i] + r) : 0.0;
+  for (int q = 0; q < 4; q++) {
+    const int i = 4 * kq + q;
+    vn[q] = (sr < n && i < k1) ? __ldg(X.p[i] + sr) : 0.0;
   }
   for (int s = 0; s < nks; s++) {
     const int buf = s % TC_STAGES;
-    double v[8];
+    double v[4];
 #pragma unroll
-    for (int q = 0; q < 8; q++) v[q] = vn[q];
+    for (int q = 0; q < 4; q++) v[q] = vn[q];
     if (s + 1 < nks) {
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const int i = (s + 1) * TC_KS + 8 * kg + q;
-        vn[q] = (r < n && i < k1) ? __ldg(X.p[i] + r) : 0.0;
+      for (int q = 0; q < 4; q++) {
+        const int i = (s + 1) * TC_KS + 4 * kq + q;
+        vn[q] = (sr < n && i < k1) ? __ldg(X.p[i] + sr) : 0.0;
       }
     }
     uint8_t* As = base + buf * SB;
     uint8_t* Bs = As + TC_ABYTES;
     if (s >= TC_STAGES) {
       // the MMAs of stage s - TC_STAGES read this buffer
-      if (!gcge::tc::mbar_wait(&mbar[buf], ((s / TC_STAGES) - 1) & 1, TC_WAIT)) ok = false;
+      if (!gcge::tc::mbar_wait_warp(&mbar[buf], ((s / TC_STAGES) - 1) & 1, TC_WAIT)) ok = false;
     }
-    // digits of this thread's 8 values -> 7 x 16 bytes
     {
-      float f[8][D8_S];
+      int E[4];
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const int i = s * TC_KS + 8 * kg + q;
-        const int E = (myexp >= 4096) ? 4096 : myexp + ((i < k1) ? oz_bal(xe, i) : 0);
-        d8_digits(myexp >= 4096 ? 0.0 : v[q], E, f[q]);
+      for (int q = 0; q < 4; q++) {
+        const int i = s * TC_KS + 4 * kq + q;
+        E[q] = (myexp >= 4096) ? 4096 : myexp + ((i < k1) ? oz_bal(xe, i) : 0);
+        if (myexp >= 4096) v[q] = 0.0;
       }
-      uint8_t* dst = As + kg * 2048 + (rr >> 3) * 128 + (rr & 7) * 16;
-#pragma unroll
-      for (int a = 0; a < D8_S; a++) {
-        uint4 w;
-        w.x = d8_pack(f[0][a], f[1][a]);
-        w.y = d8_pack(f[2][a], f[3][a]);
-        w.z = d8_pack(f[4][a], f[5][a]);
-        w.w = d8_pack(f[6][a], f[7][a]);
-        *reinterpret_cast<uint4*>(dst + a * (TC_M * TC_KS * 2)) = w;
-      }
+      d8_slice4(v, E, As + doff, TC_M * TC_KS * 2);
     }
     // B operand of this stage: one contiguous block of BB bytes
     {
@@ -360,26 +385,14 @@ __global__ void __launch_bounds__(TC_T, 1)
     __syncthreads();
     if (tid == 0) {
       gcge::tc::fence_after();
-      const uint32_t abase = gcge::tc::smem_u32(As), bbase = gcge::tc::smem_u32(Bs);
-#pragma unroll
-      for (int L = 2; L <= D8_NL + 1; L++) {
-#pragma unroll
-        for (int a = 1; a <= D8_S; a++) {
-          const int b = L - a;
-          if (b < 1 || b > D8_S) continue;
-          const uint64_t ad = gcge::tc::smem_desc(abase + (a - 1) * (TC_M * TC_KS * 2), 2048, 128);
-          const uint64_t bd = gcge::tc::smem_desc(bbase + (b - 1) * (N * 32), N * 16, 128);
-          const uint32_t accum = (s > 0 || a != (L - D8_S > 1 ? L - D8_S : 1)) ? 1u : 0u;
-          gcge::tc::mma_bf16(tmem + (uint32_t)((L - 2) * N), ad, bd, idesc, accum);
-        }
-      }
+      d8_issue(tmem, gcge::tc::smem_u32(As), TC_M * TC_KS * 2, gcge::tc::smem_u32(Bs), N, s == 0);
       gcge::tc::commit(&mbar[buf]);
     }
   }
   // wait for the last stage (its commit covers every earlier MMA)
   {
     const int s = nks - 1;
-    if (!gcge::tc::mbar_wait(&mbar[s % TC_STAGES], (s / TC_STAGES) & 1, TC_WAIT)) ok = false;
+    if (!gcge::tc::mbar_wait_warp(&mbar[s % TC_STAGES], (s / TC_STAGES) & 1, TC_WAIT)) ok = false;
   }
   gcge::tc::fence_after();
   const int anybad = __syncthreads_or(ok ? 0 : 1);
@@ -387,19 +400,19 @@ __global__ void __launch_bounds__(TC_T, 1)
     if (tid == 0) atomicExch(&g_oz_tc_status, 1);
     d8_fill_nan(Y, j0, N, k2, n, r0);
   } else {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, column half w / 4
-    const int q4 = warp & 3, h = warp >> 2;
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, column quarter w / 4
+    const int q4 = warp & 3, cg = warp >> 2;
     const int row = r0 + 32 * q4 + lane;
     const int re = rexp[32 * q4 + lane];
-    const int half = N / 2;
-    for (int c0 = h * half; c0 < (h + 1) * half; c0 += 8) {
-      uint32_t acc[D8_NL][8];
+    const int quarter = N / 4;
+    for (int c0 = cg * quarter; c0 < (cg + 1) * quarter; c0 += 4) {
+      uint32_t acc[D8_NL][4];
 #pragma unroll
       for (int l = 0; l < D8_NL; l++)
-        gcge::tc::tmem_ld8(tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(l * N + c0), acc[l]);
+        gcge::tc::tmem_ld4(tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(l * N + c0), acc[l]);
       gcge::tc::tmem_wait_ld();
 #pragma unroll
-      for (int jj = 0; jj < 8; jj++) {
+      for (int jj = 0; jj < 4; jj++) {
         const int j = j0 + c0 + jj;
         if (j >= k2 || row >= n) continue;
         long long T = 0;
@@ -431,171 +444,407 @@ size_t tc_lincomb_smem(int N) {
   const int SB = (TC_ABYTES + D8_S * N * 32 + 1023) / 1024 * 1024;
   return (size_t)TC_STAGES * SB + 1024 /* alignment */ + TC_M * 4 + TC_STAGES * 8 + 16;
 }
-// ---------------------------------------------------------------- Gram
-// G = V^T W (k1 x k2) over n rows with FP64 accuracy.  Rows are processed in
-// chunks of OG_R = 32; within a chunk every column of V and of W gets its own
-// power-of-two scale, the 8 x 8 slice products of a level are summed exactly
-// in FP32 by the MMAs (32 * 8 * 127^2 < 2^24), the levels are combined in a
-// 64-bit fixed-point integer and the chunk's exact value is added to an FP64
-// per-CTA partial sum.  A CTA owns a group of GM columns of V x GN columns of
-// W; warp w owns m-tile w of its group.  A warp reads one column's 32 rows of
-// a chunk with one coalesced load (lane = row), finds the column's scale by
-// a warp max and writes the 8 slices, so each value is read from HBM once.
-constexpr int OG_R = 32;
-constexpr int OG_LD = OG_R + 8;  // 20 words per staged column: conflict-free fragments
+// ---------------------------------------------------------------- tcgen05 Gram
+// G = V^T diag(wd) W (wd NULL: identity) with FP64 accuracy.  One CTA owns up
+// to 128 columns of V (MMA M, TMEM lane = column of V) and up to 32 columns
+// of W (MMA N) over a strided set of 128-row chunks.  In a chunk every column
+// has one power-of-two scale (its largest |value| over the chunk, a W column
+// taken with the diagonal applied), the 7 balanced base-256 digits of the
+// lincomb are used, and the 8 level sums over the chunk's 128 rows are exact
+// in FP32 tensor memory.  The column exponents of chunk c+1 are gathered
+// while chunk c is sliced (its values are re-read from L2 one chunk later);
+// with two accumulator sets in tensor memory, the fold of chunk c-1
+// (tcgen05.ld -> 64-bit fixed point -> FP64 partial sum in shared memory)
+// overlaps the MMAs of chunk c.  Each CTA writes its FP64 partial Gram; a
+// second kernel adds the partials in a fixed order.
+constexpr int GC_K = 128;            // rows per exact chunk
+constexpr int GC_ST = GC_K / TC_KS;  // stages per chunk (8)
+constexpr int GC_STAGES = 2;         // shared-memory stage buffers
+constexpr int GC_NMAX = 32;          // W columns per CTA (MMA N)
+constexpr int GC_CE = TC_M + GC_NMAX;
 
-template <int GM, int GN>
-struct OgSmem {
-  __nv_bfloat16 vs[OZ_S][GM][OG_LD];  // [slice][col of V][row]
-  __nv_bfloat16 ws[OZ_S][GN][OG_LD];  // [slice][col of W][row]
-  int cexp[GM + GN];
-  double gsum[GM][GN];  // FP64 partial sums of this CTA
-};
+// width (MMA N) of W-column tile nt of the Gram
+__host__ __device__ __forceinline__ int gc_tile_n(int k2, int nt) {
+  const int rem = k2 - nt * GC_NMAX;
+  return rem >= GC_NMAX ? GC_NMAX : tc_round16(rem);
+}
 
-template <int GM, int GN>
-__global__ void __launch_bounds__(OZ_T, (GM <= 96 ? 2 : 1))
-    k_gram_oz(ColList<double> V, int k1, ColList<double> W, int k2, int n, int groups_n,
-              const double* __restrict__ wdiag, double* __restrict__ partial) {
-  constexpr int MT = GM / 16, NTN = GN / 8;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  OgSmem<GM, GN>& sm = *reinterpret_cast<OgSmem<GM, GN>*>(smraw);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = lane >> 2, tq = lane & 3;
-  const int gi = blockIdx.y / groups_n, gj = blockIdx.y % groups_n;
-  const int i0 = gi * GM, j0 = gj * GN;
-  const int mi = min(GM, k1 - i0), nj = min(GN, k2 - j0);
-  for (int e = tid; e < GM * GN; e += OZ_T) (&sm.gsum[0][0])[e] = 0.0;
-  const int nchunks = (n + OG_R - 1) / OG_R;
-  const int mt = warp;
-  const bool active = mt < MT && mt * 16 < mi;
-  const int ntiles = (nj + 7) / 8;
-  for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    const int r = ch * OG_R + lane;
-    __syncthreads();
-    // one warp per column (lane = row): all of the warp's loads are issued
-    // first, then each column is scaled by its chunk maximum and sliced
-    constexpr int CPW = (GM + GN + 7) / 8;  // columns per warp
-    double cv[CPW];
+__host__ __device__ __forceinline__ uint32_t tc_cols_pow2(int c) {
+  uint32_t p = 32;
+  while ((int)p < c) p <<= 1;
+  return p;
+}
+
+__device__ __forceinline__ int d8_prod_exp(int ew, int eb) {
+  if (ew >= 4096 || eb >= 4096) return 4096;
+  if (ew <= -2000 || eb <= -2000) return -2000;
+  return ew + eb;
+}
+
+// v[q] = p[r + q] for q < 4 (0 beyond n)
+template <bool VEC>
+__device__ __forceinline__ void gc_load4(const double* __restrict__ p, int r, int n, double* v) {
+  if (VEC && r + 4 <= n) {
+    const double2* p2 = reinterpret_cast<const double2*>(p + r);
+    const double2 t0 = __ldg(p2), t1 = __ldg(p2 + 1);
+    v[0] = t0.x;
+    v[1] = t0.y;
+    v[2] = t1.x;
+    v[3] = t1.y;
+  } else {
 #pragma unroll
-    for (int q = 0; q < CPW; q++) {
-      const int c = warp + 8 * q;
-      const bool isv = c < GM;
-      const int cc = isv ? c : c - GM;
-      const bool valid = c < GM + GN && (isv ? (cc < mi) : (cc < nj));
-      double v = 0.0;
-      if (valid && r < n) {
-        if (isv) v = __ldg(V.p[i0 + cc] + r);
-        else v = wdiag ? __ldg(wdiag + r) * __ldg(W.p[j0 + cc] + r) : __ldg(W.p[j0 + cc] + r);
-      }
-      cv[q] = v;
-    }
-#pragma unroll
-    for (int q = 0; q < CPW; q++) {
-      const int c = warp + 8 * q;
-      if (c >= GM + GN) break;
-      const bool isv = c < GM;
-      const int cc = isv ? c : c - GM;
-      const double v = cv[q];
-      int e = oz_exp(v);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-      if (lane == 0) sm.cexp[c] = e;
-      bool neg = false;
-      const uint64_t m = (e >= 4096) ? 0 : oz_m56(v, e, &neg);
-#pragma unroll
-      for (int a = 1; a <= OZ_S; a++) {
-        const __nv_bfloat16 sv = oz_slice(m, a, neg);
-        if (isv) sm.vs[a - 1][cc][lane] = sv;
-        else sm.ws[a - 1][cc][lane] = sv;
-      }
-    }
-    __syncthreads();
-    if (active) {
-      float acc[OZ_NL][NTN][4];
-#pragma unroll
-      for (int l = 0; l < OZ_NL; l++)
-#pragma unroll
-        for (int a = 0; a < NTN; a++)
-#pragma unroll
-          for (int b = 0; b < 4; b++) acc[l][a][b] = 0.f;
-#pragma unroll
-      for (int ks = 0; ks < OG_R; ks += 16) {
-        uint32_t af[OZ_S][4];
-#pragma unroll
-        for (int a = 0; a < OZ_S; a++) {
-          // A = V^T: row m = column of V, k = row of the chunk
-          const __nv_bfloat16* base = &sm.vs[a][mt * 16][ks];
-          af[a][0] = *reinterpret_cast<const uint32_t*>(base + g * OG_LD + tq * 2);
-          af[a][1] = *reinterpret_cast<const uint32_t*>(base + (g + 8) * OG_LD + tq * 2);
-          af[a][2] = *reinterpret_cast<const uint32_t*>(base + g * OG_LD + tq * 2 + 8);
-          af[a][3] = *reinterpret_cast<const uint32_t*>(base + (g + 8) * OG_LD + tq * 2 + 8);
-        }
-#pragma unroll
-        for (int b = 0; b < OZ_S; b++) {
-#pragma unroll
-          for (int nt = 0; nt < NTN; nt++) {
-            if (nt < ntiles) {
-              const __nv_bfloat16* bb = &sm.ws[b][nt * 8 + g][ks];
-              const uint32_t b0 = *reinterpret_cast<const uint32_t*>(bb + tq * 2);
-              const uint32_t b1 = *reinterpret_cast<const uint32_t*>(bb + tq * 2 + 8);
-#pragma unroll
-              for (int a = 0; a < OZ_S; a++)
-                if (a + b <= OZ_NL - 1) mma_bf16(acc[a + b][nt], af[a], b0, b1);
-            }
-          }
-        }
-      }
-      // exact chunk value -> FP64 partial sums
-#pragma unroll
-      for (int nt = 0; nt < NTN; nt++) {
-        if (nt >= ntiles) continue;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          int64_t T = 0;
-#pragma unroll
-          for (int l = 0; l < OZ_NL; l++) {
-            const int sh = 54 - 7 * (l + 2);
-            const int64_t v = (int64_t)__float2int_rn(acc[l][nt][q]);
-            T += (sh >= 0) ? v * ((int64_t)1 << sh) : (v >> (-sh));
-          }
-          const int ii = mt * 16 + g + ((q >= 2) ? 8 : 0);
-          const int jj = nt * 8 + tq * 2 + (q & 1);
-          if (ii < mi && jj < nj) {
-            const int ea = sm.cexp[ii], eb = sm.cexp[GM + jj];
-            double v;
-            if (ea >= 4096 || eb >= 4096) v = __longlong_as_double(0x7ff8000000000000ll);
-            else if (ea <= -2000 || eb <= -2000) v = 0.0;
-            else v = scalbn((double)T, ea + eb - 54);
-            sm.gsum[ii][jj] += v;
-          }
-        }
-      }
-    }
-  }
-  __syncthreads();
-  // partial layout [block][o], o = i + j*k1 (the flex-Gram reduction layout)
-  double* out = partial + (size_t)blockIdx.x * k1 * k2;
-  for (int e = tid; e < mi * nj; e += OZ_T) {
-    const int ii = e % mi, jj = e / mi;
-    out[(i0 + ii) + (size_t)(j0 + jj) * k1] = sm.gsum[ii][jj];
+    for (int q = 0; q < 4; q++) v[q] = (r + q < n) ? __ldg(p + r + q) : 0.0;
   }
 }
 
-template <int GM, int GN>
-int launch_gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
-                   const double* wdiag, double* partial, cudaStream_t st) {
-  const int groups_m = (k1 + GM - 1) / GM, groups_n = (k2 + GN - 1) / GN;
-  const int nchunks = (n + OG_R - 1) / OG_R;
-  const int per_sm = GM <= 96 ? 2 : 1;
+// A quad of the Gram tile: 4 consecutive rows of one column.  Per 16-row
+// stage a tile of ncolt = mi + nj columns has 4 * ncolt quads; quad u covers
+// half h = u & 1 of the core-matrix row of column col = (u >> 1) % ncolt in
+// K slab g = (u >> 1) / ncolt, i.e. rows 8 g + 4 h .. +3 of the stage, so
+// the two threads of a lane pair fill one 16-byte core-matrix row.
+struct GcQuad {
+  int col, roff, g, h;
+};
+__device__ __forceinline__ GcQuad gc_quad(int u, int ncolt) {
+  GcQuad q;
+  q.h = u & 1;
+  const int rest = u >> 1;
+  q.col = rest % ncolt;
+  q.g = rest / ncolt;
+  q.roff = q.g * 8 + q.h * 4;
+  return q;
+}
+
+// largest exponent of the 4 values of a quad (W values with the diagonal)
+template <bool VEC>
+__device__ __forceinline__ int gc_quad_exp(const double* __restrict__ p,
+                                           const double* __restrict__ wd, int r, int n) {
+  int e = -2000;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (r + q >= n) break;
+    const int ex = oz_exp_hi(ld_hi(p + r + q));
+    e = max(e, wd ? d8_prod_exp(ex, oz_exp_hi(ld_hi(wd + r + q))) : ex);
+  }
+  return e;
+}
+
+// exponents of one 16-row stage of a chunk into ce (atomicMax)
+template <bool VEC>
+__device__ __forceinline__ void gc_stage_exp(const ColList<double>& V, int i0, int mi,
+                                             const ColList<double>& W, int j0, int nj,
+                                             const double* __restrict__ wd, int row0, int n,
+                                             int* ce, int ufirst) {
+  const int ncolt = mi + nj;
+  for (int u = ufirst; u < 4 * ncolt; u += TC_T) {
+    const GcQuad q = gc_quad(u, ncolt);
+    const int r = row0 + q.roff;
+    if (r >= n) continue;
+    const bool isv = q.col < mi;
+    const int e = isv ? gc_quad_exp<VEC>(V.p[i0 + q.col], nullptr, r, n)
+                      : gc_quad_exp<VEC>(W.p[j0 + q.col - mi], wd, r, n);
+    if (e > -2000) atomicMax(ce + (isv ? q.col : TC_M + q.col - mi), e);
+  }
+}
+
+// Adds the exact chunk value held in tensor memory at tacc to output (i, j)
+// (slot j * TC_M + i); warp w reads lanes 32 (w % 4).. and column quarter
+// w / 4.  A chunk's levels combine into T = sum_L acc_L 2^{50-8L} (|T| <
+// 2^55 for 128 rows) worth T 2^{ea+eb-48}.  While the chunk exponent ea+eb
+// repeats, T is added to a 64-bit accumulator (exactly, until the sum would
+// overflow); when it changes the accumulator is rounded to FP64 and added to
+// gsum.  gexp holds the exponent of the accumulator (GC_NOEXP: empty).
+constexpr int GC_NOEXP = -1000000;
+
+__device__ __forceinline__ void gc_flush(long long* gT, int* gE, double* gs) {
+  if (*gT != 0) *gs += d8_to_double(*gT, *gE - 48);
+  *gT = 0;
+  *gE = GC_NOEXP;
+}
+
+__device__ __forceinline__ void gc_fold(uint32_t tacc, int N, int mi, int nj,
+                                        const int* __restrict__ ce, double* gsum, long long* gT,
+                                        int* gE) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q4 = warp & 3, cg = warp >> 2;
+  const int i = 32 * q4 + lane;
+  const int ea = ce[i];
+  const int quarter = N / 4;
+  for (int c0 = cg * quarter; c0 < (cg + 1) * quarter; c0 += 4) {
+    uint32_t acc[D8_NL][4];
+#pragma unroll
+    for (int l = 0; l < D8_NL; l++)
+      gcge::tc::tmem_ld4(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)(l * N + c0), acc[l]);
+    gcge::tc::tmem_wait_ld();
+#pragma unroll
+    for (int jj = 0; jj < 4; jj++) {
+      const int j = c0 + jj;
+      if (i >= mi || j >= nj) continue;
+      const int eb = ce[TC_M + j];
+      const int o = j * TC_M + i;
+      if (ea >= 4096 || eb >= 4096) {
+        gsum[o] = __longlong_as_double(0x7ff8000000000000ll);
+      } else if (ea > -2000 && eb > -2000) {
+        long long T = 0;
+#pragma unroll
+        for (int l = 0; l < D8_NL; l++) {
+          const long long v = (long long)__float2int_rn(__uint_as_float(acc[l][jj]));
+          const int sh = 50 - 8 * (l + 2);
+          T += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+        }
+        const int E = ea + eb;
+        long long t = gT[o];
+        const long long r = t + T;
+        if (gE[o] != E || ((t ^ r) & (T ^ r)) < 0) {
+          gc_flush(gT + o, gE + o, gsum + o);
+          gT[o] = T;
+          gE[o] = E;
+        } else {
+          gT[o] = r;
+        }
+      }
+    }
+  }
+  gcge::tc::fence_before();
+}
+
+size_t tc_gram_smem(int N) {
+  const int SB = (TC_ABYTES + D8_S * N * 32 + 1023) / 1024 * 1024;
+  size_t b = (size_t)GC_STAGES * SB + (size_t)TC_M * N * 20 + 3 * GC_CE * 4 + GC_STAGES * 8 + 16 +
+             1024;
+  // tensor memory: two CTAs per SM only when both fit in its 512 columns
+  const int nbuf = N <= 32 ? 2 : 1;
+  if (tc_cols_pow2(nbuf * D8_NL * N) > 256 && b < 118 * 1024) b = 118 * 1024;
+  return b;
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(TC_T, 2)
+    k_gram_tc(ColList<double> V, int k1, ColList<double> W, int k2, int n, int ntn,
+              const double* __restrict__ wd, double* __restrict__ partial, int nchunks) {
+  extern __shared__ __align__(1024) uint8_t smgc[];
+  const int tid = threadIdx.x;
+  const int mt = blockIdx.y / ntn, nt = blockIdx.y % ntn;
+  const int i0 = mt * TC_M, j0 = nt * GC_NMAX;
+  const int mi = min(TC_M, k1 - i0), N = gc_tile_n(k2, nt), nj = min(N, k2 - j0);
+  const int nbuf = N <= 32 ? 2 : 1;
+  const uint32_t ncols = tc_cols_pow2(nbuf * D8_NL * N);
+  const int BB = D8_S * N * 32;
+  const int SB = (TC_ABYTES + BB + 1023) / 1024 * 1024;
+  uint8_t* base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smgc) + 1023) & ~(uintptr_t)1023);
+  double* gsum = reinterpret_cast<double*>(base + GC_STAGES * SB);
+  long long* gT = reinterpret_cast<long long*>(gsum + TC_M * N);
+  int* gE = reinterpret_cast<int*>(gT + TC_M * N);
+  int* cexp = gE + TC_M * N;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(cexp + 3 * GC_CE);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + GC_STAGES);
+  const int nch = (nchunks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int ncolt = mi + nj;
+  const int nquads = 4 * ncolt;
+
+  if ((tid >> 5) == 0) gcge::tc::tmem_alloc(tslot, ncols);
+  if (tid == 0)
+    for (int s = 0; s < GC_STAGES; s++) gcge::tc::mbar_init(&mbar[s], 1);
+  for (int e = tid; e < TC_M * N; e += TC_T) {
+    gsum[e] = 0.0;
+    gT[e] = 0;
+    gE[e] = GC_NOEXP;
+  }
+  for (int e = tid; e < 3 * GC_CE; e += TC_T) cexp[e] = -2000;
+  gcge::tc::fence_before();
+  __syncthreads();
+  gcge::tc::fence_after();
+  const uint32_t tmem = *tslot;
+
+  // exponents of the first chunk
+  for (int st = 0; st < GC_ST; st++)
+    gc_stage_exp<VEC>(V, i0, mi, W, j0, nj, wd, (int)blockIdx.x * GC_K + st * TC_KS, n, cexp,
+                      tid);
+  __syncthreads();
+
+  // This thread's first quad runs through two register pipelines: the high
+  // words for the exponents of global stage g + 9 are loaded during stage g
+  // and folded into the exponent slots during stage g + 1 (so a chunk's
+  // exponents are complete one stage before its slicing starts), and the
+  // values of stage g + 1 are loaded during stage g.  Further quads of wide
+  // tiles run synchronously.
+  const bool has_u = tid < nquads;
+  const GcQuad uq = gc_quad(has_u ? tid : 0, ncolt);
+  const bool uisv = uq.col < mi;
+  const double* up = has_u ? (uisv ? V.p[i0 + uq.col] : W.p[j0 + uq.col - mi]) : nullptr;
+  const double* uwd = (has_u && !uisv) ? wd : nullptr;
+  const int uslot = uisv ? uq.col : TC_M + uq.col - mi;
+  auto stage_row = [&](int gs) {  // first row of this quad in global stage gs, -1 past the end
+    const int c = gs / GC_ST;
+    if (c >= nch) return -1;
+    return ((int)blockIdx.x + c * (int)gridDim.x) * GC_K + (gs % GC_ST) * TC_KS + uq.roff;
+  };
+  int xh[4], wh[4];
+  auto exp_issue = [&](int gs) {
+    const int r = has_u ? stage_row(gs) : -1;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const bool in = r >= 0 && r + q < n;
+      xh[q] = in ? ld_hi(up + r + q) : 0;
+      wh[q] = (in && uwd) ? ld_hi(uwd + r + q) : 0x3FE00000;  // 0.5 (exponent 0) without
+    }
+  };
+  // exponent of the quad from the raw 11-bit exponent fields: without the
+  // diagonal the largest field decides; with it the largest sum of fields of
+  // the nonzero products (a field of 0x7FF anywhere flags the quad non-finite)
+  auto exp_consume = [&](int* ce) {
+    int fmax = 0, bad = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int fx = (xh[q] >> 20) & 0x7FF, fw = (wh[q] >> 20) & 0x7FF;
+      bad |= (fx == 0x7FF) | (fw == 0x7FF);
+      // fw of 0.5 is 1022; a product at the bottom of the range still gets a field >= 1
+      const int f = (fx == 0 || fw == 0) ? 0 : max(fx + fw - 1022, 1);
+      fmax = max(fmax, f);
+    }
+    const int e = bad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
+    if (has_u && e > -2000) atomicMax(ce + uslot, e);
+  };
+  double sv[4];
+  auto slice_issue = [&](int gs) {
+    const int r = has_u ? stage_row(gs) : -1;
+    if (r < 0) return;
+    gc_load4<VEC>(up, r, n, sv);
+    if (uwd) {
+      double w[4];
+      gc_load4<VEC>(uwd, r, n, w);
+#pragma unroll
+      for (int q = 0; q < 4; q++) sv[q] *= w[q];
+    }
+  };
+  exp_issue(GC_ST);  // chunk 1, stage 0
+  slice_issue(0);
+
+  bool ok = true;
+  for (int c = 0; c < nch; c++) {
+    const int cb = (int)blockIdx.x + c * (int)gridDim.x;
+    const int* ce = cexp + (c % 3) * GC_CE;
+    int* ce_next = cexp + ((c + 1) % 3) * GC_CE;
+    const uint32_t tacc = tmem + (uint32_t)((c % nbuf) * D8_NL * N);
+    for (int st = 0; st < GC_ST; st++) {
+      const int g = c * GC_ST + st;
+      const int buf = g % GC_STAGES;
+      // exponents of global stage g + 8 (chunk c + 1) -> slots; issue g + 9
+      exp_consume(ce_next);
+      exp_issue(g + GC_ST + 1);
+      double v[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) v[q] = sv[q];
+      slice_issue(g + 1);
+      if (g >= GC_STAGES &&
+          !gcge::tc::mbar_wait_warp(&mbar[buf], ((g / GC_STAGES) - 1) & 1, TC_WAIT))
+        ok = false;
+      if (c > 0 && nbuf == 1 && st == 0) {
+        // one accumulator set: fold chunk c-1 before this chunk's first MMA
+        const int gl = g - 1;
+        if (!gcge::tc::mbar_wait_warp(&mbar[gl % GC_STAGES], (gl / GC_STAGES) & 1, TC_WAIT))
+          ok = false;
+        gcge::tc::fence_after();
+        gc_fold(tmem, N, mi, nj, cexp + ((c - 1) % 3) * GC_CE, gsum, gT, gE);
+      } else if (c > 0 && nbuf == 2 && st == GC_STAGES - 1) {
+        // the wait above covered the last stage of chunk c-1
+        gcge::tc::fence_after();
+        gc_fold(tmem + (uint32_t)(((c - 1) % 2) * D8_NL * N), N, mi, nj,
+                cexp + ((c - 1) % 3) * GC_CE, gsum, gT, gE);
+      }
+      uint8_t* As = base + buf * SB;
+      uint8_t* Bs = As + TC_ABYTES;
+      const int row0 = cb * GC_K + st * TC_KS;
+      for (int u = tid; u < nquads; u += TC_T) {
+        const GcQuad q = (u == tid) ? uq : gc_quad(u, ncolt);
+        const int r = row0 + q.roff;
+        const bool isv = q.col < mi;
+        if (u != tid) {  // a further quad: load now
+          if (isv) {
+            gc_load4<VEC>(V.p[i0 + q.col], r, n, v);
+          } else {
+            gc_load4<VEC>(W.p[j0 + q.col - mi], r, n, v);
+            if (wd) {
+              double w[4];
+              gc_load4<VEC>(wd, r, n, w);
+#pragma unroll
+              for (int t = 0; t < 4; t++) v[t] *= w[t];
+            }
+          }
+        }
+        const int E0 = ce[isv ? q.col : TC_M + q.col - mi];
+        int E[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          E[t] = E0;
+          if (E0 >= 4096) v[t] = 0.0;
+        }
+        const int cc = isv ? q.col : q.col - mi;
+        uint8_t* dst = (isv ? As + q.g * (TC_M / 8 * 128) : Bs + q.g * (D8_S * N * 16)) +
+                       (cc >> 3) * 128 + (cc & 7) * 16 + q.h * 8;
+        d8_slice4(v, E, dst, isv ? TC_M * TC_KS * 2 : N * 16);
+      }
+      // further quads: exponents of chunk c + 1 now
+      if (c + 1 < nch && nquads > TC_T)
+        gc_stage_exp<VEC>(V, i0, mi, W, j0, nj, wd, (cb + (int)gridDim.x) * GC_K + st * TC_KS, n,
+                          ce_next, tid + TC_T);
+      if (st == GC_ST - 1)  // slots of chunk c+2 (last read by the fold of chunk c-1)
+        for (int e = tid; e < GC_CE; e += TC_T) cexp[((c + 2) % 3) * GC_CE + e] = -2000;
+      gcge::tc::fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        gcge::tc::fence_after();
+        d8_issue(tacc, gcge::tc::smem_u32(As), TC_M * TC_KS * 2, gcge::tc::smem_u32(Bs), N,
+                 st == 0);
+        gcge::tc::commit(&mbar[buf]);
+      }
+    }
+  }
+  if (nch > 0) {
+    const int gl = nch * GC_ST - 1;
+    if (!gcge::tc::mbar_wait_warp(&mbar[gl % GC_STAGES], (gl / GC_STAGES) & 1, TC_WAIT))
+      ok = false;
+    gcge::tc::fence_after();
+    gc_fold(tmem + (uint32_t)(((nch - 1) % nbuf) * D8_NL * N), N, mi, nj,
+            cexp + ((nch - 1) % 3) * GC_CE, gsum, gT, gE);
+  }
+  __syncthreads();
+  for (int e = tid; e < TC_M * N; e += TC_T) gc_flush(gT + e, gE + e, gsum + e);
+  const int anybad = __syncthreads_or(ok ? 0 : 1);
+  if (anybad && tid == 0) atomicExch(&g_oz_tc_status, 1);
+  // partial layout [block][o], o = i + j*k1 (the flex-Gram reduction layout)
+  double* out = partial + (size_t)blockIdx.x * k1 * k2;
+  for (int e = tid; e < mi * nj; e += TC_T) {
+    const int ii = e % mi, jj = e / mi;
+    out[(i0 + ii) + (size_t)(j0 + jj) * k1] =
+        anybad ? __longlong_as_double(0x7ff8000000000000ll) : gsum[(size_t)jj * TC_M + ii];
+  }
+  gcge::tc::fence_before();
+  __syncthreads();
+  if ((tid >> 5) == 0) {
+    gcge::tc::fence_after();
+    gcge::tc::tmem_dealloc(tmem, ncols);
+  }
+}
+
+template <bool VEC>
+int launch_gram_tc(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
+                   const double* wd, double* partial, cudaStream_t st) {
+  const int ntm = (k1 + TC_M - 1) / TC_M, ntn = (k2 + GC_NMAX - 1) / GC_NMAX;
+  const int nchunks = (n + GC_K - 1) / GC_K;
+  const int N0 = gc_tile_n(k2, 0);
+  const size_t sm = tc_gram_smem(N0);
+  const int per_sm = (227 * 1024) / (int)(sm + 1024) >= 2 ? 2 : 1;
   const int nblk = nchunks < 152 * per_sm ? nchunks : 152 * per_sm;
-  const size_t sm = sizeof(OgSmem<GM, GN>);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_gram_oz<GM, GN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_gram_tc<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc_gram_smem(GC_NMAX));
     attr = true;
   }
-  k_gram_oz<GM, GN><<<dim3(nblk, groups_m * groups_n), OZ_T, sm, st>>>(V, k1, W, k2, n, groups_n,
-                                                                       wdiag, partial);
+  k_gram_tc<VEC><<<dim3(nblk, ntm * ntn), TC_T, sm, st>>>(V, k1, W, k2, n, ntn, wd, partial,
+                                                          nchunks);
   return nblk;
 }
 
@@ -668,14 +917,17 @@ size_t gram_oz_partial_doubles(int k1, int k2) {
   return (size_t)304 * k1 * k2;
 }
 
-// G = V^T W (k1 x k2) into partial (gram_oz_partial_doubles) then G (ldg);
-// sym: only the upper triangle is kept and mirrored.
+// G = V^T diag(wd) W (k1 x k2, ldg) through per-CTA partials (partial holds
+// gram_oz_partial_doubles(k1, k2) doubles); sym: only the upper triangle is
+// kept and mirrored.
 void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n, double* G,
              int ldg, bool sym, double* partial, cudaStream_t st, const double* wdiag) {
   if (k1 <= 0 || k2 <= 0 || n <= 0) return;
-  int nblk;
-  if (k1 <= 96 && k2 <= 16) nblk = launch_gram_oz<96, 16>(V, k1, W, k2, n, wdiag, partial, st);
-  else nblk = launch_gram_oz<128, 32>(V, k1, W, k2, n, wdiag, partial, st);
+  bool vec = ((uintptr_t)wdiag & 15) == 0;
+  for (int i = 0; i < k1; i++) vec = vec && ((uintptr_t)V.p[i] & 15) == 0;
+  for (int j = 0; j < k2; j++) vec = vec && ((uintptr_t)W.p[j] & 15) == 0;
+  const int nblk = vec ? launch_gram_tc<true>(V, k1, W, k2, n, wdiag, partial, st)
+                       : launch_gram_tc<false>(V, k1, W, k2, n, wdiag, partial, st);
   gram_reduce_partials(k1, k2, nblk, sym, partial, G, ldg, st);
 }
 

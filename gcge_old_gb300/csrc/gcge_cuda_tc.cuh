@@ -73,6 +73,26 @@ __device__ __forceinline__ uint32_t mbar_wait(uint64_t* mbar, uint32_t parity, i
   return done;
 }
 
+// Warp-wide wait: lane 0 polls (sleeping between polls, at most `limit`
+// polls), the warp then continues together.  Returns 0 when it gave up.
+__device__ __forceinline__ uint32_t mbar_wait_warp(uint64_t* mbar, uint32_t parity, int limit) {
+  uint32_t done = 0;
+  if ((threadIdx.x & 31) == 0) {
+    for (int it = 0; it < limit && !done; it++) {
+      asm volatile(
+          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+          "selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(done)
+          : "r"(smem_u32(mbar)), "r"(parity)
+          : "memory");
+      if (!done) __nanosleep(64);
+    }
+  }
+  done = __shfl_sync(0xffffffffu, done, 0);
+  __syncwarp();
+  return done;
+}
+
 __device__ __forceinline__ void fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -103,6 +123,12 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
                  "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+// warp-wide: 4 consecutive FP32 columns (valid after tmem_wait_ld())
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_wait_ld() {
