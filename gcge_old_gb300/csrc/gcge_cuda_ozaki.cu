@@ -445,63 +445,55 @@ size_t tc_lincomb_smem(int N) {
   return (size_t)TC_STAGES * SB + 1024 /* alignment */ + TC_M * 4 + TC_STAGES * 8 + 16;
 }
 // ---------------------------------------------------------------- tcgen05 Gram
-// G = V^T diag(wd) W (wd NULL: identity) with FP64 accuracy.  One CTA owns up
-// to 128 columns of V (MMA M, TMEM lane = column of V) and up to 32 columns
-// of W (MMA N) over a strided set of 128-row chunks.  In a chunk every column
-// has one power-of-two scale (its largest |value| over the chunk, a W column
-// taken with the diagonal applied), the 7 balanced base-256 digits of the
-// lincomb are used, and the 8 level sums over the chunk's 128 rows are exact
-// in FP32 tensor memory.  The column exponents of chunk c+1 are gathered
-// while chunk c is sliced (its values are re-read from L2 one chunk later);
-// with two accumulator sets in tensor memory, the fold of chunk c-1
-// (tcgen05.ld -> 64-bit fixed point -> FP64 partial sum in shared memory)
-// overlaps the MMAs of chunk c.  Each CTA writes its FP64 partial Gram; a
-// second kernel adds the partials in a fixed order.
-constexpr int GC_K = 128;            // rows per exact chunk
-constexpr int GC_ST = GC_K / TC_KS;  // stages per chunk (8)
-constexpr int GC_STAGES = 2;         // shared-memory stage buffers
-constexpr int GC_NMAX = 32;          // W columns per CTA (MMA N)
-constexpr int GC_CE = TC_M + GC_NMAX;
+// G = V^T diag(wd) W (wd NULL: identity) with FP64 accuracy.  One CTA per SM
+// owns up to GC_MI columns of V (MMA M, TMEM lane = column of V) and 16
+// columns of W (MMA N) over a strided set of 64-row chunks.  Its warps have
+// fixed roles and hand work over through mbarriers (no block-wide barrier in
+// the loop):
+//  * producer/MMA warp: streams each chunk's columns (and the diagonal) into
+//    a ring of raw FP64 buffers in shared memory with cp.async.bulk, and for
+//    every 16-row stage issues the skewed digit MMAs into the chunk's 8 level
+//    accumulators in tensor memory (two accumulator sets alternate);
+//  * 12 slicer warps: per chunk the column scales (largest exponent over the
+//    chunk's 64 rows, a W column taken with the diagonal; a warp max of the
+//    raw exponent fields), then per stage the 7 balanced base-256 digits of
+//    every value into a double-buffered stage in shared memory;
+//  * 4 fold warps (one per TMEM lane quadrant): per chunk, the exact level
+//    sums (FP32, below 2^24 for 64 rows) combined in 32-bit pairs into a
+//    64-bit fixed-point value, added to a 64-bit accumulator per output that
+//    is rounded into an FP64 partial sum only when the chunk exponent changes
+//    (or the integer sum would overflow).
+// Each CTA writes its FP64 partial Gram; a second kernel adds the partials in
+// a fixed order.
+constexpr int GC_K = 64;                 // rows per exact chunk
+constexpr int GC_ST = GC_K / TC_KS;      // stages per chunk (4)
+constexpr int GC_N = 16;                 // W columns per CTA
+constexpr int GC_MI = 96;                // V columns per CTA
+constexpr int GC_SW = 12;                // slicer warps
+constexpr int GC_FW = 4;                 // fold warps
+constexpr int GC_THREADS = (GC_SW + GC_FW + 1) * 32;
+constexpr int GC_PW = GC_SW + GC_FW;     // producer/MMA warp
+constexpr int GC_RAWLD = GC_K * 8 + 16;  // bytes per raw column (padded: conflict-free reads)
+constexpr int GC_MAXRAW = 3;
+constexpr int GC_CE = TC_M + GC_N;       // exponent slots: V columns, then W columns
+constexpr int GC_SB = (TC_ABYTES + D8_S * GC_N * 32 + 1023) / 1024 * 1024;  // stage bytes
+constexpr int GC_FOLDB = TC_M * GC_N * 20;  // fold state: FP64 sum, 64-bit value, exponent
+constexpr int GC_FIXED = 1024 + 3 * GC_CE * 4 + (8 + GC_MAXRAW) * 8 + 16;
+constexpr int GC_SMEM_CAP = 227 * 1024;
 
-// width (MMA N) of W-column tile nt of the Gram
-__host__ __device__ __forceinline__ int gc_tile_n(int k2, int nt) {
-  const int rem = k2 - nt * GC_NMAX;
-  return rem >= GC_NMAX ? GC_NMAX : tc_round16(rem);
+__host__ __device__ __forceinline__ int gc_nraw(int rawcols) {
+  const int room = GC_SMEM_CAP - 2 * GC_SB - GC_FOLDB - GC_FIXED;
+  const int k = room / (rawcols * GC_RAWLD);
+  return k < GC_MAXRAW ? k : GC_MAXRAW;
+}
+size_t gc_smem(int rawcols) {
+  return (size_t)2 * GC_SB + GC_FOLDB + GC_FIXED + (size_t)gc_nraw(rawcols) * rawcols * GC_RAWLD;
 }
 
-__host__ __device__ __forceinline__ uint32_t tc_cols_pow2(int c) {
-  uint32_t p = 32;
-  while ((int)p < c) p <<= 1;
-  return p;
-}
-
-__device__ __forceinline__ int d8_prod_exp(int ew, int eb) {
-  if (ew >= 4096 || eb >= 4096) return 4096;
-  if (ew <= -2000 || eb <= -2000) return -2000;
-  return ew + eb;
-}
-
-// v[q] = p[r + q] for q < 4 (0 beyond n)
-template <bool VEC>
-__device__ __forceinline__ void gc_load4(const double* __restrict__ p, int r, int n, double* v) {
-  if (VEC && r + 4 <= n) {
-    const double2* p2 = reinterpret_cast<const double2*>(p + r);
-    const double2 t0 = __ldg(p2), t1 = __ldg(p2 + 1);
-    v[0] = t0.x;
-    v[1] = t0.y;
-    v[2] = t1.x;
-    v[3] = t1.y;
-  } else {
-#pragma unroll
-    for (int q = 0; q < 4; q++) v[q] = (r + q < n) ? __ldg(p + r + q) : 0.0;
-  }
-}
-
-// A quad of the Gram tile: 4 consecutive rows of one column.  Per 16-row
-// stage a tile of ncolt = mi + nj columns has 4 * ncolt quads; quad u covers
-// half h = u & 1 of the core-matrix row of column col = (u >> 1) % ncolt in
-// K slab g = (u >> 1) / ncolt, i.e. rows 8 g + 4 h .. +3 of the stage, so
-// the two threads of a lane pair fill one 16-byte core-matrix row.
+// A quad: 4 consecutive rows of one column of a 16-row stage.  A tile of
+// ncolt columns has 4 * ncolt quads per stage; quad u is half h = u & 1 of
+// the core-matrix row of column (u >> 1) % ncolt in K slab g = (u >> 1) /
+// ncolt (rows 8 g + 4 h .. +3), so a lane pair fills one 16-byte row.
 struct GcQuad {
   int col, roff, g, h;
 };
@@ -515,336 +507,274 @@ __device__ __forceinline__ GcQuad gc_quad(int u, int ncolt) {
   return q;
 }
 
-// largest exponent of the 4 values of a quad (W values with the diagonal)
-template <bool VEC>
-__device__ __forceinline__ int gc_quad_exp(const double* __restrict__ p,
-                                           const double* __restrict__ wd, int r, int n) {
-  int e = -2000;
-#pragma unroll
-  for (int q = 0; q < 4; q++) {
-    if (r + q >= n) break;
-    const int ex = oz_exp_hi(ld_hi(p + r + q));
-    e = max(e, wd ? d8_prod_exp(ex, oz_exp_hi(ld_hi(wd + r + q))) : ex);
-  }
-  return e;
-}
-
-// exponents of one 16-row stage of a chunk into ce (atomicMax)
-template <bool VEC>
-__device__ __forceinline__ void gc_stage_exp(const ColList<double>& V, int i0, int mi,
-                                             const ColList<double>& W, int j0, int nj,
-                                             const double* __restrict__ wd, int row0, int n,
-                                             int* ce, int ufirst) {
-  const int ncolt = mi + nj;
-  for (int u = ufirst; u < 4 * ncolt; u += TC_T) {
-    const GcQuad q = gc_quad(u, ncolt);
-    const int r = row0 + q.roff;
-    if (r >= n) continue;
-    const bool isv = q.col < mi;
-    const int e = isv ? gc_quad_exp<VEC>(V.p[i0 + q.col], nullptr, r, n)
-                      : gc_quad_exp<VEC>(W.p[j0 + q.col - mi], wd, r, n);
-    if (e > -2000) atomicMax(ce + (isv ? q.col : TC_M + q.col - mi), e);
-  }
-}
-
-// Adds the exact chunk value held in tensor memory at tacc to output (i, j)
-// (slot j * TC_M + i); warp w reads lanes 32 (w % 4).. and column quarter
-// w / 4.  A chunk's levels combine into T = sum_L acc_L 2^{50-8L} (|T| <
-// 2^55 for 128 rows) worth T 2^{ea+eb-48}.  While the chunk exponent ea+eb
-// repeats, T is added to a 64-bit accumulator (exactly, until the sum would
-// overflow); when it changes the accumulator is rounded to FP64 and added to
-// gsum.  gexp holds the exponent of the accumulator (GC_NOEXP: empty).
-constexpr int GC_NOEXP = -1000000;
-
-__device__ __forceinline__ void gc_flush(long long* gT, int* gE, double* gs) {
-  if (*gT != 0) *gs += d8_to_double(*gT, *gE - 48);
+__device__ __forceinline__ void gc_flush(long long* gT, int* gE, double* gS) {
+  if (*gT != 0) *gS += d8_to_double(*gT, *gE - 48);
   *gT = 0;
-  *gE = GC_NOEXP;
+  *gE = -1000000;
 }
 
-__device__ __forceinline__ void gc_fold(uint32_t tacc, int N, int mi, int nj,
-                                        const int* __restrict__ ce, double* gsum, long long* gT,
-                                        int* gE) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q4 = warp & 3, cg = warp >> 2;
-  const int i = 32 * q4 + lane;
-  const int ea = ce[i];
-  const int quarter = N / 4;
-  for (int c0 = cg * quarter; c0 < (cg + 1) * quarter; c0 += 4) {
-    uint32_t acc[D8_NL][4];
-#pragma unroll
-    for (int l = 0; l < D8_NL; l++)
-      gcge::tc::tmem_ld4(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)(l * N + c0), acc[l]);
-    gcge::tc::tmem_wait_ld();
-#pragma unroll
-    for (int jj = 0; jj < 4; jj++) {
-      const int j = c0 + jj;
-      if (i >= mi || j >= nj) continue;
-      const int eb = ce[TC_M + j];
-      const int o = j * TC_M + i;
-      if (ea >= 4096 || eb >= 4096) {
-        gsum[o] = __longlong_as_double(0x7ff8000000000000ll);
-      } else if (ea > -2000 && eb > -2000) {
-        long long T = 0;
-#pragma unroll
-        for (int l = 0; l < D8_NL; l++) {
-          const long long v = (long long)__float2int_rn(__uint_as_float(acc[l][jj]));
-          const int sh = 50 - 8 * (l + 2);
-          T += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
-        }
-        const int E = ea + eb;
-        long long t = gT[o];
-        const long long r = t + T;
-        if (gE[o] != E || ((t ^ r) & (T ^ r)) < 0) {
-          gc_flush(gT + o, gE + o, gsum + o);
-          gT[o] = T;
-          gE[o] = E;
-        } else {
-          gT[o] = r;
-        }
-      }
-    }
-  }
-  gcge::tc::fence_before();
-}
-
-size_t tc_gram_smem(int N) {
-  const int SB = (TC_ABYTES + D8_S * N * 32 + 1023) / 1024 * 1024;
-  size_t b = (size_t)GC_STAGES * SB + (size_t)TC_M * N * 20 + 3 * GC_CE * 4 + GC_STAGES * 8 + 16 +
-             1024;
-  // tensor memory: two CTAs per SM only when both fit in its 512 columns
-  const int nbuf = N <= 32 ? 2 : 1;
-  if (tc_cols_pow2(nbuf * D8_NL * N) > 256 && b < 118 * 1024) b = 118 * 1024;
-  return b;
-}
-
-template <bool VEC>
-__global__ void __launch_bounds__(TC_T, 2)
+template <bool BULK>
+__global__ void __launch_bounds__(GC_THREADS, 1)
     k_gram_tc(ColList<double> V, int k1, ColList<double> W, int k2, int n, int ntn,
-              const double* __restrict__ wd, double* __restrict__ partial, int nchunks) {
+              const double* __restrict__ wd, double* __restrict__ partial, int nchunks,
+              int nraw) {
   extern __shared__ __align__(1024) uint8_t smgc[];
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int mt = blockIdx.y / ntn, nt = blockIdx.y % ntn;
-  const int i0 = mt * TC_M, j0 = nt * GC_NMAX;
-  const int mi = min(TC_M, k1 - i0), N = gc_tile_n(k2, nt), nj = min(N, k2 - j0);
-  const int nbuf = N <= 32 ? 2 : 1;
-  const uint32_t ncols = tc_cols_pow2(nbuf * D8_NL * N);
-  const int BB = D8_S * N * 32;
-  const int SB = (TC_ABYTES + BB + 1023) / 1024 * 1024;
+  const int i0 = mt * GC_MI, j0 = nt * GC_N;
+  const int mi = min(GC_MI, k1 - i0), nj = min(GC_N, k2 - j0);
+  const int ncolt = mi + nj;
+  const int rawcols = ncolt + (wd ? 1 : 0);
+  const int RC = rawcols * GC_RAWLD;
+  constexpr uint32_t ncols = 2 * D8_NL * GC_N;  // two sets of 8 levels (256)
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smgc) + 1023) & ~(uintptr_t)1023);
-  double* gsum = reinterpret_cast<double*>(base + GC_STAGES * SB);
-  long long* gT = reinterpret_cast<long long*>(gsum + TC_M * N);
-  int* gE = reinterpret_cast<int*>(gT + TC_M * N);
-  int* cexp = gE + TC_M * N;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(cexp + 3 * GC_CE);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + GC_STAGES);
+  double* gS = reinterpret_cast<double*>(base + 2 * GC_SB);
+  long long* gT = reinterpret_cast<long long*>(gS + TC_M * GC_N);
+  int* gE = reinterpret_cast<int*>(gT + TC_M * GC_N);
+  uint8_t* rawbase = reinterpret_cast<uint8_t*>(gE + TC_M * GC_N);
+  int* cex = reinterpret_cast<int*>(rawbase + nraw * RC);
+  uint64_t* mfull = reinterpret_cast<uint64_t*>(cex + 3 * GC_CE);  // stage digits ready (2)
+  uint64_t* mempty = mfull + 2;   // stage MMAs done (2)
+  uint64_t* maccf = mfull + 4;    // chunk accumulators complete (2)
+  uint64_t* macce = mfull + 6;    // chunk accumulators folded (2)
+  uint64_t* mraw = mfull + 8;     // raw chunk arrived (nraw)
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mraw + GC_MAXRAW);
   const int nch = (nchunks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int ncolt = mi + nj;
-  const int nquads = 4 * ncolt;
+  auto colptr = [&](int col) -> const double* {
+    return col < mi ? V.p[i0 + col] : (col < ncolt ? W.p[j0 + col - mi] : wd);
+  };
 
-  if ((tid >> 5) == 0) gcge::tc::tmem_alloc(tslot, ncols);
-  if (tid == 0)
-    for (int s = 0; s < GC_STAGES; s++) gcge::tc::mbar_init(&mbar[s], 1);
-  for (int e = tid; e < TC_M * N; e += TC_T) {
-    gsum[e] = 0.0;
-    gT[e] = 0;
-    gE[e] = GC_NOEXP;
+  if (warp == 0) gcge::tc::tmem_alloc(tslot, ncols);
+  if (tid == 0) {
+    for (int b = 0; b < 2; b++) {
+      gcge::tc::mbar_init(&mfull[b], GC_SW);
+      gcge::tc::mbar_init(&mempty[b], 1);
+      gcge::tc::mbar_init(&maccf[b], 1);
+      gcge::tc::mbar_init(&macce[b], GC_FW);
+    }
+    for (int b = 0; b < nraw; b++) gcge::tc::mbar_init(&mraw[b], 1);
   }
-  for (int e = tid; e < 3 * GC_CE; e += TC_T) cexp[e] = -2000;
+  for (int e = tid; e < TC_M * GC_N; e += GC_THREADS) {
+    gS[e] = 0.0;
+    gT[e] = 0;
+    gE[e] = -1000000;
+  }
   gcge::tc::fence_before();
   __syncthreads();
   gcge::tc::fence_after();
   const uint32_t tmem = *tslot;
-
-  // exponents of the first chunk
-  for (int st = 0; st < GC_ST; st++)
-    gc_stage_exp<VEC>(V, i0, mi, W, j0, nj, wd, (int)blockIdx.x * GC_K + st * TC_KS, n, cexp,
-                      tid);
-  __syncthreads();
-
-  // This thread's first quad runs through two register pipelines: the high
-  // words for the exponents of global stage g + 9 are loaded during stage g
-  // and folded into the exponent slots during stage g + 1 (so a chunk's
-  // exponents are complete one stage before its slicing starts), and the
-  // values of stage g + 1 are loaded during stage g.  Further quads of wide
-  // tiles run synchronously.
-  const bool has_u = tid < nquads;
-  const GcQuad uq = gc_quad(has_u ? tid : 0, ncolt);
-  const bool uisv = uq.col < mi;
-  const double* up = has_u ? (uisv ? V.p[i0 + uq.col] : W.p[j0 + uq.col - mi]) : nullptr;
-  const double* uwd = (has_u && !uisv) ? wd : nullptr;
-  const int uslot = uisv ? uq.col : TC_M + uq.col - mi;
-  auto stage_row = [&](int gs) {  // first row of this quad in global stage gs, -1 past the end
-    const int c = gs / GC_ST;
-    if (c >= nch) return -1;
-    return ((int)blockIdx.x + c * (int)gridDim.x) * GC_K + (gs % GC_ST) * TC_KS + uq.roff;
-  };
-  int xh[4], wh[4];
-  auto exp_issue = [&](int gs) {
-    const int r = has_u ? stage_row(gs) : -1;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const bool in = r >= 0 && r + q < n;
-      xh[q] = in ? ld_hi(up + r + q) : 0;
-      wh[q] = (in && uwd) ? ld_hi(uwd + r + q) : 0x3FE00000;  // 0.5 (exponent 0) without
-    }
-  };
-  // exponent of the quad from the raw 11-bit exponent fields: without the
-  // diagonal the largest field decides; with it the largest sum of fields of
-  // the nonzero products (a field of 0x7FF anywhere flags the quad non-finite)
-  auto exp_consume = [&](int* ce) {
-    int fmax = 0, bad = 0;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int fx = (xh[q] >> 20) & 0x7FF, fw = (wh[q] >> 20) & 0x7FF;
-      bad |= (fx == 0x7FF) | (fw == 0x7FF);
-      // fw of 0.5 is 1022; a product at the bottom of the range still gets a field >= 1
-      const int f = (fx == 0 || fw == 0) ? 0 : max(fx + fw - 1022, 1);
-      fmax = max(fmax, f);
-    }
-    const int e = bad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
-    if (has_u && e > -2000) atomicMax(ce + uslot, e);
-  };
-  double sv[4];
-  auto slice_issue = [&](int gs) {
-    const int r = has_u ? stage_row(gs) : -1;
-    if (r < 0) return;
-    gc_load4<VEC>(up, r, n, sv);
-    if (uwd) {
-      double w[4];
-      gc_load4<VEC>(uwd, r, n, w);
-#pragma unroll
-      for (int q = 0; q < 4; q++) sv[q] *= w[q];
-    }
-  };
-  exp_issue(GC_ST);  // chunk 1, stage 0
-  slice_issue(0);
-
   bool ok = true;
-  for (int c = 0; c < nch; c++) {
-    const int cb = (int)blockIdx.x + c * (int)gridDim.x;
-    const int* ce = cexp + (c % 3) * GC_CE;
-    int* ce_next = cexp + ((c + 1) % 3) * GC_CE;
-    const uint32_t tacc = tmem + (uint32_t)((c % nbuf) * D8_NL * N);
-    for (int st = 0; st < GC_ST; st++) {
-      const int g = c * GC_ST + st;
-      const int buf = g % GC_STAGES;
-      // exponents of global stage g + 8 (chunk c + 1) -> slots; issue g + 9
-      exp_consume(ce_next);
-      exp_issue(g + GC_ST + 1);
-      double v[4];
-#pragma unroll
-      for (int q = 0; q < 4; q++) v[q] = sv[q];
-      slice_issue(g + 1);
-      if (g >= GC_STAGES &&
-          !gcge::tc::mbar_wait_warp(&mbar[buf], ((g / GC_STAGES) - 1) & 1, TC_WAIT))
-        ok = false;
-      if (c > 0 && nbuf == 1 && st == 0) {
-        // one accumulator set: fold chunk c-1 before this chunk's first MMA
-        const int gl = g - 1;
-        if (!gcge::tc::mbar_wait_warp(&mbar[gl % GC_STAGES], (gl / GC_STAGES) & 1, TC_WAIT))
-          ok = false;
-        gcge::tc::fence_after();
-        gc_fold(tmem, N, mi, nj, cexp + ((c - 1) % 3) * GC_CE, gsum, gT, gE);
-      } else if (c > 0 && nbuf == 2 && st == GC_STAGES - 1) {
-        // the wait above covered the last stage of chunk c-1
-        gcge::tc::fence_after();
-        gc_fold(tmem + (uint32_t)(((c - 1) % 2) * D8_NL * N), N, mi, nj,
-                cexp + ((c - 1) % 3) * GC_CE, gsum, gT, gE);
+
+  if (warp == GC_PW) {
+    // ------------------------------------------------ producer / MMA warp
+    auto issue_raw = [&](int cc) {
+      const int row0 = ((int)blockIdx.x + cc * (int)gridDim.x) * GC_K;
+      const int valid = min(GC_K, n - row0);
+      const int rows = BULK ? (valid & ~1) : 0;
+      uint64_t* mb = &mraw[cc % nraw];
+      if (lane == 0) gcge::tc::mbar_arrive_expect_tx(mb, (uint32_t)(rawcols * rows * 8));
+      __syncwarp();
+      if (rows > 0) {
+        uint8_t* dst = rawbase + (cc % nraw) * RC;
+        for (int col = lane; col < rawcols; col += 32)
+          gcge::tc::bulk_g2s(dst + col * GC_RAWLD, colptr(col) + row0, (uint32_t)(rows * 8), mb);
       }
-      uint8_t* As = base + buf * SB;
-      uint8_t* Bs = As + TC_ABYTES;
-      const int row0 = cb * GC_K + st * TC_KS;
-      for (int u = tid; u < nquads; u += TC_T) {
-        const GcQuad q = (u == tid) ? uq : gc_quad(u, ncolt);
-        const int r = row0 + q.roff;
-        const bool isv = q.col < mi;
-        if (u != tid) {  // a further quad: load now
-          if (isv) {
-            gc_load4<VEC>(V.p[i0 + q.col], r, n, v);
-          } else {
-            gc_load4<VEC>(W.p[j0 + q.col - mi], r, n, v);
-            if (wd) {
-              double w[4];
-              gc_load4<VEC>(wd, r, n, w);
+    };
+    for (int cc = 0; cc < nraw && cc < nch; cc++) issue_raw(cc);
+    for (int c = 0; c < nch; c++) {
+      const int tb = c & 1;
+      if (c >= 2 && !gcge::tc::mbar_wait_warp(&macce[tb], ((c >> 1) - 1) & 1, TC_WAIT)) ok = false;
+      for (int st = 0; st < GC_ST; st++) {
+        const int g = c * GC_ST + st, buf = g & 1;
+        if (!gcge::tc::mbar_wait_warp(&mfull[buf], (g >> 1) & 1, TC_WAIT)) ok = false;
+        if (lane == 0) {
+          gcge::tc::fence_after();
+          uint8_t* As = base + buf * GC_SB;
+          d8_issue(tmem + (uint32_t)(tb * D8_NL * GC_N), gcge::tc::smem_u32(As),
+                   TC_M * TC_KS * 2, gcge::tc::smem_u32(As + TC_ABYTES), GC_N, st == 0);
+          gcge::tc::commit(&mempty[buf]);
+          if (st == GC_ST - 1) gcge::tc::commit(&maccf[tb]);
+        }
+        __syncwarp();
+      }
+      // every slicer has cut chunk c: its raw buffer can be refilled
+      if (c + nraw < nch) issue_raw(c + nraw);
+    }
+  } else if (warp >= GC_SW) {
+    // ------------------------------------------------ fold warps
+    const int q4 = warp - GC_SW;
+    const int i = 32 * q4 + lane;
+    for (int c = 0; c < nch; c++) {
+      const int tb = c & 1;
+      if (!gcge::tc::mbar_wait_warp(&maccf[tb], (c >> 1) & 1, TC_WAIT)) ok = false;
+      gcge::tc::fence_after();
+      if (32 * q4 < mi) {
+        const int* ce = cex + (c % 3) * GC_CE;
+        const int ea = ce[i];
+        const uint32_t tacc = tmem + (uint32_t)(tb * D8_NL * GC_N) + ((uint32_t)(32 * q4) << 16);
 #pragma unroll
-              for (int t = 0; t < 4; t++) v[t] *= w[t];
+        for (int c0 = 0; c0 < GC_N; c0 += 4) {
+          uint32_t acc[D8_NL][4];
+#pragma unroll
+          for (int l = 0; l < D8_NL; l++)
+            gcge::tc::tmem_ld4(tacc + (uint32_t)(l * GC_N + c0), acc[l]);
+          gcge::tc::tmem_wait_ld();
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) {
+            const int j = c0 + jj;
+            if (i >= mi || j >= nj) continue;
+            const int eb = ce[TC_M + j];
+            const int o = j * TC_M + i;
+            if (ea >= 4096 || eb >= 4096) {
+              gS[o] = __longlong_as_double(0x7ff8000000000000ll);
+            } else if (ea > -2000 && eb > -2000) {
+              int lv[D8_NL];
+#pragma unroll
+              for (int l = 0; l < D8_NL; l++) lv[l] = __float2int_rn(__uint_as_float(acc[l][jj]));
+              // level pairs (L, L+1) in 32 bits: |acc_L| <= 7 * 2^14 * 64 < 2^23
+              const int p0 = lv[0] * 256 + lv[1], p1 = lv[2] * 256 + lv[3];
+              const int p2 = lv[4] * 256 + lv[5], p3 = lv[6] * 256 + lv[7];
+              const long long T = ((long long)p0 << 26) + ((long long)p1 << 10) +
+                                  (long long)((p2 + 32) >> 6) +
+                                  (long long)((p3 + (1 << 21)) >> 22);  // sum_L acc_L 2^{50-8L}
+              const int E = ea + eb;
+              const long long t = gT[o], r = t + T;
+              if (gE[o] != E || ((t ^ r) & (T ^ r)) < 0) {
+                gc_flush(gT + o, gE + o, gS + o);
+                gT[o] = T;
+                gE[o] = E;
+              } else {
+                gT[o] = r;
+              }
             }
           }
         }
-        const int E0 = ce[isv ? q.col : TC_M + q.col - mi];
-        int E[4];
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          E[t] = E0;
-          if (E0 >= 4096) v[t] = 0.0;
-        }
-        const int cc = isv ? q.col : q.col - mi;
-        uint8_t* dst = (isv ? As + q.g * (TC_M / 8 * 128) : Bs + q.g * (D8_S * N * 16)) +
-                       (cc >> 3) * 128 + (cc & 7) * 16 + q.h * 8;
-        d8_slice4(v, E, dst, isv ? TC_M * TC_KS * 2 : N * 16);
       }
-      // further quads: exponents of chunk c + 1 now
-      if (c + 1 < nch && nquads > TC_T)
-        gc_stage_exp<VEC>(V, i0, mi, W, j0, nj, wd, (cb + (int)gridDim.x) * GC_K + st * TC_KS, n,
-                          ce_next, tid + TC_T);
-      if (st == GC_ST - 1)  // slots of chunk c+2 (last read by the fold of chunk c-1)
-        for (int e = tid; e < GC_CE; e += TC_T) cexp[((c + 2) % 3) * GC_CE + e] = -2000;
-      gcge::tc::fence_proxy_async();
-      __syncthreads();
-      if (tid == 0) {
-        gcge::tc::fence_after();
-        d8_issue(tacc, gcge::tc::smem_u32(As), TC_M * TC_KS * 2, gcge::tc::smem_u32(Bs), N,
-                 st == 0);
-        gcge::tc::commit(&mbar[buf]);
+      gcge::tc::fence_before();
+      __syncwarp();
+      if (lane == 0) gcge::tc::mbar_arrive(&macce[tb]);
+    }
+  } else {
+    // ------------------------------------------------ slicer warps
+    const int nquads = 4 * ncolt;
+    const int st0 = warp * 32 + lane;  // first quad of this thread
+    const GcQuad uq = gc_quad(st0 < nquads ? st0 : 0, ncolt);
+    for (int c = 0; c < nch; c++) {
+      const int cb = (int)blockIdx.x + c * (int)gridDim.x;
+      const int row0 = cb * GC_K;
+      const int valid = min(GC_K, n - row0);
+      const int rb = c % nraw;
+      double* raw = reinterpret_cast<double*>(rawbase + rb * RC);
+      if (!gcge::tc::mbar_wait_warp(&mraw[rb], (c / nraw) & 1, TC_WAIT)) ok = false;
+      const int rfill = BULK ? (valid & ~1) : 0;
+      if (rfill < GC_K) {  // rows the bulk copy did not bring: tail row, zero padding
+        const int nr = GC_K - rfill;
+        for (int e = st0; e < rawcols * nr; e += GC_SW * 32) {
+          const int col = e / nr, rr = rfill + e % nr;
+          raw[col * (GC_RAWLD / 8) + rr] = rr < valid ? __ldg(colptr(col) + row0 + rr) : 0.0;
+        }
+        gcge::tc::named_sync(1, GC_SW * 32);
+      }
+      // chunk exponents: warp per column, lane = rows 2 lane, 2 lane + 1
+      int* ce = cex + (c % 3) * GC_CE;
+      for (int col = warp; col < ncolt; col += GC_SW) {
+        const double2 v2 =
+            *reinterpret_cast<const double2*>(raw + col * (GC_RAWLD / 8) + 2 * lane);
+        int f0 = (__double2hiint(v2.x) >> 20) & 0x7FF, f1 = (__double2hiint(v2.y) >> 20) & 0x7FF;
+        int bad = (f0 == 0x7FF) | (f1 == 0x7FF);
+        if (wd && col >= mi) {
+          const double2 w2 =
+              *reinterpret_cast<const double2*>(raw + ncolt * (GC_RAWLD / 8) + 2 * lane);
+          const int g0 = (__double2hiint(w2.x) >> 20) & 0x7FF,
+                    g1 = (__double2hiint(w2.y) >> 20) & 0x7FF;
+          bad |= (g0 == 0x7FF) | (g1 == 0x7FF);
+          // product fields (a product at the bottom of the range still gets >= 1)
+          f0 = (f0 == 0 || g0 == 0) ? 0 : max(f0 + g0 - 1022, 1);
+          f1 = (f1 == 0 || g1 == 0) ? 0 : max(f1 + g1 - 1022, 1);
+        }
+        const int fmax = __reduce_max_sync(0xffffffffu, max(f0, f1));
+        const int anybad = __reduce_or_sync(0xffffffffu, bad);
+        if (lane == 0)
+          ce[col < mi ? col : TC_M + col - mi] = anybad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
+      }
+      gcge::tc::named_sync(1, GC_SW * 32);
+      for (int st = 0; st < GC_ST; st++) {
+        const int g = c * GC_ST + st, buf = g & 1;
+        if (g >= 2 && !gcge::tc::mbar_wait_warp(&mempty[buf], ((g >> 1) - 1) & 1, TC_WAIT))
+          ok = false;
+        uint8_t* As = base + buf * GC_SB;
+        uint8_t* Bs = As + TC_ABYTES;
+        for (int u = st0; u < nquads; u += GC_SW * 32) {
+          const GcQuad q = (u == st0) ? uq : gc_quad(u, ncolt);
+          const bool isv = q.col < mi;
+          const double* src = raw + q.col * (GC_RAWLD / 8) + st * TC_KS + q.roff;
+          const double2 a01 = *reinterpret_cast<const double2*>(src);
+          const double2 a23 = *reinterpret_cast<const double2*>(src + 2);
+          double v[4] = {a01.x, a01.y, a23.x, a23.y};
+          if (wd && !isv) {
+            const double* ws = raw + ncolt * (GC_RAWLD / 8) + st * TC_KS + q.roff;
+            const double2 w01 = *reinterpret_cast<const double2*>(ws);
+            const double2 w23 = *reinterpret_cast<const double2*>(ws + 2);
+            v[0] *= w01.x;
+            v[1] *= w01.y;
+            v[2] *= w23.x;
+            v[3] *= w23.y;
+          }
+          const int E0 = ce[isv ? q.col : TC_M + q.col - mi];
+          int E[4];
+#pragma unroll
+          for (int t = 0; t < 4; t++) {
+            E[t] = E0;
+            if (E0 >= 4096) v[t] = 0.0;
+          }
+          const int cc = isv ? q.col : q.col - mi;
+          uint8_t* dst = (isv ? As + q.g * (TC_M / 8 * 128) : Bs + q.g * (D8_S * GC_N * 16)) +
+                         (cc >> 3) * 128 + (cc & 7) * 16 + q.h * 8;
+          d8_slice4(v, E, dst, isv ? TC_M * TC_KS * 2 : GC_N * 16);
+        }
+        gcge::tc::fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) gcge::tc::mbar_arrive(&mfull[buf]);
       }
     }
   }
-  if (nch > 0) {
-    const int gl = nch * GC_ST - 1;
-    if (!gcge::tc::mbar_wait_warp(&mbar[gl % GC_STAGES], (gl / GC_STAGES) & 1, TC_WAIT))
-      ok = false;
-    gcge::tc::fence_after();
-    gc_fold(tmem + (uint32_t)(((nch - 1) % nbuf) * D8_NL * N), N, mi, nj,
-            cexp + ((nch - 1) % 3) * GC_CE, gsum, gT, gE);
-  }
-  __syncthreads();
-  for (int e = tid; e < TC_M * N; e += TC_T) gc_flush(gT + e, gE + e, gsum + e);
   const int anybad = __syncthreads_or(ok ? 0 : 1);
   if (anybad && tid == 0) atomicExch(&g_oz_tc_status, 1);
   // partial layout [block][o], o = i + j*k1 (the flex-Gram reduction layout)
   double* out = partial + (size_t)blockIdx.x * k1 * k2;
-  for (int e = tid; e < mi * nj; e += TC_T) {
+  for (int e = tid; e < mi * nj; e += GC_THREADS) {
     const int ii = e % mi, jj = e / mi;
+    const int o = jj * TC_M + ii;
+    gc_flush(gT + o, gE + o, gS + o);
     out[(i0 + ii) + (size_t)(j0 + jj) * k1] =
-        anybad ? __longlong_as_double(0x7ff8000000000000ll) : gsum[(size_t)jj * TC_M + ii];
+        anybad ? __longlong_as_double(0x7ff8000000000000ll) : gS[o];
   }
   gcge::tc::fence_before();
   __syncthreads();
-  if ((tid >> 5) == 0) {
+  if (warp == 0) {
     gcge::tc::fence_after();
     gcge::tc::tmem_dealloc(tmem, ncols);
   }
 }
 
-template <bool VEC>
-int launch_gram_tc(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
-                   const double* wd, double* partial, cudaStream_t st) {
-  const int ntm = (k1 + TC_M - 1) / TC_M, ntn = (k2 + GC_NMAX - 1) / GC_NMAX;
+// Returns the CTAs along the rows (the partial blocks to add).
+template <bool BULK>
+int gram_tc_all(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n,
+                const double* wd, double* partial, cudaStream_t st) {
+  const int ntm = (k1 + GC_MI - 1) / GC_MI, ntn = (k2 + GC_N - 1) / GC_N;
   const int nchunks = (n + GC_K - 1) / GC_K;
-  const int N0 = gc_tile_n(k2, 0);
-  const size_t sm = tc_gram_smem(N0);
-  const int per_sm = (227 * 1024) / (int)(sm + 1024) >= 2 ? 2 : 1;
-  const int nblk = nchunks < 152 * per_sm ? nchunks : 152 * per_sm;
+  const int rawcols = (k1 < GC_MI ? k1 : GC_MI) + (k2 < GC_N ? k2 : GC_N) + (wd ? 1 : 0);
+  const int nraw = gc_nraw(rawcols);
+  const int nblk = nchunks < 152 ? nchunks : 152;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_gram_tc<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc_gram_smem(GC_NMAX));
+    cudaFuncSetAttribute(k_gram_tc<BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         GC_SMEM_CAP);
     attr = true;
   }
-  k_gram_tc<VEC><<<dim3(nblk, ntm * ntn), TC_T, sm, st>>>(V, k1, W, k2, n, ntn, wd, partial,
-                                                          nchunks);
+  k_gram_tc<BULK><<<dim3(nblk, ntm * ntn), GC_THREADS, gc_smem(rawcols), st>>>(
+      V, k1, W, k2, n, ntn, wd, partial, nchunks, nraw);
   return nblk;
 }
 
@@ -926,8 +856,8 @@ void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2,
   bool vec = ((uintptr_t)wdiag & 15) == 0;
   for (int i = 0; i < k1; i++) vec = vec && ((uintptr_t)V.p[i] & 15) == 0;
   for (int j = 0; j < k2; j++) vec = vec && ((uintptr_t)W.p[j] & 15) == 0;
-  const int nblk = vec ? launch_gram_tc<true>(V, k1, W, k2, n, wdiag, partial, st)
-                       : launch_gram_tc<false>(V, k1, W, k2, n, wdiag, partial, st);
+  const int nblk = vec ? gram_tc_all<true>(V, k1, W, k2, n, wdiag, partial, st)
+                       : gram_tc_all<false>(V, k1, W, k2, n, wdiag, partial, st);
   gram_reduce_partials(k1, k2, nblk, sym, partial, G, ldg, st);
 }
 
