@@ -18,7 +18,7 @@ namespace gcge {
 namespace {
 
 constexpr int kT = 256;
-constexpr int KC = 8;
+constexpr int kBatch = 4;  // steps launched per host synchronisation
 
 __device__ inline double block_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -33,7 +33,7 @@ __device__ inline double block_sum(double v, double* sh) {
 }
 
 // r_c = rhs_c - A x_c  and  partial ||r_c||^2, for every column c < len.
-template <typename T>
+template <typename T, int KC>
 __global__ void __launch_bounds__(kT) k_bcg_init(int n, const int* __restrict__ rp,
                                                  const int* __restrict__ ci,
                                                  const T* __restrict__ val, ColList<T> X,
@@ -115,7 +115,7 @@ __global__ void k_bcg_p(int n, ColList<T> R, ColList<T> P, BcgScalars s, int fir
 }
 
 // :429-445 w = A p and partial p.w for the active ids (KC per pass).
-template <typename T>
+template <typename T, int KC>
 __global__ void __launch_bounds__(kT) k_bcg_ap(int n, const int* __restrict__ rp,
                                                const int* __restrict__ ci,
                                                const T* __restrict__ val, ColList<T> P,
@@ -126,14 +126,9 @@ __global__ void __launch_bounds__(kT) k_bcg_ap(int n, const int* __restrict__ rp
   const int c0 = blockIdx.y * KC;
   if (c0 >= nu) return;
   const int kc = min(KC, nu - c0);
-  const T* pc[KC];
-  T* wc[KC];
+  int ix[KC];  // column of each active id (pointers read from the parameter block)
 #pragma unroll
-  for (int c = 0; c < KC; c++) {
-    const int idx = (c < kc) ? s.unl[c0 + c] : s.unl[c0];
-    pc[c] = P.p[idx];
-    wc[c] = W.p[idx];
-  }
+  for (int c = 0; c < KC; c++) ix[c] = (c < kc) ? s.unl[c0 + c] : s.unl[c0];
   T dot[KC];
 #pragma unroll
   for (int c = 0; c < KC; c++) dot[c] = T(0);
@@ -146,13 +141,13 @@ __global__ void __launch_bounds__(kT) k_bcg_ap(int n, const int* __restrict__ rp
       const T a = __ldg(val + j);
 #pragma unroll
       for (int c = 0; c < KC; c++)
-        if (c < kc) ap[c] = fma(a, pc[c][col], ap[c]);
+        if (c < kc) ap[c] = fma(a, P.p[ix[c]][col], ap[c]);
     }
 #pragma unroll
     for (int c = 0; c < KC; c++)
       if (c < kc) {
-        wc[c][r] = ap[c];
-        dot[c] = fma(pc[c][r], ap[c], dot[c]);
+        W.p[ix[c]][r] = ap[c];
+        dot[c] = fma(P.p[ix[c]][r], ap[c], dot[c]);
       }
   }
   for (int c = 0; c < kc; c++) {
@@ -185,8 +180,9 @@ __global__ void k_bcg_update(int n, ColList<T> X, ColList<T> R, ColList<T> P, Co
   if (threadIdx.x == 0) partial[(size_t)id * gridDim.x + blockIdx.x] = v;
 }
 
-// :465-495 rho1 <- rho2, rho2 <- r.r, error update and the new active list.
-__global__ void k_ctrl_step(BcgScalars s, double rate) {
+// :465-495 rho1 <- rho2, rho2 <- r.r, error update and the new active list;
+// the active count also goes to host slot `slot` (one per step of a batch).
+__global__ void k_ctrl_step(BcgScalars s, double rate, int slot) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int nu = *s.nu;
   for (int id = 0; id < nu; id++) {
@@ -200,7 +196,7 @@ __global__ void k_ctrl_step(BcgScalars s, double rate) {
     if (s.lerr[idx] >= rate * s.err[idx] && s.lerr[idx] >= 1e-15) s.unl[m++] = idx;
   }
   *s.nu = m;
-  *s.nu_host = m;
+  s.nu_host[slot] = m;
 }
 
 inline int nblocks(int n) {
@@ -218,25 +214,44 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
   if (len <= 0) return 0;
   const int nb = nblocks(n);
   int nl = 0;
-  k_bcg_init<T><<<dim3(nb, (len + KC - 1) / KC), kT, 0, st>>>(n, rp, ci, val, X, RHS, len,
-                                                               partial);
+  // one pass over A for up to 16 columns
+  if (len <= 8)
+    k_bcg_init<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, X, RHS, len, partial);
+  else
+    k_bcg_init<T, 16><<<dim3(nb, (len + 15) / 16), kT, 0, st>>>(n, rp, ci, val, X, RHS, len,
+                                                                  partial);
   k_reduce<<<len, 256, 0, st>>>(partial, nb, len, nullptr, s.rho2);
   k_ctrl_init<<<1, 1, 0, st>>>(s, len);
   nl += 3;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
   int niter = 1;
-  int nu = *s.nu_host;
+  int nu = s.nu_host[0];
+  // Steps are launched kBatch at a time between host synchronisations.  Every
+  // kernel of a step reads the active count on the device and does nothing
+  // once it is 0, so the steps past convergence are empty; step j of a batch
+  // leaves the active count in host slot j, from which the host counts the
+  // steps that ran (the reference's niter).
   while (nu > 0 && niter < max_it) {
-    k_bcg_p<T><<<dim3(nb, len), kT, 0, st>>>(n, RHS, P, s, niter == 1 ? 1 : 0);
-    k_bcg_ap<T><<<dim3(nb, (len + KC - 1) / KC), kT, 0, st>>>(n, rp, ci, val, P, W, s, partial);
-    k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.ptw);
-    k_bcg_update<T><<<dim3(nb, len), kT, 0, st>>>(n, X, RHS, P, W, s, partial);
-    k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.rnew);
-    k_ctrl_step<<<1, 1, 0, st>>>(s, rate);
-    nl += 6;
+    const int batch = (max_it - niter) < kBatch ? (max_it - niter) : kBatch;
+    for (int j = 0; j < batch; j++) {
+      k_bcg_p<T><<<dim3(nb, len), kT, 0, st>>>(n, RHS, P, s, niter + j == 1 ? 1 : 0);
+      if (len <= 8)
+        k_bcg_ap<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, P, W, s, partial);
+      else
+        k_bcg_ap<T, 16><<<dim3(nb, (len + 15) / 16), kT, 0, st>>>(n, rp, ci, val, P, W, s,
+                                                                   partial);
+      k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.ptw);
+      k_bcg_update<T><<<dim3(nb, len), kT, 0, st>>>(n, X, RHS, P, W, s, partial);
+      k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.rnew);
+      k_ctrl_step<<<1, 1, 0, st>>>(s, rate, j);
+      nl += 6;
+    }
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
-    nu = *s.nu_host;
-    niter++;
+    for (int j = 0; j < batch; j++) {
+      niter++;  // step j ran: the count before it was > 0
+      nu = s.nu_host[j];
+      if (nu == 0) break;
+    }
   }
   if (launches) *launches += nl;
   return niter;

@@ -5,7 +5,8 @@
 namespace gcge {
 
 // Per-column scalars of the block CG, all device arrays of length >= len,
-// except nu_host which is mapped pinned host memory.
+// except nu_host which is mapped pinned host memory of at least 4 ints (the
+// active count after each step of a batch).
 struct BcgScalars {
   double* rho1;
   double* rho2;

@@ -447,7 +447,7 @@ size_t tc_lincomb_smem(int N) {
 // ---------------------------------------------------------------- tcgen05 Gram
 // G = V^T diag(wd) W (wd NULL: identity) with FP64 accuracy.  One CTA per SM
 // owns up to GC_MI columns of V (MMA M, TMEM lane = column of V) and 16
-// columns of W (MMA N) over a strided set of 64-row chunks.  Its warps have
+// columns of W (MMA N) over a contiguous run of 64-row chunks.  Its warps have
 // fixed roles and hand work over through mbarriers (no block-wide barrier in
 // the loop):
 //  * producer/MMA warp: streams each chunk's columns (and the diagonal) into
@@ -540,7 +540,10 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   uint64_t* macce = mfull + 6;    // chunk accumulators folded (2)
   uint64_t* mraw = mfull + 8;     // raw chunk arrived (nraw)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mraw + GC_MAXRAW);
-  const int nch = (nchunks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  // this CTA's chunks: a contiguous run (consecutive reads of every column)
+  const int cbase = nchunks / (int)gridDim.x, crem = nchunks % (int)gridDim.x;
+  const int nch = cbase + ((int)blockIdx.x < crem ? 1 : 0);
+  const int cfirst = (int)blockIdx.x * cbase + min((int)blockIdx.x, crem);
   auto colptr = [&](int col) -> const double* {
     return col < mi ? V.p[i0 + col] : (col < ncolt ? W.p[j0 + col - mi] : wd);
   };
@@ -569,7 +572,7 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   if (warp == GC_PW) {
     // ------------------------------------------------ producer / MMA warp
     auto issue_raw = [&](int cc) {
-      const int row0 = ((int)blockIdx.x + cc * (int)gridDim.x) * GC_K;
+      const int row0 = (cfirst + cc) * GC_K;
       const int valid = min(GC_K, n - row0);
       const int rows = BULK ? (valid & ~1) : 0;
       uint64_t* mb = &mraw[cc % nraw];
@@ -661,7 +664,7 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
     const int st0 = warp * 32 + lane;  // first quad of this thread
     const GcQuad uq = gc_quad(st0 < nquads ? st0 : 0, ncolt);
     for (int c = 0; c < nch; c++) {
-      const int cb = (int)blockIdx.x + c * (int)gridDim.x;
+      const int cb = cfirst + c;
       const int row0 = cb * GC_K;
       const int valid = min(GC_K, n - row0);
       const int rb = c % nraw;
