@@ -214,12 +214,14 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
   if (len <= 0) return 0;
   const int nb = nblocks(n);
   int nl = 0;
-  // one pass over A for up to 16 columns
+  // FP64: one pass over A for up to 16 columns; FP32: passes of 8 columns
+  // (the 16-column FP32 pass, at 80 registers, left too few warps per SM)
+  constexpr int KW = sizeof(T) == 8 ? 16 : 8;
   if (len <= 8)
     k_bcg_init<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, X, RHS, len, partial);
   else
-    k_bcg_init<T, 16><<<dim3(nb, (len + 15) / 16), kT, 0, st>>>(n, rp, ci, val, X, RHS, len,
-                                                                  partial);
+    k_bcg_init<T, KW><<<dim3(nb, (len + KW - 1) / KW), kT, 0, st>>>(n, rp, ci, val, X, RHS,
+                                                                      len, partial);
   k_reduce<<<len, 256, 0, st>>>(partial, nb, len, nullptr, s.rho2);
   k_ctrl_init<<<1, 1, 0, st>>>(s, len);
   nl += 3;
@@ -238,8 +240,8 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
       if (len <= 8)
         k_bcg_ap<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, P, W, s, partial);
       else
-        k_bcg_ap<T, 16><<<dim3(nb, (len + 15) / 16), kT, 0, st>>>(n, rp, ci, val, P, W, s,
-                                                                   partial);
+        k_bcg_ap<T, KW><<<dim3(nb, (len + KW - 1) / KW), kT, 0, st>>>(n, rp, ci, val, P, W, s,
+                                                                       partial);
       k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.ptw);
       k_bcg_update<T><<<dim3(nb, len), kT, 0, st>>>(n, X, RHS, P, W, s, partial);
       k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.rnew);

@@ -356,21 +356,22 @@ __global__ void k_split_pairs(const double* __restrict__ pr, int k, double* __re
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
-// A is read once per pass of 8 (k <= 8) or 16 columns.
+// Y[:, j] = A X[:, j]: 8 columns per pass (a 16-column pass halves the
+// CTAs per row range and measured slower on GB300).
 void spmm_f64(const GcgeDevCsr& A, const ColList<double>& X, const ColList<double>& Y, int k,
               cudaStream_t st) {
   if (k <= 0 || A.n <= 0) return;
-  const int nb = (A.n + kThreads - 1) / kThreads;
-  if (k <= 8) k_spmm<double, 8><<<dim3(nb, 1), kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v, X, Y, k);
-  else k_spmm<double, 16><<<dim3(nb, (k + 15) / 16), kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v, X, Y, k);
+  constexpr int KC = 8;
+  dim3 g((A.n + kThreads - 1) / kThreads, (k + KC - 1) / KC);
+  k_spmm<double, KC><<<g, kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v, X, Y, k);
 }
 
 void spmm_f32(const GcgeDevCsr& A, const ColList<float>& X, const ColList<float>& Y, int k,
               cudaStream_t st) {
   if (k <= 0 || A.n <= 0) return;
-  const int nb = (A.n + kThreads - 1) / kThreads;
-  if (k <= 8) k_spmm<float, 8><<<dim3(nb, 1), kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v32, X, Y, k);
-  else k_spmm<float, 16><<<dim3(nb, (k + 15) / 16), kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v32, X, Y, k);
+  constexpr int KC = 8;
+  dim3 g((A.n + kThreads - 1) / kThreads, (k + KC - 1) / KC);
+  k_spmm<float, KC><<<g, kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v32, X, Y, k);
 }
 
 void apply_b_f64(const GcgeDevCsr* B, const ColList<double>& X, const ColList<double>& Y, int k,
