@@ -268,3 +268,349 @@ template int bcg_run<float>(const int*, const int*, const float*, int, const Col
                             int, int, double, const BcgScalars&, double*, cudaStream_t, int*);
 
 }  // namespace gcge
+
+// ---------------------------------------------------------------- row-interleaved FP32 block CG
+namespace gcge {
+namespace {
+
+// per-column block sums in the order of block_sum, into partial[c*nblk + b]
+template <int KW>
+__device__ __forceinline__ void block_sum_cols(const float* acc, int len, double* sh,
+                                               double* __restrict__ partial) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < KW; c++) {
+    double v = (double)acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[wid * 16 + c] = v;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < len) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w * 16 + threadIdx.x];
+    partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+template <int KW>
+__device__ __forceinline__ void load_row(const float* __restrict__ base, size_t r, float* v) {
+  const float4* p = reinterpret_cast<const float4*>(base + r * KW);
+#pragma unroll
+  for (int q = 0; q < KW / 4; q++) {
+    const float4 t = __ldg(p + q);
+    v[4 * q] = t.x;
+    v[4 * q + 1] = t.y;
+    v[4 * q + 2] = t.z;
+    v[4 * q + 3] = t.w;
+  }
+}
+template <int KW>
+__device__ __forceinline__ void store_row(float* base, size_t r, const float* v) {
+  float4* p = reinterpret_cast<float4*>(base + r * KW);
+#pragma unroll
+  for (int q = 0; q < KW / 4; q++) p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
+// r = rhs - A x and partial ||r_c||^2 (c < len)
+template <int KW>
+__global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__ rp,
+                                                  const int* __restrict__ ci,
+                                                  const float* __restrict__ val,
+                                                  const float* __restrict__ X, float* R, int len,
+                                                  double* __restrict__ partial) {
+  __shared__ double sh[(kT / 32) * 16];
+  float acc2[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) acc2[c] = 0.f;
+  for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
+    float ax[KW];
+#pragma unroll
+    for (int c = 0; c < KW; c++) ax[c] = 0.f;
+    for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+      const int col = __ldg(ci + j);
+      const float a = __ldg(val + j);
+      float xv[KW];
+      load_row<KW>(X, col, xv);
+#pragma unroll
+      for (int c = 0; c < KW; c++) ax[c] = fmaf(a, xv[c], ax[c]);
+    }
+    float rv[KW];
+    load_row<KW>(R, r, rv);
+#pragma unroll
+    for (int c = 0; c < KW; c++) {
+      rv[c] = rv[c] - ax[c];
+      acc2[c] = fmaf(rv[c], rv[c], acc2[c]);
+    }
+    store_row<KW>(R, r, rv);
+  }
+  block_sum_cols<KW>(acc2, len, sh, partial);
+}
+
+// p = r (first step) or p = r + beta p, beta = rho2[c] / rho1[c], for the active columns
+template <int KW>
+__global__ void __launch_bounds__(kT) k_rows_p(int n, const float* __restrict__ R, float* P,
+                                               BcgScalars s, int first) {
+  if (*s.nu == 0) return;
+  float beta[KW];
+  bool on[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) {
+    on[c] = s.mask[c] != 0;
+    beta[c] = (on[c] && !first) ? (float)(s.rho2[c] / s.rho1[c]) : 0.f;
+  }
+  for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
+    float rv[KW], pv[KW];
+    load_row<KW>(R, r, rv);
+    load_row<KW>(P, r, pv);
+#pragma unroll
+    for (int c = 0; c < KW; c++)
+      if (on[c]) pv[c] = first ? rv[c] : rv[c] + beta[c] * pv[c];
+    store_row<KW>(P, r, pv);
+  }
+}
+
+// w = A p and partial p.w for the active columns
+template <int KW>
+__global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ rp,
+                                                const int* __restrict__ ci,
+                                                const float* __restrict__ val,
+                                                const float* __restrict__ P, float* W, int len,
+                                                BcgScalars s, double* __restrict__ partial) {
+  __shared__ double sh[(kT / 32) * 16];
+  if (*s.nu == 0) return;
+  bool on[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) on[c] = s.mask[c] != 0;
+  float dot[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) dot[c] = 0.f;
+  for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
+    float ap[KW];
+#pragma unroll
+    for (int c = 0; c < KW; c++) ap[c] = 0.f;
+    for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+      const int col = __ldg(ci + j);
+      const float a = __ldg(val + j);
+      float pv[KW];
+      load_row<KW>(P, col, pv);
+#pragma unroll
+      for (int c = 0; c < KW; c++) ap[c] = fmaf(a, pv[c], ap[c]);
+    }
+    store_row<KW>(W, r, ap);
+    float pr[KW];
+    load_row<KW>(P, r, pr);
+#pragma unroll
+    for (int c = 0; c < KW; c++)
+      if (on[c]) dot[c] = fmaf(pr[c], ap[c], dot[c]);
+  }
+  block_sum_cols<KW>(dot, len, sh, partial);
+}
+
+// x += alpha p, r -= alpha w and partial r.r for the active columns
+template <int KW>
+__global__ void __launch_bounds__(kT) k_rows_update(int n, float* X, float* R,
+                                                    const float* __restrict__ P,
+                                                    const float* __restrict__ W, int len,
+                                                    BcgScalars s, double* __restrict__ partial) {
+  __shared__ double sh[(kT / 32) * 16];
+  if (*s.nu == 0) return;
+  bool on[KW];
+  float alpha[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) {
+    on[c] = s.mask[c] != 0;
+    alpha[c] = on[c] ? (float)s.acol[c] : 0.f;
+  }
+  float acc[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) acc[c] = 0.f;
+  for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
+    float xv[KW], rv[KW], pv[KW], wv[KW];
+    load_row<KW>(X, r, xv);
+    load_row<KW>(R, r, rv);
+    load_row<KW>(P, r, pv);
+    load_row<KW>(W, r, wv);
+#pragma unroll
+    for (int c = 0; c < KW; c++)
+      if (on[c]) {
+        xv[c] = fmaf(alpha[c], pv[c], xv[c]);
+        rv[c] = fmaf(-alpha[c], wv[c], rv[c]);
+        acc[c] = fmaf(rv[c], rv[c], acc[c]);
+      }
+    store_row<KW>(X, r, xv);
+    store_row<KW>(R, r, rv);
+  }
+  block_sum_cols<KW>(acc, len, sh, partial);
+}
+
+// column sums of the per-block partials (fixed order, as k_reduce)
+__device__ __forceinline__ void reduce_cols(const double* __restrict__ partial, int nblk, int len,
+                                            double* out /* shared, 16 */) {
+  __shared__ double sh[32];
+  for (int c = 0; c < len; c++) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += partial[(size_t)c * nblk + b];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) out[c] = v;
+    __syncthreads();
+  }
+}
+
+// initial rho2 (by column), err, lerr, active list and mask
+__global__ void k_rows_init_ctrl(const double* __restrict__ partial, int nblk, int len,
+                                 BcgScalars s) {
+  __shared__ double rr[16];
+  reduce_cols(partial, nblk, len, rr);
+  if (threadIdx.x != 0) return;
+  int nu = 0;
+  for (int c = 0; c < 16; c++) s.mask[c] = 0;
+  for (int idx = 0; idx < len; idx++) {
+    s.rho2[idx] = rr[idx];
+    s.err[idx] = sqrt(s.rho2[idx]);
+    s.lerr[idx] = s.err[idx];
+    if (s.err[idx] >= 1e-15) {
+      s.unl[nu++] = idx;
+      s.mask[idx] = 1;
+    }
+  }
+  *s.nu = nu;
+  s.nu_host[0] = nu;
+}
+
+// ptw[id] = p.w of column unl[id]; alpha of that column = rho2[id] / ptw[id]
+__global__ void k_rows_alpha(const double* __restrict__ partial, int nblk, int len,
+                             BcgScalars s) {
+  __shared__ double pw[16];
+  const int nu = *s.nu;
+  if (nu == 0) return;
+  reduce_cols(partial, nblk, len, pw);
+  if (threadIdx.x != 0) return;
+  for (int id = 0; id < nu; id++) {
+    const int c = s.unl[id];
+    s.ptw[id] = pw[c];
+    s.acol[c] = s.rho2[id] / s.ptw[id];
+  }
+}
+
+// rnew[id] = r.r of column unl[id]; then the step control of k_ctrl_step and the mask
+__global__ void k_rows_step(const double* __restrict__ partial, int nblk, int len, BcgScalars s,
+                            double rate, int slot) {
+  __shared__ double rr[16];
+  const int nu = *s.nu;
+  if (nu == 0) {
+    if (threadIdx.x == 0) s.nu_host[slot] = 0;
+    return;
+  }
+  reduce_cols(partial, nblk, len, rr);
+  if (threadIdx.x != 0) return;
+  for (int id = 0; id < nu; id++) s.rnew[id] = rr[s.unl[id]];
+  for (int id = 0; id < nu; id++) {
+    s.rho1[id] = s.rho2[id];
+    s.rho2[id] = s.rnew[id];
+  }
+  for (int id = 0; id < nu; id++) s.lerr[s.unl[id]] = sqrt(fabs(s.rho2[id]));
+  for (int c = 0; c < 16; c++) s.mask[c] = 0;
+  int m = 0;
+  for (int id = 0; id < nu; id++) {
+    const int idx = s.unl[id];
+    if (s.lerr[idx] >= rate * s.err[idx] && s.lerr[idx] >= 1e-15) {
+      s.unl[m++] = idx;
+      s.mask[idx] = 1;
+    }
+  }
+  *s.nu = m;
+  s.nu_host[slot] = m;
+}
+
+template <int KW>
+__global__ void k_cols_to_rows(ColList<double> R, int len, float* __restrict__ Rr, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  float v[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) v[c] = c < len ? (float)R.p[c][r] : 0.f;
+  store_row<KW>(Rr, r, v);
+}
+
+template <int KW>
+__global__ void k_rows_add(const float* __restrict__ Xr, int len, ColList<double> Y, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  float v[KW];
+  load_row<KW>(Xr, r, v);
+#pragma unroll
+  for (int c = 0; c < KW; c++)
+    if (c < len) Y.p[c][r] += (double)v[c];
+}
+
+template <int KW>
+int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, float* X, float* P,
+             float* W, int len, int max_it, double rate, const BcgScalars& s, double* partial,
+             cudaStream_t st, int* launches) {
+  // four CTAs of 8 warps per SM for the row-streaming kernels
+  const int nb = min((n + kT - 1) / kT, 4 * 152);
+  int nl = 0;
+  k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial);
+  k_rows_init_ctrl<<<1, 256, 0, st>>>(partial, nb, len, s);
+  nl += 2;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  int niter = 1;
+  int nu = s.nu_host[0];
+  while (nu > 0 && niter < max_it) {
+    const int batch = (max_it - niter) < kBatch ? (max_it - niter) : kBatch;
+    for (int j = 0; j < batch; j++) {
+      k_rows_p<KW><<<nb, kT, 0, st>>>(n, R, P, s, niter + j == 1 ? 1 : 0);
+      k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial);
+      k_rows_alpha<<<1, 256, 0, st>>>(partial, nb, len, s);
+      k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
+      k_rows_step<<<1, 256, 0, st>>>(partial, nb, len, s, rate, j);
+      nl += 5;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    for (int j = 0; j < batch; j++) {
+      niter++;
+      nu = s.nu_host[j];
+      if (nu == 0) break;
+    }
+  }
+  if (launches) *launches += nl;
+  return niter;
+}
+
+}  // namespace
+
+int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, float* R, float* X,
+                     float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
+                     double* partial, cudaStream_t st, int* launches) {
+  if (len <= 0) return 0;
+  switch (bcg_rows_width(len)) {
+    case 4: return rows_run<4>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 8: return rows_run<8>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 12: return rows_run<12>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+  }
+  return -1;
+}
+
+void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st) {
+  const int g = (n + 255) / 256;
+  switch (bcg_rows_width(len)) {
+    case 4: k_cols_to_rows<4><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 8: k_cols_to_rows<8><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 12: k_cols_to_rows<12><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 16: k_cols_to_rows<16><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+  }
+}
+
+void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
+                          cudaStream_t st) {
+  const int g = (n + 255) / 256;
+  switch (bcg_rows_width(len)) {
+    case 4: k_rows_add<4><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 8: k_rows_add<8><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 12: k_rows_add<12><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 16: k_rows_add<16><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+  }
+}
+
+}  // namespace gcge

@@ -17,6 +17,8 @@ struct BcgScalars {
   int* unl;
   int* nu;
   volatile int* nu_host;
+  double* acol;  // row-interleaved path: alpha of each column (16 doubles)
+  int* mask;     // row-interleaved path: 1 for the active columns (16 ints)
 };
 
 // Solves A x_c = rhs_c for the len columns (rhs is overwritten by the
@@ -26,5 +28,20 @@ template <typename T>
 int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>& RHS,
             const ColList<T>& X, const ColList<T>& P, const ColList<T>& W, int len, int max_it,
             double rate, const BcgScalars& s, double* partial, cudaStream_t st, int* launches);
+
+// The same FP32 block CG with the four vectors stored row-interleaved: R, X,
+// P, W are n x KW float arrays (element (r, c) at r*KW + c, KW = len rounded
+// up to a multiple of 4, rows 16-byte aligned) for len <= 16, so the SpMM
+// gathers one contiguous KW-float row per nonzero and every vector kernel
+// streams whole rows.  Same steps, scalars and reductions (same order) as
+// bcg_run<float>; s.acol and s.mask must be set.  Returns niter or -1.
+int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, float* R, float* X,
+                     float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
+                     double* partial, cudaStream_t st, int* launches);
+inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
+// Rr (n x KW rows) <- FP64 columns R[0:len] (zero-padded); Y[c] += Xr[:, c].
+void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st);
+void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
+                          cudaStream_t st);
 
 }  // namespace gcge

@@ -247,6 +247,8 @@ extern "C" int GCGE_CUDA_BlockCG(const GCGE_CUDA_MAT* A, double* const* rhs, dou
   s.unl = ints;
   s.nu = ints + GCGE_MAXCOLS;
   s.nu_host = pinned;
+  s.acol = nullptr;  // column path only
+  s.mask = nullptr;
   double* partial = buf + 6 * GCGE_MAXCOLS;
   double* vecs = partial + (size_t)k * nb;
   int it = -1;

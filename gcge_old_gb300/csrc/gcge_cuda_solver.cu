@@ -465,8 +465,11 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   take(s->evec, nev);
   if (p.precision == 1) {
     CHK(mat_ensure_f32(s->A->m, s->st));
-    CU(cudaMalloc(&s->pool32, sizeof(float) * (size_t)s->ldn * 4 * s->bs));
-    CU(cudaMemsetAsync(s->pool32, 0, sizeof(float) * (size_t)s->ldn * 4 * s->bs, s->st));
+    // four column blocks of the block CG, wide enough for the row-interleaved
+    // layout (block size rounded up to 4)
+    const size_t f32n = (size_t)s->ldn * 4 * gcge::bcg_rows_width(s->bs);
+    CU(cudaMalloc(&s->pool32, sizeof(float) * f32n));
+    CU(cudaMemsetAsync(s->pool32, 0, sizeof(float) * f32n, s->st));
     float* f = s->pool32;
     auto takef = [&](std::vector<float*>& v) {
       v.resize(s->bs);
@@ -498,9 +501,10 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   if (s->partial_len < colpart) s->partial_len = colpart;
   CU(cudaMalloc(&s->partial, sizeof(double) * s->partial_len));
   // block-CG scalars
-  CU(cudaMalloc(&s->bcg_mem, sizeof(double) * 6 * GCGE_MAXCOLS));
-  CU(cudaMemsetAsync(s->bcg_mem, 0, sizeof(double) * 6 * GCGE_MAXCOLS, s->st));
-  CU(cudaMalloc(&s->bcg_int, sizeof(int) * (GCGE_MAXCOLS + 1)));
+  CU(cudaMalloc(&s->bcg_mem, sizeof(double) * 7 * GCGE_MAXCOLS));
+  CU(cudaMemsetAsync(s->bcg_mem, 0, sizeof(double) * 7 * GCGE_MAXCOLS, s->st));
+  CU(cudaMalloc(&s->bcg_int, sizeof(int) * (2 * GCGE_MAXCOLS + 1)));
+  CU(cudaMemsetAsync(s->bcg_int, 0, sizeof(int) * (2 * GCGE_MAXCOLS + 1), s->st));
   CU(cudaHostAlloc(&s->h_pinned_int, sizeof(int) * 16, cudaHostAllocMapped));
   int* dev_alias = nullptr;
   CU(cudaHostGetDevicePointer((void**)&dev_alias, s->h_pinned_int, 0));
@@ -515,6 +519,8 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   s->bcg.unl = s->bcg_int;
   s->bcg.nu = s->bcg_int + GCGE_MAXCOLS;
   s->bcg.nu_host = s->h_pinned_int;
+  s->bcg.acol = s->bcg_mem + 6 * GCGE_MAXCOLS;
+  s->bcg.mask = s->bcg_int + GCGE_MAXCOLS + 1;
   CU(cudaStreamSynchronize(s->st));
   (void)add;
   s->setup_done = true;
@@ -824,15 +830,30 @@ static int compute_w(Solver* s) {
     ColList<double> AW = cols(s->evec, 0, wl);
     KL(gcge::spmm_f64(s->A->m, Wc, AW, wl, s->st));
     KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
-    ColList<float> fr = colsf(s->f_rhs, 0, wl), fx = colsf(s->f_x, 0, wl);
-    KL(gcge::convert_f64_to_f32(R, fr, wl, s->n, s->st));
-    for (int i = 0; i < wl; i++)
-      CU(cudaMemsetAsync(fx.p[i], 0, sizeof(float) * s->n, s->st));
-    steps = gcge::bcg_run<float>(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, fr, fx,
-                                 colsf(s->f_p, 0, wl), colsf(s->f_w, 0, wl), wl,
-                                 s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
-                                 &launches);
-    KL(gcge::add_f32_to_f64(fx, Wc, wl, s->n, s->st));
+    if (wl <= 16) {
+      // row-interleaved FP32 vectors: one contiguous row per SpMM gather
+      const size_t blk = (size_t)s->ldn * gcge::bcg_rows_width(wl);
+      float* Rr = s->pool32;
+      float* Xr = Rr + blk;
+      float* Pr = Xr + blk;
+      float* Wr = Pr + blk;
+      KL(gcge::cols_to_rows_f32(R, wl, Rr, s->n, s->st));
+      CU(cudaMemsetAsync(Xr, 0, sizeof(float) * blk, s->st));
+      steps = gcge::bcg_run_rows_f32(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, Rr, Xr, Pr, Wr,
+                                     wl, s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial,
+                                     s->st, &launches);
+      KL(gcge::rows_add_to_cols_f64(Xr, wl, Wc, s->n, s->st));
+    } else {
+      ColList<float> fr = colsf(s->f_rhs, 0, wl), fx = colsf(s->f_x, 0, wl);
+      KL(gcge::convert_f64_to_f32(R, fr, wl, s->n, s->st));
+      for (int i = 0; i < wl; i++)
+        CU(cudaMemsetAsync(fx.p[i], 0, sizeof(float) * s->n, s->st));
+      steps = gcge::bcg_run<float>(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, fr, fx,
+                                   colsf(s->f_p, 0, wl), colsf(s->f_w, 0, wl), wl,
+                                   s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
+                                   &launches);
+      KL(gcge::add_f32_to_f64(fx, Wc, wl, s->n, s->st));
+    }
   }
   s->launches += launches;
   if (steps < 0) return set_err(GCGE_CUDA_ERR_CUDA, "block CG: %s", cudaGetErrorString(cudaGetLastError()));
