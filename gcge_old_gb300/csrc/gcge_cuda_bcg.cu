@@ -522,6 +522,28 @@ __global__ void k_rows_step(const double* __restrict__ partial, int nblk, int le
   s.nu_host[slot] = m;
 }
 
+// y = A x on row-interleaved blocks (the operator of the mixed block CG)
+template <int KW>
+__global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__ rp,
+                                                  const int* __restrict__ ci,
+                                                  const float* __restrict__ val,
+                                                  const float* __restrict__ X, float* Y) {
+  const int r = blockIdx.x * kT + threadIdx.x;
+  if (r >= n) return;
+  float acc[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) acc[c] = 0.f;
+  for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+    const int col = __ldg(ci + j);
+    const float a = __ldg(val + j);
+    float xv[KW];
+    load_row<KW>(X, col, xv);
+#pragma unroll
+    for (int c = 0; c < KW; c++) acc[c] = fmaf(a, xv[c], acc[c]);
+  }
+  store_row<KW>(Y, r, acc);
+}
+
 template <int KW>
 __global__ void k_cols_to_rows(ColList<double> R, int len, float* __restrict__ Rr, int n) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -590,6 +612,17 @@ int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, floa
     case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
   }
   return -1;
+}
+
+void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
+                   float* Y, int k, cudaStream_t st) {
+  const int g = (n + kT - 1) / kT;
+  switch (bcg_rows_width(k)) {
+    case 4: k_rows_spmm<4><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+  }
 }
 
 void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st) {

@@ -39,6 +39,9 @@ int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, floa
                      float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
                      double* partial, cudaStream_t st, int* launches);
 inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
+// Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 16).
+void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
+                   float* Y, int k, cudaStream_t st);
 // Rr (n x KW rows) <- FP64 columns R[0:len] (zero-padded); Y[c] += Xr[:, c].
 void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st);
 void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,

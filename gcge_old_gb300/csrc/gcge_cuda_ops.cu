@@ -85,6 +85,21 @@ extern "C" int GCGE_CUDA_MatDotMultiVecF32Async(GCGE_CUDA_MAT* A, float* const* 
   return cudaGetLastError() == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
 }
 
+extern "C" int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k,
+                                            void* stream) {
+  if (!A || !x || !y || k <= 0 || k > 16 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))
+    return GCGE_CUDA_ERR_ARG;
+  if (!A->m.v32) {
+    if (cudaMalloc(&A->m.v32, sizeof(float) * (A->m.nnz > 0 ? A->m.nnz : 1)) != cudaSuccess)
+      return GCGE_CUDA_ERR_ALLOC;
+    if (A->m.nnz > 0)
+      k_val_to_f32<<<(A->m.nnz + 255) / 256, 256, 0, (cudaStream_t)stream>>>(A->m.v, A->m.v32,
+                                                                             A->m.nnz);
+  }
+  gcge::spmm_rows_f32(A->m.rp, A->m.ci, A->m.v32, A->m.n, x, y, k, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
+}
+
 extern "C" int GCGE_CUDA_MultiVecInnerProd(double* const* V, int k1, double* const* W, int k2,
                                            int n, double* a, int lda, int sym) {
   if (!V || !W || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||

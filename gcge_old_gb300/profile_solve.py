@@ -5,7 +5,8 @@ iterations, so a profiler sees a bounded, repeatable launch sequence.
     python -m gcge_old_gb300.profile_solve --grid 96 --iters 6 --precision mixed
 
 With --spmm K it only runs K-column CSR SpMMs of the same matrix (five FP64
-launches, then five FP32 launches), for traffic counters of that kernel:
+launches, five FP32 column launches, five FP32 row-interleaved launches), for
+traffic counters of those kernels:
 
     python -m gcge_old_gb300.profile_solve --grid 96 --spmm 10
 """
@@ -33,6 +34,13 @@ def spmm_only(A, k):
         L.check(lib.GCGE_CUDA_MatDotMultiVecAsync(dA.handle, xp, yp, k, None), "spmm")
     for _ in range(5):
         L.check(lib.GCGE_CUDA_MatDotMultiVecF32Async(dA.handle, xp32, yp32, k, None), "spmm32")
+    if k <= 16:  # the block CG's row-interleaved FP32 operator
+        kw = (k + 3) // 4 * 4
+        XR = torch.randn(A.n, kw, dtype=torch.float32, device="cuda")
+        YR = torch.empty(A.n, kw, dtype=torch.float32, device="cuda")
+        for _ in range(5):
+            L.check(lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(XR.data_ptr()),
+                                                     C.c_void_p(YR.data_ptr()), k, None), "rows")
     torch.cuda.synchronize()
     print("spmm n=%d nnz=%d k=%d done" % (A.n, A.nnz, k))
 

@@ -32,6 +32,33 @@ def test_spmm_matches_csr_matdotvec(cuda_lib, gen, k):
     np.testing.assert_allclose(host(ys), ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("k", [1, 4, 10, 13, 16])
+def test_rows_spmm_matches_column_spmm(cuda_lib, k):
+    """The row-interleaved FP32 operator of the mixed block CG equals A x
+    column by column (FP32 sums of the same products in the same order)."""
+    import torch
+    A = M.laplace3d_mass(14, seed=1)[0]
+    kw = (k + 3) // 4 * 4
+    rng = np.random.default_rng(k)
+    X = rng.standard_normal((A.n, kw)).astype(np.float32)
+    X[:, k:] = 0.0
+    x = torch.from_numpy(X).cuda()
+    y = torch.full((A.n, kw), np.nan, dtype=torch.float32, device="cuda")
+    dA = DeviceMatrix(A)
+    assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(x.data_ptr()),
+                                                 C.c_void_p(y.data_ptr()), k, None) == 0
+    torch.cuda.synchronize()
+    got = y.cpu().numpy()[:, :k]
+    ref = (A.to_scipy().astype(np.float64) @ X[:, :k].astype(np.float64))
+    # FP32 products summed in FP32 over <= 7 entries per row
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-5 * np.abs(ref).max())
+    # bad arguments: more than 16 columns, misaligned rows
+    assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(x.data_ptr()),
+                                                 C.c_void_p(y.data_ptr()), 17, None) == 1
+    assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(x.data_ptr() + 4),
+                                                 C.c_void_p(y.data_ptr()), k, None) == 1
+
+
 @pytest.mark.parametrize("k1,k2,sym,n", [(7, 3, 0, 1000), (90, 10, 0, 50000), (20, 20, 1, 30001),
                                          (130, 70, 0, 4099), (64, 64, 1, 777), (1, 1, 1, 5)])
 def test_gram_matches_inner_prod(cuda_lib, k1, k2, sym, n):
