@@ -346,29 +346,41 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
   block_sum_cols<KW>(acc2, len, sh, partial);
 }
 
-// The direction update fused into the SpMM: with p' = r (first step) or
-// p' = r + beta p (beta = rho2[c] / rho1[c]) on the active columns and p' = p
-// elsewhere, w = A p' (p' formed at every gathered row from r and the old p),
-// p' is stored for this row into the other P buffer, and partial p'.w.  The
-// old and new P are separate arrays, so no thread reads a row another thread
-// has already updated.
+// p = r (first step) or p = r + beta p, beta = rho2[c] / rho1[c], for the active columns
 template <int KW>
-__global__ void __launch_bounds__(kT) k_rows_pap(int n, const int* __restrict__ rp,
-                                                 const int* __restrict__ ci,
-                                                 const float* __restrict__ val,
-                                                 const float* __restrict__ R,
-                                                 const float* __restrict__ Pold, float* Pnew,
-                                                 float* W, int len, BcgScalars s, int first,
-                                                 double* __restrict__ partial) {
-  __shared__ double sh[(kT / 32) * 16];
+__global__ void __launch_bounds__(kT) k_rows_p(int n, const float* __restrict__ R, float* P,
+                                               BcgScalars s, int first) {
   if (*s.nu == 0) return;
-  bool on[KW];
   float beta[KW];
+  bool on[KW];
 #pragma unroll
   for (int c = 0; c < KW; c++) {
     on[c] = s.mask[c] != 0;
     beta[c] = (on[c] && !first) ? (float)(s.rho2[c] / s.rho1[c]) : 0.f;
   }
+  for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
+    float rv[KW], pv[KW];
+    load_row<KW>(R, r, rv);
+    load_row<KW>(P, r, pv);
+#pragma unroll
+    for (int c = 0; c < KW; c++)
+      if (on[c]) pv[c] = first ? rv[c] : rv[c] + beta[c] * pv[c];
+    store_row<KW>(P, r, pv);
+  }
+}
+
+// w = A p and partial p.w for the active columns
+template <int KW>
+__global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ rp,
+                                                const int* __restrict__ ci,
+                                                const float* __restrict__ val,
+                                                const float* __restrict__ P, float* W, int len,
+                                                BcgScalars s, double* __restrict__ partial) {
+  __shared__ double sh[(kT / 32) * 16];
+  if (*s.nu == 0) return;
+  bool on[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) on[c] = s.mask[c] != 0;
   float dot[KW];
 #pragma unroll
   for (int c = 0; c < KW; c++) dot[c] = 0.f;
@@ -379,27 +391,17 @@ __global__ void __launch_bounds__(kT) k_rows_pap(int n, const int* __restrict__ 
     for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
       const int col = __ldg(ci + j);
       const float a = __ldg(val + j);
-      float rv[KW], pv[KW];
-      load_row<KW>(R, col, rv);
-      load_row<KW>(Pold, col, pv);
+      float pv[KW];
+      load_row<KW>(P, col, pv);
 #pragma unroll
-      for (int c = 0; c < KW; c++) {
-        if (on[c]) pv[c] = first ? rv[c] : rv[c] + beta[c] * pv[c];
-        ap[c] = fmaf(a, pv[c], ap[c]);
-      }
+      for (int c = 0; c < KW; c++) ap[c] = fmaf(a, pv[c], ap[c]);
     }
     store_row<KW>(W, r, ap);
-    float rv[KW], pv[KW];
-    load_row<KW>(R, r, rv);
-    load_row<KW>(Pold, r, pv);
+    float pr[KW];
+    load_row<KW>(P, r, pr);
 #pragma unroll
-    for (int c = 0; c < KW; c++) {
-      if (on[c]) {
-        pv[c] = first ? rv[c] : rv[c] + beta[c] * pv[c];
-        dot[c] = fmaf(pv[c], ap[c], dot[c]);
-      }
-    }
-    store_row<KW>(Pnew, r, pv);
+    for (int c = 0; c < KW; c++)
+      if (on[c]) dot[c] = fmaf(pr[c], ap[c], dot[c]);
   }
   block_sum_cols<KW>(dot, len, sh, partial);
 }
@@ -567,10 +569,10 @@ __global__ void k_rows_add(const float* __restrict__ Xr, int len, ColList<double
 
 template <int KW>
 int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, float* X, float* P,
-             float* P2, float* W, int len, int max_it, double rate, const BcgScalars& s,
-             double* partial, cudaStream_t st, int* launches) {
-  // three CTAs of 8 warps per SM (the fused SpMM holds 84 registers a thread)
-  const int nb = min((n + kT - 1) / kT, 3 * 152);
+             float* W, int len, int max_it, double rate, const BcgScalars& s, double* partial,
+             cudaStream_t st, int* launches) {
+  // four CTAs of 8 warps per SM for the row-streaming kernels
+  const int nb = min((n + kT - 1) / kT, 4 * 152);
   int nl = 0;
   k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial);
   k_rows_init_ctrl<<<1, 512, 0, st>>>(partial, nb, len, s);
@@ -581,16 +583,12 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
   while (nu > 0 && niter < max_it) {
     const int batch = (max_it - niter) < kBatch ? (max_it - niter) : kBatch;
     for (int j = 0; j < batch; j++) {
-      // step k reads P[k % 2] and writes P[(k + 1) % 2]
-      const int k = niter + j;
-      float* Pold = (k & 1) ? P : P2;
-      float* Pnew = (k & 1) ? P2 : P;
-      k_rows_pap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, R, Pold, Pnew, W, len, s, k == 1 ? 1 : 0,
-                                        partial);
+      k_rows_p<KW><<<nb, kT, 0, st>>>(n, R, P, s, niter + j == 1 ? 1 : 0);
+      k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial);
       k_rows_alpha<<<1, 512, 0, st>>>(partial, nb, len, s);
-      k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, Pnew, W, len, s, partial);
+      k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
       k_rows_step<<<1, 512, 0, st>>>(partial, nb, len, s, rate, j);
-      nl += 4;
+      nl += 5;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
     for (int j = 0; j < batch; j++) {
@@ -606,14 +604,14 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
 }  // namespace
 
 int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, float* R, float* X,
-                     float* P, float* P2, float* W, int len, int max_it, double rate,
-                     const BcgScalars& s, double* partial, cudaStream_t st, int* launches) {
+                     float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
+                     double* partial, cudaStream_t st, int* launches) {
   if (len <= 0) return 0;
   switch (bcg_rows_width(len)) {
-    case 4: return rows_run<4>(rp, ci, val, n, R, X, P, P2, W, len, max_it, rate, s, partial, st, launches);
-    case 8: return rows_run<8>(rp, ci, val, n, R, X, P, P2, W, len, max_it, rate, s, partial, st, launches);
-    case 12: return rows_run<12>(rp, ci, val, n, R, X, P, P2, W, len, max_it, rate, s, partial, st, launches);
-    case 16: return rows_run<16>(rp, ci, val, n, R, X, P, P2, W, len, max_it, rate, s, partial, st, launches);
+    case 4: return rows_run<4>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 8: return rows_run<8>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 12: return rows_run<12>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
   }
   return -1;
 }

@@ -29,16 +29,15 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
             const ColList<T>& X, const ColList<T>& P, const ColList<T>& W, int len, int max_it,
             double rate, const BcgScalars& s, double* partial, cudaStream_t st, int* launches);
 
-// The same FP32 block CG with its vectors stored row-interleaved: R, X, two
-// P buffers and W are n x KW float arrays (element (r, c) at r*KW + c, KW =
-// len rounded up to a multiple of 4, rows 16-byte aligned) for len <= 16, so
-// the SpMM gathers contiguous KW-float rows and every vector kernel streams
-// whole rows.  Same steps and scalar rules as bcg_run<float>; the direction
-// update is fused into the SpMM (P alternates between the two buffers).
-// s.acol and s.mask must be set.  Returns niter or -1.
+// The same FP32 block CG with the four vectors stored row-interleaved: R, X,
+// P, W are n x KW float arrays (element (r, c) at r*KW + c, KW = len rounded
+// up to a multiple of 4, rows 16-byte aligned) for len <= 16, so the SpMM
+// gathers one contiguous KW-float row per nonzero and every vector kernel
+// streams whole rows.  Same steps, scalars and reductions (same order) as
+// bcg_run<float>; s.acol and s.mask must be set.  Returns niter or -1.
 int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, float* R, float* X,
-                     float* P, float* P2, float* W, int len, int max_it, double rate,
-                     const BcgScalars& s, double* partial, cudaStream_t st, int* launches);
+                     float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
+                     double* partial, cudaStream_t st, int* launches);
 inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
 // Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 16).
 void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,

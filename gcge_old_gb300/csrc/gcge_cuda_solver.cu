@@ -467,7 +467,7 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
     CHK(mat_ensure_f32(s->A->m, s->st));
     // four column blocks of the block CG, wide enough for the row-interleaved
     // layout (block size rounded up to 4)
-    const size_t f32n = (size_t)s->ldn * 5 * gcge::bcg_rows_width(s->bs);
+    const size_t f32n = (size_t)s->ldn * 4 * gcge::bcg_rows_width(s->bs);
     CU(cudaMalloc(&s->pool32, sizeof(float) * f32n));
     CU(cudaMemsetAsync(s->pool32, 0, sizeof(float) * f32n, s->st));
     float* f = s->pool32;
@@ -836,13 +836,12 @@ static int compute_w(Solver* s) {
       float* Rr = s->pool32;
       float* Xr = Rr + blk;
       float* Pr = Xr + blk;
-      float* Pr2 = Pr + blk;
-      float* Wr = Pr2 + blk;
+      float* Wr = Pr + blk;
       KL(gcge::cols_to_rows_f32(R, wl, Rr, s->n, s->st));
       CU(cudaMemsetAsync(Xr, 0, sizeof(float) * blk, s->st));
-      steps = gcge::bcg_run_rows_f32(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, Rr, Xr, Pr, Pr2,
-                                     Wr, wl, s->para.cg_max_it, s->para.cg_rate, s->bcg,
-                                     s->partial, s->st, &launches);
+      steps = gcge::bcg_run_rows_f32(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, Rr, Xr, Pr, Wr,
+                                     wl, s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial,
+                                     s->st, &launches);
       KL(gcge::rows_add_to_cols_f64(Xr, wl, Wc, s->n, s->st));
     } else {
       ColList<float> fr = colsf(s->f_rhs, 0, wl), fx = colsf(s->f_x, 0, wl);
