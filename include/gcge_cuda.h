@@ -132,8 +132,9 @@ int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int
  * triangle and mirrors it (MultiVecInnerProd, src/gcge_ops.h:113-114). */
 int GCGE_CUDA_MultiVecInnerProd(double* const* V, int k1, double* const* W, int k2, int n,
                                 double* a, int lda, int sym);
-/* The same inner products with FP64 accuracy on the bf16 tensor cores
- * (per-32-row column scaling, 8 slices of 7 bits, exact level sums). */
+/* The same inner products with FP64 accuracy on the tcgen05 bf16 tensor
+ * cores: per-64-row column scaling, 7 balanced base-256 digits per value,
+ * exact FP32 level sums in tensor memory, 64-bit fixed-point combination. */
 int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W, int k2, int n,
                                      double* a, int lda, int sym);
 /* Allocation-free FP64 inner products (no counterpart in the reference):
@@ -155,12 +156,13 @@ int GCGE_CUDA_MultiVecInnerProdNoAlloc(double* const* V, int k1, double* const* 
  * (MultiVecLinearComb, src/gcge_ops.h:109-111). */
 int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int k2, int n,
                                  const double* a, int lda, double beta);
-/* The same linear combination with FP64 accuracy computed on the bf16
- * tensor cores (error-free splitting into 8 slices of 7 bits, exact FP32
- * level sums, 64-bit fixed-point combination); the solver's default for
- * its X, P and W updates on GB300, where FP64 FMA is ~600x slower than
- * bf16 MMA.  The columns of x are balanced by powers of two first, so
- * columns of very different magnitude keep their accuracy. */
+/* The same linear combination with FP64 accuracy computed on the tcgen05
+ * bf16 tensor cores (per-row scaling, 7 balanced base-256 digits per value,
+ * exact FP32 level sums in tensor memory, 64-bit fixed-point combination);
+ * the solver's default for its X, P and W updates on GB300, where FP64 FMA
+ * runs at ~1 TFLOP/s against ~2 PFLOP/s of bf16 MMA.  The columns of x are
+ * balanced by powers of two first, so columns of very different magnitude
+ * keep their accuracy. */
 int GCGE_CUDA_MultiVecLinearCombOzaki(double* const* x, int k1, double* const* y, int k2, int n,
                                       const double* a, int lda, double beta);
 /* y[j] = alpha x[j] + beta y[j] (MultiVecAxpby, src/gcge_ops.h:98-99) */
