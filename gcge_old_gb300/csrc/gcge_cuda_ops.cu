@@ -85,6 +85,32 @@ extern "C" int GCGE_CUDA_MatDotMultiVecF32Async(GCGE_CUDA_MAT* A, float* const* 
   return cudaGetLastError() == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
 }
 
+namespace {
+// grad[e] = sum_j c_j x_j[row(e)] x_j[col(e)] over the stored entries e of M
+__global__ void k_eiggrad(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                          ColList<double> X, DblList c, int k, double* __restrict__ grad) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int e = __ldg(rp + r); e < __ldg(rp + r + 1); e++) {
+    const int col = __ldg(ci + e);
+    double s = 0.0;
+    for (int j = 0; j < k; j++) s = fma(c.v[j] * X.p[j][r], X.p[j][col], s);
+    grad[e] = s;
+  }
+}
+}  // namespace
+
+extern "C" int GCGE_CUDA_EigGradCSR(const GCGE_CUDA_MAT* M, double* const* x, const double* coef,
+                                    int k, double* grad) {
+  if (!M || !x || !coef || !grad || k <= 0 || k > GCGE_MAXCOLS) return GCGE_CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  DblList c;
+  for (int j = 0; j < k; j++) c.v[j] = coef[j];
+  if (M->m.n > 0)
+    k_eiggrad<<<(M->m.n + 255) / 256, 256>>>(M->m.n, M->m.rp, M->m.ci, mk(x, k), c, k, grad);
+  return finish();
+}
+
 extern "C" int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k,
                                             void* stream) {
   if (!A || !x || !y || k <= 0 || k > 16 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))

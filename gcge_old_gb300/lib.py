@@ -69,6 +69,7 @@ SIGNATURES = {
     "GCGE_CUDA_MatDotMultiVec": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int]),
     "GCGE_CUDA_MatDotMultiVecAsync": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MatDotMultiVecF32Async": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int, C.c_void_p]),
+    "GCGE_CUDA_EigGradCSR": (C.c_int, [C.c_void_p, c_pp, C.c_void_p, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MatDotRowsF32Async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                                C.c_void_p]),
     "GCGE_CUDA_MultiVecInnerProd": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int, C.c_void_p,

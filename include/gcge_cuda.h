@@ -108,6 +108,16 @@ GCGE_CUDA_SOLVER* GCGE_CUDA_Solver_Init(const GCGE_CUDA_CSR_HOST* A, const GCGE_
  * (GCGE_SOLVER_Free_All, src/gcge_solver.c:75-82). */
 int GCGE_CUDA_SOLVER_Free_All(GCGE_CUDA_SOLVER** solver);
 
+/* ---------------------------------------------------------------- eigenvalue adjoint
+ * grad[e] = sum_j coef[j] * x[j][row(e)] * x[j][col(e)] for every stored entry e of M
+ * (grad: DEVICE array of nnz doubles, in M's CSR order; x: k device columns of length n;
+ * coef: host array of k doubles; synchronous).  For B-normalised eigenpairs
+ * (lambda_j, x_j) of A x = lambda B x and a loss L(lambda), dL/dA over A's pattern is this
+ * with coef = dL/dlambda, and dL/dB over B's pattern with coef = -lambda dL/dlambda.
+ * The reference has no derivatives; this is the adjoint of the eigenvalues it computes. */
+int GCGE_CUDA_EigGradCSR(const GCGE_CUDA_MAT* M, double* const* x, const double* coef, int k,
+                         double* grad);
+
 /* ---------------------------------------------------------------- multivector ops
  * Device kernels in the shape of the GCGE_OPS multivector callbacks
  * (src/gcge_ops.h:76-127).  Columns are device pointers of length n; the
