@@ -13,14 +13,22 @@ everything else) with the matrices and the initial block resident in HBM,
 timed with CUDA events on the solver's stream; fp64_s: the all-FP64 form.
 e2e: the same solve through the C ABI with HOST buffers: matrix upload,
 initial block upload and eigenvector download inside the timed region.
-roofline: the FP64 CSR SpMM on the W block (k = block size = 10), algorithmic
-bytes nnz*12 + 4(n+1) + 2*k*n*8 per launch.
+roofline: the SpMM of the mixed solve's block CG: FP32 CSR SpMM on
+row-interleaved blocks (k = block size = 10), algorithmic bytes
+nnz*8 + 4(n+1) + 2*k*n*4 per launch; the FP64 SpMM rate (bound by GB300's
+FP64 FMA rate) is reported beside it.
 cpu_baseline: the oracle port (C restatement of the reference, OpenMP on all
 host cores) on a bounded sample of the same solve: the start phase plus one
 GCG iteration, extrapolated to the reference's iteration count.
 
 --impl reference runs that CPU path alone (rank 0), each step one bounded
 sample, and prints the same metric.
+
+--config 3 instead runs the mixed-precision configuration of the headline
+once in each precision: 27-point Q1 variable-coefficient diffusion (per-cell
+kappa = exp(N(0,1))) with its consistent mass on a 160^3 grid (n = 4,096,000,
+nnz = 109,215,352), nev = 100, and reports both times and the per-pair
+difference of the mixed result from the FP64 one (not the default line).
 """
 from __future__ import annotations
 
@@ -258,11 +266,19 @@ def true_residuals_gpu(torch, A, B, ev, evec_rows):
     a = torch.sparse_csr_tensor(torch.from_numpy(A.rowptr.astype(np.int64)),
                                 torch.from_numpy(A.col.astype(np.int64)),
                                 torch.from_numpy(A.val), size=(A.n, A.n)).to("cuda")
-    bd = torch.from_numpy(B.val).to("cuda")
     X = evec_rows.T.contiguous()  # n x nev
     AX = a @ X
     lam = torch.from_numpy(ev).to("cuda")
-    R = AX - lam[None, :] * (bd[:, None] * X)
+    if B.nnz == B.n and np.array_equal(B.col, np.arange(B.n)):
+        BX = torch.from_numpy(B.val).to("cuda")[:, None] * X
+    else:
+        b = torch.sparse_csr_tensor(torch.from_numpy(B.rowptr.astype(np.int64)),
+                                    torch.from_numpy(B.col.astype(np.int64)),
+                                    torch.from_numpy(B.val), size=(B.n, B.n)).to("cuda")
+        BX = b @ X
+        del b
+    del a
+    R = AX - lam[None, :] * BX
     return (R.norm(dim=0) / (lam.abs() * X.norm(dim=0))).cpu().numpy()
 
 
@@ -316,6 +332,43 @@ def run_reference_arm(args):
     return 0
 
 
+def run_config3(args):
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    from gcge_old_gb300 import lib as L
+    from gcge_old_gb300 import matrices as M
+    from gcge_old_gb300 import solver as S
+    m, nev = 160, 100
+    t0 = time.time()
+    A, B = M.diffusion27(m, seed=0)
+    x0 = M.initial_block(A.n, nev, seed=0)
+    gen_s = time.time() - t0
+    dA, dB = S.DeviceMatrix(A), S.DeviceMatrix(B)
+    x0_dev = torch.from_numpy(x0).to("cuda")
+    res = {}
+    for prec in ("mixed", "fp64"):
+        t, st, ev, vec = time_solves(torch, S, L, dA, dB, nev, x0_dev, prec, 0, 1)
+        r = true_residuals_gpu(torch, A, B, ev, vec)
+        res[prec] = {"s": t[0], "gcg_iterations": st[0]["num_iter"], "bcg_steps": st[0]["bcg_steps"],
+                     "max_residual": float(r.max()), "ev": ev,
+                     "phase_s": {k: round(v, 3) for k, v in st[0].items() if k.startswith("t_")}}
+        del vec
+        torch.cuda.empty_cache()
+    ev_m, ev_d = res["mixed"].pop("ev"), res["fp64"].pop("ev")
+    rel = np.abs(ev_m - ev_d) / np.abs(ev_d)
+    out = {"metric": METRIC, "config": {"workload": "diffusion27_q1_lognormal_%d^3_consistent_mass_"
+                                                    "nev100_tol1e-10" % m,
+                                        "n": A.n, "nnz_A": A.nnz, "nnz_B": B.nnz, "nev": nev},
+           "unit": "s", "mixed": res["mixed"], "fp64": res["fp64"],
+           "mixed_speedup_vs_fp64": res["fp64"]["s"] / res["mixed"]["s"],
+           "per_pair_eigenvalue_rel_diff_mixed_vs_fp64": {"max": float(rel.max()),
+                                                          "median": float(np.median(rel))},
+           "generator_s": gen_s, "data": "synthetic (seeded generator)"}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -324,9 +377,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="48^3 grid (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
+                    help="3: the 160^3 27-point mixed-precision configuration (one solve each)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.config == 3:
+        return run_config3(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
