@@ -282,12 +282,12 @@ __device__ __forceinline__ void block_sum_cols(const float* acc, int len, double
   for (int c = 0; c < KW; c++) {
     double v = (double)acc[c];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[wid * 16 + c] = v;
+    if (lane == 0) sh[wid * 32 + c] = v;
   }
   __syncthreads();
   if ((int)threadIdx.x < len) {
     double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w * 16 + threadIdx.x];
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w * 32 + threadIdx.x];
     partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
   }
 }
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
                                                   const float* __restrict__ val,
                                                   const float* __restrict__ X, float* R, int len,
                                                   double* __restrict__ partial) {
-  __shared__ double sh[(kT / 32) * 16];
+  __shared__ double sh[(kT / 32) * 32];
   float acc2[KW];
 #pragma unroll
   for (int c = 0; c < KW; c++) acc2[c] = 0.f;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ r
                                                 const float* __restrict__ val,
                                                 const float* __restrict__ P, float* W, int len,
                                                 BcgScalars s, double* __restrict__ partial) {
-  __shared__ double sh[(kT / 32) * 16];
+  __shared__ double sh[(kT / 32) * 32];
   if (*s.nu == 0) return;
   bool on[KW];
 #pragma unroll
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kT) k_rows_update(int n, float* X, float* R,
                                                     const float* __restrict__ P,
                                                     const float* __restrict__ W, int len,
                                                     BcgScalars s, double* __restrict__ partial) {
-  __shared__ double sh[(kT / 32) * 16];
+  __shared__ double sh[(kT / 32) * 32];
   if (*s.nu == 0) return;
   bool on[KW];
   float alpha[KW];
@@ -445,9 +445,9 @@ __global__ void __launch_bounds__(kT) k_rows_update(int n, float* X, float* R,
 
 // column sums of the per-block partials: warp w adds column w (lanes take
 // blocks lane, lane + 32, ...; then a fixed shuffle tree), so the order is
-// fixed.  Launched with 512 threads (16 warps, one per column).
+// fixed.  Launched with 1024 threads (32 warps, one per column).
 __device__ __forceinline__ void reduce_cols(const double* __restrict__ partial, int nblk, int len,
-                                            double* out /* shared, 16 */) {
+                                            double* out /* shared, 32 */) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (w < len) {
     double v = 0.0;
@@ -461,11 +461,11 @@ __device__ __forceinline__ void reduce_cols(const double* __restrict__ partial, 
 // initial rho2 (by column), err, lerr, active list and mask
 __global__ void k_rows_init_ctrl(const double* __restrict__ partial, int nblk, int len,
                                  BcgScalars s) {
-  __shared__ double rr[16];
+  __shared__ double rr[32];
   reduce_cols(partial, nblk, len, rr);
   if (threadIdx.x != 0) return;
   int nu = 0;
-  for (int c = 0; c < 16; c++) s.mask[c] = 0;
+  for (int c = 0; c < 32; c++) s.mask[c] = 0;
   for (int idx = 0; idx < len; idx++) {
     s.rho2[idx] = rr[idx];
     s.err[idx] = sqrt(s.rho2[idx]);
@@ -482,7 +482,7 @@ __global__ void k_rows_init_ctrl(const double* __restrict__ partial, int nblk, i
 // ptw[id] = p.w of column unl[id]; alpha of that column = rho2[id] / ptw[id]
 __global__ void k_rows_alpha(const double* __restrict__ partial, int nblk, int len,
                              BcgScalars s) {
-  __shared__ double pw[16];
+  __shared__ double pw[32];
   const int nu = *s.nu;
   if (nu == 0) return;
   reduce_cols(partial, nblk, len, pw);
@@ -497,7 +497,7 @@ __global__ void k_rows_alpha(const double* __restrict__ partial, int nblk, int l
 // rnew[id] = r.r of column unl[id]; then the step control of k_ctrl_step and the mask
 __global__ void k_rows_step(const double* __restrict__ partial, int nblk, int len, BcgScalars s,
                             double rate, int slot) {
-  __shared__ double rr[16];
+  __shared__ double rr[32];
   const int nu = *s.nu;
   if (nu == 0) {
     if (threadIdx.x == 0) s.nu_host[slot] = 0;
@@ -511,7 +511,7 @@ __global__ void k_rows_step(const double* __restrict__ partial, int nblk, int le
     s.rho2[id] = s.rnew[id];
   }
   for (int id = 0; id < nu; id++) s.lerr[s.unl[id]] = sqrt(fabs(s.rho2[id]));
-  for (int c = 0; c < 16; c++) s.mask[c] = 0;
+  for (int c = 0; c < 32; c++) s.mask[c] = 0;
   int m = 0;
   for (int id = 0; id < nu; id++) {
     const int idx = s.unl[id];
@@ -571,11 +571,12 @@ template <int KW>
 int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, float* X, float* P,
              float* W, int len, int max_it, double rate, const BcgScalars& s, double* partial,
              cudaStream_t st, int* launches) {
-  // four CTAs of 8 warps per SM for the row-streaming kernels
-  const int nb = min((n + kT - 1) / kT, 4 * 152);
+  // four CTAs of 8 warps per SM for the row-streaming kernels (two from 20
+  // columns up, where the update kernel holds over 100 registers a thread)
+  const int nb = min((n + kT - 1) / kT, (KW <= 16 ? 4 : 2) * 152);
   int nl = 0;
   k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial);
-  k_rows_init_ctrl<<<1, 512, 0, st>>>(partial, nb, len, s);
+  k_rows_init_ctrl<<<1, 1024, 0, st>>>(partial, nb, len, s);
   nl += 2;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
   int niter = 1;
@@ -585,9 +586,9 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
     for (int j = 0; j < batch; j++) {
       k_rows_p<KW><<<nb, kT, 0, st>>>(n, R, P, s, niter + j == 1 ? 1 : 0);
       k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial);
-      k_rows_alpha<<<1, 512, 0, st>>>(partial, nb, len, s);
+      k_rows_alpha<<<1, 1024, 0, st>>>(partial, nb, len, s);
       k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
-      k_rows_step<<<1, 512, 0, st>>>(partial, nb, len, s, rate, j);
+      k_rows_step<<<1, 1024, 0, st>>>(partial, nb, len, s, rate, j);
       nl += 5;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
@@ -612,6 +613,10 @@ int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, floa
     case 8: return rows_run<8>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
     case 12: return rows_run<12>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
     case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 20: return rows_run<20>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 24: return rows_run<24>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 28: return rows_run<28>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 32: return rows_run<32>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
   }
   return -1;
 }
@@ -624,6 +629,10 @@ void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const 
     case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
     case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
     case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 20: k_rows_spmm<20><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 24: k_rows_spmm<24><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 28: k_rows_spmm<28><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 32: k_rows_spmm<32><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
   }
 }
 
@@ -634,6 +643,10 @@ void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaS
     case 8: k_cols_to_rows<8><<<g, 256, 0, st>>>(R, len, Rr, n); break;
     case 12: k_cols_to_rows<12><<<g, 256, 0, st>>>(R, len, Rr, n); break;
     case 16: k_cols_to_rows<16><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 20: k_cols_to_rows<20><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 24: k_cols_to_rows<24><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 28: k_cols_to_rows<28><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 32: k_cols_to_rows<32><<<g, 256, 0, st>>>(R, len, Rr, n); break;
   }
 }
 
@@ -645,6 +658,10 @@ void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, in
     case 8: k_rows_add<8><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
     case 12: k_rows_add<12><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
     case 16: k_rows_add<16><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 20: k_rows_add<20><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 24: k_rows_add<24><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 28: k_rows_add<28><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 32: k_rows_add<32><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
   }
 }
 

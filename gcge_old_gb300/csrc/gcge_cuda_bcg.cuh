@@ -17,8 +17,8 @@ struct BcgScalars {
   int* unl;
   int* nu;
   volatile int* nu_host;
-  double* acol;  // row-interleaved path: alpha of each column (16 doubles)
-  int* mask;     // row-interleaved path: 1 for the active columns (16 ints)
+  double* acol;  // row-interleaved path: alpha of each column (32 doubles)
+  int* mask;     // row-interleaved path: 1 for the active columns (32 ints)
 };
 
 // Solves A x_c = rhs_c for the len columns (rhs is overwritten by the
@@ -39,7 +39,7 @@ int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, floa
                      float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
                      double* partial, cudaStream_t st, int* launches);
 inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
-// Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 16).
+// Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 32).
 void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
                    float* Y, int k, cudaStream_t st);
 // Rr (n x KW rows) <- FP64 columns R[0:len] (zero-padded); Y[c] += Xr[:, c].

@@ -113,7 +113,7 @@ extern "C" int GCGE_CUDA_EigGradCSR(const GCGE_CUDA_MAT* M, double* const* x, co
 
 extern "C" int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k,
                                             void* stream) {
-  if (!A || !x || !y || k <= 0 || k > 16 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))
+  if (!A || !x || !y || k <= 0 || k > 32 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))
     return GCGE_CUDA_ERR_ARG;
   if (!A->m.v32) {
     if (cudaMalloc(&A->m.v32, sizeof(float) * (A->m.nnz > 0 ? A->m.nnz : 1)) != cudaSuccess)

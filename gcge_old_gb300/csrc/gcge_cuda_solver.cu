@@ -830,7 +830,7 @@ static int compute_w(Solver* s) {
     ColList<double> AW = cols(s->evec, 0, wl);
     KL(gcge::spmm_f64(s->A->m, Wc, AW, wl, s->st));
     KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
-    if (wl <= 16) {
+    if (wl <= 32) {
       // row-interleaved FP32 vectors: one contiguous row per SpMM gather
       const size_t blk = (size_t)s->ldn * gcge::bcg_rows_width(wl);
       float* Rr = s->pool32;

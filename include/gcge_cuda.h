@@ -134,7 +134,7 @@ int GCGE_CUDA_MatDotMultiVecF32Async(GCGE_CUDA_MAT* A, float* const* x, float* c
                                      void* stream);
 /* FP32 y = A x on row-interleaved blocks: x and y are device arrays of
  * n x round_up(k, 4) floats (element (r, c) at r*round_up(k,4) + c, 16-byte
- * aligned), k <= 16.  The operator of the mixed-precision block CG
+ * aligned), k <= 32.  The operator of the mixed-precision block CG
  * (GCGE_BCG, src/gcge_cg.c:429-445, on FP32 copies), whose gathers read one
  * contiguous row per nonzero; asynchronous on the given cudaStream_t. */
 int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k, void* stream);

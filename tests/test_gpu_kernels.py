@@ -32,7 +32,7 @@ def test_spmm_matches_csr_matdotvec(cuda_lib, gen, k):
     np.testing.assert_allclose(host(ys), ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max())
 
 
-@pytest.mark.parametrize("k", [1, 4, 10, 13, 16])
+@pytest.mark.parametrize("k", [1, 4, 10, 13, 16, 20, 32])
 def test_rows_spmm_matches_column_spmm(cuda_lib, k):
     """The row-interleaved FP32 operator of the mixed block CG equals A x
     column by column (FP32 sums of the same products in the same order)."""
@@ -52,9 +52,9 @@ def test_rows_spmm_matches_column_spmm(cuda_lib, k):
     ref = (A.to_scipy().astype(np.float64) @ X[:, :k].astype(np.float64))
     # FP32 products summed in FP32 over <= 7 entries per row
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-5 * np.abs(ref).max())
-    # bad arguments: more than 16 columns, misaligned rows
+    # bad arguments: more than 32 columns, misaligned rows
     assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(x.data_ptr()),
-                                                 C.c_void_p(y.data_ptr()), 17, None) == 1
+                                                 C.c_void_p(y.data_ptr()), 33, None) == 1
     assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(x.data_ptr() + 4),
                                                  C.c_void_p(y.data_ptr()), k, None) == 1
 
