@@ -111,6 +111,167 @@ extern "C" int GCGE_CUDA_EigGradCSR(const GCGE_CUDA_MAT* M, double* const* x, co
   return finish();
 }
 
+namespace {
+constexpr int kPcgBlocks = 304;
+
+__global__ void k_inv_diag(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                           const double* __restrict__ v, double* __restrict__ dinv) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double d = 0.0;
+  for (int e = rp[r]; e < rp[r + 1]; e++)
+    if (ci[e] == r) d += v[e];
+  dinv[r] = (d != 0.0) ? 1.0 / d : 1.0;
+}
+
+// partial[c * gridDim.x + b] = sum over this block's rows of X_c . Y_c
+__global__ void k_coldot(ColList<double> X, ColList<double> Y, int k, int n,
+                         double* __restrict__ partial) {
+  __shared__ double sh[256];
+  const int c = blockIdx.y;
+  double s = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    s = fma(X.p[c][r], Y.p[c][r], s);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(size_t)c * gridDim.x + blockIdx.x] = sh[0];
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int nblk, int k,
+                               double* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; b++) s += partial[(size_t)c * nblk + b];
+  out[c] = s;
+}
+
+// r = rhs - w (in place in rhs); z = D^-1 r; p = z
+__global__ void k_pcg_start(ColList<double> R, ColList<double> W, ColList<double> Z,
+                            ColList<double> P, const double* __restrict__ dinv, int n) {
+  const int c = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double r = R.p[c][i] - W.p[c][i];
+    R.p[c][i] = r;
+    const double z = dinv[i] * r;
+    Z.p[c][i] = z;
+    P.p[c][i] = z;
+  }
+}
+
+// x += alpha p, r -= alpha w
+__global__ void k_pcg_update(ColList<double> X, ColList<double> R, ColList<double> P,
+                             ColList<double> W, DblList alpha, int n) {
+  const int c = blockIdx.y;
+  const double a = alpha.v[c];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    X.p[c][i] = fma(a, P.p[c][i], X.p[c][i]);
+    R.p[c][i] = fma(-a, W.p[c][i], R.p[c][i]);
+  }
+}
+
+// z = D^-1 r
+__global__ void k_pcg_prec(ColList<double> R, ColList<double> Z, const double* __restrict__ dinv,
+                           int n) {
+  const int c = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    Z.p[c][i] = dinv[i] * R.p[c][i];
+}
+
+// p = z + beta p
+__global__ void k_pcg_dir(ColList<double> Z, ColList<double> P, DblList beta, int n) {
+  const int c = blockIdx.y;
+  const double b = beta.v[c];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    P.p[c][i] = fma(b, P.p[c][i], Z.p[c][i]);
+}
+
+// per-column dots X_c . Y_c (c < k) -> host array out
+int coldots(const ColList<double>& X, const ColList<double>& Y, int k, int n, double* partial,
+            double* dout, double* out, cudaStream_t st) {
+  k_coldot<<<dim3(kPcgBlocks, k), 256, 0, st>>>(X, Y, k, n, partial);
+  k_sum_partials<<<(k + 63) / 64, 64, 0, st>>>(partial, kPcgBlocks, k, dout);
+  if (cudaMemcpyAsync(out, dout, sizeof(double) * k, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  return cudaStreamSynchronize(st) == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
+}
+
+ColList<double> pick(const ColList<double>& X, const std::vector<int>& idx) {
+  ColList<double> c;
+  for (size_t j = 0; j < idx.size(); j++) c.p[j] = X.p[idx[j]];
+  return c;
+}
+}  // namespace
+
+extern "C" int GCGE_CUDA_JacobiPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs,
+                                   double* const* x, int k, int n, void* stream) {
+  if (!A || !rhs || !x || k <= 0 || k > GCGE_MAXCOLS || n != A->m.n) return GCGE_CUDA_ERR_ARG;
+  const GCGE_CUDA_PCG_PARAM* prm = static_cast<const GCGE_CUDA_PCG_PARAM*>(ctx);
+  const int max_it = prm ? prm->max_it : 20;
+  const double rate = prm ? prm->rate : 1e-2;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const size_t ld = ((size_t)n + 31) / 32 * 32;
+  const size_t need = 3 * (size_t)k * ld + ld + (size_t)kPcgBlocks * k + GCGE_MAXCOLS;
+  double* buf;
+  if (scratch(need, &buf)) return GCGE_CUDA_ERR_ALLOC;
+  ColList<double> R = mk(rhs, k), X = mk(x, k), Z, P, W;
+  for (int j = 0; j < k; j++) {
+    Z.p[j] = buf + (size_t)j * ld;
+    P.p[j] = buf + (size_t)(k + j) * ld;
+    W.p[j] = buf + (size_t)(2 * k + j) * ld;
+  }
+  double* dinv = buf + 3 * (size_t)k * ld;
+  double* partial = dinv + ld;
+  double* dout = partial + (size_t)kPcgBlocks * k;
+  const GcgeDevCsr& M = A->m;
+  k_inv_diag<<<(n + 255) / 256, 256, 0, st>>>(n, M.rp, M.ci, M.v, dinv);
+  gcge::spmm_f64(M, X, W, k, st);
+  k_pcg_start<<<dim3(kPcgBlocks, k), 256, 0, st>>>(R, W, Z, P, dinv, n);
+  std::vector<double> rz(k), r0(k), tmp(k);
+  int rc = coldots(R, R, k, n, partial, dout, r0.data(), st);
+  if (!rc) rc = coldots(R, Z, k, n, partial, dout, rz.data(), st);
+  if (rc) return rc;
+  std::vector<int> act;
+  for (int j = 0; j < k; j++) {
+    r0[j] = sqrt(r0[j]);
+    if (r0[j] > 0.0) act.push_back(j);
+  }
+  for (int it = 0; it < max_it && !act.empty(); it++) {
+    const int m = (int)act.size();
+    ColList<double> Ra = pick(R, act), Xa = pick(X, act), Za = pick(Z, act), Pa = pick(P, act),
+                    Wa = pick(W, act);
+    gcge::spmm_f64(M, Pa, Wa, m, st);
+    if ((rc = coldots(Pa, Wa, m, n, partial, dout, tmp.data(), st))) return rc;
+    DblList alpha;
+    for (int a = 0; a < m; a++) alpha.v[a] = tmp[a] != 0.0 ? rz[act[a]] / tmp[a] : 0.0;
+    k_pcg_update<<<dim3(kPcgBlocks, m), 256, 0, st>>>(Xa, Ra, Pa, Wa, alpha, n);
+    if ((rc = coldots(Ra, Ra, m, n, partial, dout, tmp.data(), st))) return rc;
+    std::vector<int> next;
+    for (int a = 0; a < m; a++)
+      if (sqrt(tmp[a]) >= rate * r0[act[a]]) next.push_back(act[a]);
+    if (next.empty() || it + 1 == max_it) break;
+    const int m2 = (int)next.size();
+    ColList<double> Rn = pick(R, next), Zn = pick(Z, next), Pn = pick(P, next);
+    k_pcg_prec<<<dim3(kPcgBlocks, m2), 256, 0, st>>>(Rn, Zn, dinv, n);
+    if ((rc = coldots(Rn, Zn, m2, n, partial, dout, tmp.data(), st))) return rc;
+    DblList beta;
+    for (int a = 0; a < m2; a++) {
+      beta.v[a] = rz[next[a]] != 0.0 ? tmp[a] / rz[next[a]] : 0.0;
+      rz[next[a]] = tmp[a];
+    }
+    k_pcg_dir<<<dim3(kPcgBlocks, m2), 256, 0, st>>>(Zn, Pn, beta, n);
+    act = next;
+  }
+  return cudaStreamSynchronize(st) == cudaSuccess && cudaGetLastError() == cudaSuccess
+             ? GCGE_CUDA_OK
+             : GCGE_CUDA_ERR_CUDA;
+}
+
 extern "C" int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k,
                                             void* stream) {
   if (!A || !x || !y || k <= 0 || k > 32 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))

@@ -239,6 +239,8 @@ struct GCGE_CUDA_SOLVER_ {
   size_t partial_len = 0;
   int* d_int = nullptr;
   gcge::BcgScalars bcg{};
+  GCGE_CUDA_MULTI_LINEAR_SOLVER mls = nullptr;  // user W-step solver
+  void* mls_ctx = nullptr;
   double* bcg_mem = nullptr;
   int* bcg_int = nullptr;
   int* h_pinned_int = nullptr;
@@ -309,6 +311,15 @@ extern "C" int GCGE_CUDA_SOLVER_SetEigenvectorsDevice(GCGE_CUDA_SOLVER* s, doubl
   s->evec_user = nullptr;
   return GCGE_CUDA_OK;
 }
+extern "C" int GCGE_CUDA_SOLVER_SetMultiLinearSolver(GCGE_CUDA_SOLVER* solver,
+                                                     GCGE_CUDA_MULTI_LINEAR_SOLVER fn,
+                                                     void* ctx) {
+  if (!solver) return set_err(GCGE_CUDA_ERR_ARG, "SetMultiLinearSolver: no solver");
+  solver->mls = fn;
+  solver->mls_ctx = fn ? ctx : nullptr;
+  return GCGE_CUDA_OK;
+}
+
 extern "C" int GCGE_CUDA_SOLVER_GetStream(GCGE_CUDA_SOLVER* s, void** stream) {
   if (!s || !stream) return set_err(GCGE_CUDA_ERR_ARG, "GetStream: null");
   if (!s->setup_done) return set_err(GCGE_CUDA_ERR_STATE, "GetStream: call Setup first");
@@ -816,6 +827,12 @@ static int compute_w(Solver* s) {
   KL((k_scale_copy<<<g, 256, 0, s->st>>>(R, R, scalars(rs), wl, s->n)));
   KL((k_scale_copy<<<g, 256, 0, s->st>>>(X, Wc, scalars(wsc), wl, s->n)));
   int launches = 0, steps;
+  if (s->mls) {
+    // a user block solver replaces the block CG (GCGE_OPS.MultiLinearSolver)
+    const int rc = s->mls(s->mls_ctx, s->A, R.p, Wc.p, wl, s->n, (void*)s->st);
+    if (rc != 0) return set_err(GCGE_CUDA_ERR_NUMERIC, "user linear solver returned %d", rc);
+    return GCGE_CUDA_OK;
+  }
   if (s->para.precision == 0) {
     steps = gcge::bcg_run<double>(s->A->m.rp, s->A->m.ci, s->A->m.v, s->n, R, Wc,
                                   cols(s->CG_p, 0, wl), cols(s->evec, 0, wl), wl,

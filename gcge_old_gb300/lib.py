@@ -24,6 +24,16 @@ class CSRHost(C.Structure):
                 ("KCol", c_int_p), ("RowPtr", c_int_p), ("Entries", c_double_p)]
 
 
+class PCGParam(C.Structure):
+    """GCGE_CUDA_PCG_PARAM: steps and relative residual target of GCGE_CUDA_JacobiPCG."""
+    _fields_ = [("max_it", C.c_int), ("rate", C.c_double)]
+
+
+# GCGE_CUDA_MULTI_LINEAR_SOLVER(ctx, A, rhs, x, k, n, stream)
+MultiLinearSolver = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
+                                C.c_void_p)
+
+
 class Stats(C.Structure):
     """GCGE_CUDA_STATS."""
     _fields_ = [("num_iter", C.c_int), ("num_conv_continuous", C.c_int), ("bcg_steps", C.c_int),
@@ -69,6 +79,9 @@ SIGNATURES = {
     "GCGE_CUDA_MatDotMultiVec": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int]),
     "GCGE_CUDA_MatDotMultiVecAsync": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MatDotMultiVecF32Async": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int, C.c_void_p]),
+    "GCGE_CUDA_SOLVER_SetMultiLinearSolver": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "GCGE_CUDA_JacobiPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
+                                      C.c_void_p]),
     "GCGE_CUDA_EigGradCSR": (C.c_int, [C.c_void_p, c_pp, C.c_void_p, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MatDotRowsF32Async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                                C.c_void_p]),

@@ -88,6 +88,23 @@ class GCGESolver:
         L.check(self._lib.GCGE_CUDA_SOLVER_SetEigenvectors(h, _ptr(self.evec)), "SetEigenvectors")
         L.check(self._lib.GCGE_CUDA_SOLVER_Setup(h), "Setup")
 
+    def set_linear_solver(self, fn, ctx=None):
+        """Replace the built-in block CG of the W step (GCGE_OPS.MultiLinearSolver,
+        src/gcge_ops.h:77) by fn, a lib.MultiLinearSolver or a C function address;
+        fn=None restores the built-in block CG.  fn and ctx must outlive the solves."""
+        self._mls = (fn, ctx)
+        if fn is not None and not isinstance(fn, L.MultiLinearSolver):
+            fn = C.cast(fn, L.MultiLinearSolver)
+        cp = C.cast(C.pointer(ctx), C.c_void_p) if isinstance(ctx, C.Structure) else ctx
+        L.check(self._lib.GCGE_CUDA_SOLVER_SetMultiLinearSolver(
+            self.handle, C.cast(fn, C.c_void_p) if fn is not None else None, cp),
+            "SetMultiLinearSolver")
+
+    def use_jacobi_pcg(self, max_it: int = 20, rate: float = 1e-2):
+        """W step by GCGE_CUDA_JacobiPCG: block CG preconditioned by diag(A)."""
+        self._pcg = L.PCGParam(max_it, rate)
+        self.set_linear_solver(self._lib.GCGE_CUDA_JacobiPCG, self._pcg)
+
     def solve(self, x0: np.ndarray):
         """x0: initial block, shape (nev, n) (= column-major n x nev)."""
         self.evec[...] = np.asarray(x0, dtype=np.float64).reshape(self.nev, self.n)

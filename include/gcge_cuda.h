@@ -85,6 +85,28 @@ int GCGE_CUDA_SOLVER_SetEigenvectors(GCGE_CUDA_SOLVER* solver, double* evec);
  * evec + j*n): the initial block is read from and the result written to
  * device memory, so a caller that keeps its data in HBM pays no transfer. */
 int GCGE_CUDA_SOLVER_SetEigenvectorsDevice(GCGE_CUDA_SOLVER* solver, double* evec);
+/* A block linear solver for the W step in place of the built-in block CG
+ * (GCGE_OPS.MultiLinearSolver, src/gcge_ops.h:77, called at src/gcge_xpw.c:178-191):
+ * on entry x[j] holds the initial guess and rhs[j] the right-hand side of
+ * A x[j] = rhs[j] (device columns of length n, j < k, FP64 in both precision
+ * modes); on return x[j] holds the approximate solution; rhs may be overwritten.
+ * stream is the solver's cudaStream_t (all earlier work is queued on it); the
+ * callback returns 0 on success.  fn = NULL restores the built-in block CG. */
+typedef int (*GCGE_CUDA_MULTI_LINEAR_SOLVER)(void* ctx, const GCGE_CUDA_MAT* A,
+                                             double* const* rhs, double* const* x, int k,
+                                             int n, void* stream);
+int GCGE_CUDA_SOLVER_SetMultiLinearSolver(GCGE_CUDA_SOLVER* solver,
+                                          GCGE_CUDA_MULTI_LINEAR_SOLVER fn, void* ctx);
+/* A stock GCGE_CUDA_MULTI_LINEAR_SOLVER: block CG preconditioned by the diagonal of A
+ * (per column: z = D^-1 r, p = z + beta p), on the GPU; ctx points to a
+ * GCGE_CUDA_PCG_PARAM (NULL: 20 steps, rate 1e-2).  A column stops once
+ * ||r|| < rate ||r_0||, as the built-in block CG does. */
+typedef struct GCGE_CUDA_PCG_PARAM_ {
+  int max_it;
+  double rate;
+} GCGE_CUDA_PCG_PARAM;
+int GCGE_CUDA_JacobiPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs, double* const* x,
+                        int k, int n, void* stream);
 /* The CUDA stream (cudaStream_t) the solver runs on, for event timing. */
 int GCGE_CUDA_SOLVER_GetStream(GCGE_CUDA_SOLVER* solver, void** stream);
 int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* solver, int argc, char** argv);
