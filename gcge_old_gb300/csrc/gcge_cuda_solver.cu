@@ -74,6 +74,7 @@ extern "C" const char* GCGE_CUDA_GetErrorString(int code) {
     case GCGE_CUDA_ERR_ALLOC: return "allocation failed";
     case GCGE_CUDA_ERR_STATE: return "invalid solver state";
     case GCGE_CUDA_ERR_NUMERIC: return "numerical failure";
+    case GCGE_CUDA_ERR_IO: return "file error";
   }
   return "unknown error";
 }
@@ -164,6 +165,13 @@ extern "C" int GCGE_CUDA_MatCreateFromCSR(GCGE_CUDA_MAT** mat, const GCGE_CUDA_C
   if (!csr || csr->N_Rows != csr->N_Columns)
     return set_err(GCGE_CUDA_ERR_ARG, "MatCreateFromCSR: matrix must be square");
   return GCGE_CUDA_MatCreate(mat, csr->N_Rows, csr->RowPtr, csr->KCol, csr->Entries, 0);
+}
+
+extern "C" int GCGE_CUDA_MatGetSize(const GCGE_CUDA_MAT* mat, int* n, int* nnz) {
+  if (!mat) return set_err(GCGE_CUDA_ERR_ARG, "MatGetSize: null matrix");
+  if (n) *n = mat->m.n;
+  if (nnz) *nnz = mat->m.nnz;
+  return GCGE_CUDA_OK;
 }
 
 extern "C" int GCGE_CUDA_MatDestroy(GCGE_CUDA_MAT** mat) {

@@ -54,6 +54,12 @@ SIGNATURES = {
     "GCGE_CUDA_MatCreate": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_int]),
     "GCGE_CUDA_MatDestroy": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "GCGE_CUDA_MatGetSize": (C.c_int, [C.c_void_p, c_int_p, c_int_p]),
+    "GCGE_CUDA_CSR_ReadFile": (C.c_int, [C.c_char_p, C.POINTER(CSRHost)]),
+    "GCGE_CUDA_CSR_WriteText": (C.c_int, [C.c_char_p, C.POINTER(CSRHost)]),
+    "GCGE_CUDA_CSR_WriteBinary": (C.c_int, [C.c_char_p, C.POINTER(CSRHost)]),
+    "GCGE_CUDA_CSR_Free": (C.c_int, [C.POINTER(CSRHost)]),
+    "GCGE_CUDA_MatCreateFromFile": (C.c_int, [C.POINTER(C.c_void_p), C.c_char_p]),
     "GCGE_CUDA_SOLVER_Create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "GCGE_CUDA_SOLVER_SetMatA": (C.c_int, [C.c_void_p, C.c_void_p]),
     "GCGE_CUDA_SOLVER_SetMatB": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -34,6 +34,22 @@ class DeviceMatrix:
                                               _ptr(self._h[2]), 0), "MatCreate")
         self.handle = h
 
+    @classmethod
+    def from_file(cls, path) -> "DeviceMatrix":
+        """A square matrix read straight from a CSR text or PETSc binary file
+        (GCGE_CUDA_MatCreateFromFile)."""
+        import os
+        self = cls.__new__(cls)
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.GCGE_CUDA_MatCreateFromFile(C.byref(h), os.fsencode(path)),
+                "MatCreateFromFile")
+        self.handle = h
+        n = C.c_int()
+        L.check(self._lib.GCGE_CUDA_MatGetSize(h, C.byref(n), None), "MatGetSize")
+        self.n = n.value
+        return self
+
     def close(self):
         if self.handle:
             h = self.handle

@@ -26,6 +26,7 @@ extern "C" {
 #define GCGE_CUDA_ERR_ALLOC 3
 #define GCGE_CUDA_ERR_STATE 4
 #define GCGE_CUDA_ERR_NUMERIC 5
+#define GCGE_CUDA_ERR_IO 6 /* file missing, unreadable or malformed */
 
 /* Layout-compatible with the reference's CSR_MAT (app/csr/gcge_app_csr.h:27-41):
  * 0-based int32 row pointers and column indices, double entries, so a
@@ -66,6 +67,26 @@ int GCGE_CUDA_MatCreateFromCSR(GCGE_CUDA_MAT** mat, const GCGE_CUDA_CSR_HOST* cs
 int GCGE_CUDA_MatCreate(GCGE_CUDA_MAT** mat, int n, const int* rowptr, const int* col,
                         const double* val, int on_device);
 int GCGE_CUDA_MatDestroy(GCGE_CUDA_MAT** mat);
+/* Rows (= columns) and stored entries of a device matrix. */
+int GCGE_CUDA_MatGetSize(const GCGE_CUDA_MAT* mat, int* n, int* nnz);
+
+/* ---------------------------------------------------------------- matrix files
+ * Text: the reference's CSR file (CSR_ReadMatFile, app/csr/gcge_app_csr.c:185-236):
+ * nrow, ncol, nnz, rowptr[nrow+1], col[nnz], val[nnz], whitespace separated,
+ * 0-based; written with 17 significant digits, so it reads back bit-exact.
+ * Binary: PETSc's Mat binary format (what the reference's PETSc app loads,
+ * test/data/*.petsc.bin): big-endian int32 classid 1211216, rows, cols, nnz,
+ * row lengths, col, then big-endian float64 val; 32-bit indices.
+ * CSR_ReadFile picks the format from the first four bytes, checks the
+ * structure (row pointers 0..nnz without decrease, columns in range) and
+ * fills csr with malloc'd arrays that CSR_Free releases.  Errors:
+ * GCGE_CUDA_ERR_IO with the reason in GCGE_CUDA_GetLastErrorMessage. */
+int GCGE_CUDA_CSR_ReadFile(const char* path, GCGE_CUDA_CSR_HOST* csr);
+int GCGE_CUDA_CSR_WriteText(const char* path, const GCGE_CUDA_CSR_HOST* csr);
+int GCGE_CUDA_CSR_WriteBinary(const char* path, const GCGE_CUDA_CSR_HOST* csr);
+int GCGE_CUDA_CSR_Free(GCGE_CUDA_CSR_HOST* csr);
+/* CSR_ReadFile + MatCreateFromCSR (square matrices). */
+int GCGE_CUDA_MatCreateFromFile(GCGE_CUDA_MAT** mat, const char* path);
 
 /* ---------------------------------------------------------------- solver
  * Mirrors GCGE_SOLVER (src/gcge_solver.h:42-60): Create, Set*, Setup,

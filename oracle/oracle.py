@@ -124,6 +124,34 @@ def ref_lib():
     return _ref
 
 
+class _RefCSR(C.Structure):
+    # CSR_MAT of app/csr/gcge_app_csr.h:27-41
+    _fields_ = [("N_Rows", C.c_int), ("N_Columns", C.c_int), ("N_Entries", C.c_int),
+                ("KCol", C.POINTER(C.c_int)), ("RowPtr", C.POINTER(C.c_int)),
+                ("Entries", C.POINTER(C.c_double))]
+
+
+def ref_read_csr(path: str):
+    """The reference's own CSR_ReadMatFile (app/csr/gcge_app_csr.c:185-236) on a
+    text file: returns (nrow, ncol, rowptr, col, val) as numpy arrays.  The
+    reference exits the process on a missing file, so the path is checked first."""
+    import numpy as np
+    if not os.path.exists(path):
+        raise FileNotFoundError(path)
+    lib = ref_lib()
+    lib.CSR_ReadMatFile.restype = C.POINTER(_RefCSR)
+    lib.CSR_ReadMatFile.argtypes = [C.c_char_p]
+    m = lib.CSR_ReadMatFile(os.fsencode(path))
+    c = m.contents
+    n, nnz = c.N_Rows, c.N_Entries
+    out = (n, c.N_Columns, np.ctypeslib.as_array(c.RowPtr, (n + 1,)).copy(),
+           np.ctypeslib.as_array(c.KCol, (nnz,)).copy(),
+           np.ctypeslib.as_array(c.Entries, (nnz,)).copy())
+    lib.CSR_MatFree.argtypes = [C.POINTER(C.POINTER(_RefCSR))]
+    lib.CSR_MatFree(C.byref(m))
+    return out
+
+
 def ref_solve(A, B, nev, x0, flags: dict | None = None):
     """Run the unmodified reference through GCGE_CSR_Solver_Init / Solve with
     the initial block x0 passed as num_init_evec = nev."""
