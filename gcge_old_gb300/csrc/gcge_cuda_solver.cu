@@ -32,6 +32,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <string>
 #include <vector>
@@ -218,6 +219,14 @@ struct Para {
   // Ozaki only for the linear combinations / only for the Gram blocks
   int gemm = 1;
   int print_level = 0;
+  // shift (GCGE_PARA use_shift / if_shift / shift, src/gcge_para.h:90-92):
+  // use_shift = 1 recomputes if_shift = 1 and shift from the Ritz values after
+  // every convergence check; if_shift = 1 with shift set gives a fixed shift.
+  // The block CG then solves (A + shift B) w = (lambda + shift) B x.
+  int use_shift = 0;
+  int if_shift = 0;
+  double shift = 0.0;
+  int eval_type = 0;  // 0 "sa" (smallest algebraic), 1 "sm" (smallest magnitude)
 };
 
 // ------------------------------------------------------------------ solver
@@ -247,6 +256,14 @@ struct GCGE_CUDA_SOLVER_ {
   size_t partial_len = 0;
   int* d_int = nullptr;
   gcge::BcgScalars bcg{};
+  // A + shift B on the union of the two patterns (built by Setup when a shift
+  // is enabled): ash_av / ash_bv hold A's / B's value per union entry
+  GcgeDevCsr ash{};
+  double *ash_av = nullptr, *ash_bv = nullptr;
+  double ash_sigma = 0.0;
+  bool ash_valid = false;
+  int if_shift_run = 0;   // the shift state of the running Solve
+  double shift_run = 0.0;
   GCGE_CUDA_MULTI_LINEAR_SOLVER mls = nullptr;  // user W-step solver
   void* mls_ctx = nullptr;
   double* bcg_mem = nullptr;
@@ -353,6 +370,13 @@ static int set_param(Para& p, const char* name, double v) {
   else if (k == "print_level") p.print_level = (int)v;
   else if (k == "precision") p.precision = (int)v;
   else if (k == "gemm") p.gemm = (int)v;
+  else if (k == "use_shift") p.use_shift = (int)v;
+  else if (k == "if_shift") p.if_shift = (int)v;
+  else if (k == "shift") p.shift = v;
+  else if (k == "eval_type") {
+    if (v != 0.0 && v != 1.0) return set_err(GCGE_CUDA_ERR_ARG, "eval_type: 0 (sa) or 1 (sm)");
+    p.eval_type = (int)v;
+  }
   else return set_err(GCGE_CUDA_ERR_ARG, "unknown parameter %s", name);
   return GCGE_CUDA_OK;
 }
@@ -375,7 +399,7 @@ extern "C" int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* s, int argc
   if (!s) return set_err(GCGE_CUDA_ERR_ARG, "SetFromCommandLine: null solver");
   static const char* ints[] = {"-gcge_nev", "-gcge_ev_max_it", "-gcge_block_size",
                                "-gcge_num_init_evec", "-gcge_cg_max_it", "-gcge_max_reorth_time",
-                               "-gcge_print_level"};
+                               "-gcge_print_level", "-gcge_use_shift"};
   static const char* dbls[] = {"-gcge_ev_tol", "-gcge_cg_rate", "-gcge_orth_zero_tol",
                                "-gcge_reorth_tol", "-gcge_scbgs_reorth_tol",
                                "-gcge_multi_tol_for_lock"};
@@ -399,6 +423,13 @@ extern "C" int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* s, int argc
         if (!strcmp(v, "ozaki") || !strcmp(v, "1")) s->para.gemm = 1;
         else if (!strcmp(v, "fp64") || !strcmp(v, "0")) s->para.gemm = 0;
         else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_gemm: fp64 or ozaki");
+        hit = true;
+      }
+      if (!strcmp(a, "-gcge_eval_type")) {  // src/gcge_para.c:184-187
+        const char* v = argv[i + 1];
+        if (!strcmp(v, "sa")) s->para.eval_type = 0;
+        else if (!strcmp(v, "sm")) s->para.eval_type = 1;
+        else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_eval_type: sa or sm");
         hit = true;
       }
       if (!strcmp(a, "-gcge_precision")) {
@@ -431,6 +462,15 @@ static void free_ws(Solver* s) {
   cudaFree(s->bcg_mem);
   cudaFree(s->bcg_int);
   if (s->h_pinned_int) cudaFreeHost(s->h_pinned_int);
+  cudaFree(s->ash.rp);
+  cudaFree(s->ash.ci);
+  cudaFree(s->ash.v);
+  cudaFree(s->ash.v32);
+  cudaFree(s->ash_av);
+  cudaFree(s->ash_bv);
+  s->ash = GcgeDevCsr{};
+  s->ash_av = s->ash_bv = nullptr;
+  s->ash_valid = false;
   if (s->st) cudaStreamDestroy(s->st);
   s->pool = nullptr;
   s->pool32 = nullptr;
@@ -438,6 +478,87 @@ static void free_ws(Solver* s) {
   s->d_eval = s->d_small = s->partial = s->jac_work = s->bcg_mem = nullptr;
   s->d_int = s->bcg_int = s->h_pinned_int = nullptr;
   s->st = nullptr;
+}
+
+// The operator of the shifted block CG (src/gcge_cg.c:348-360, 420-432 apply
+// A p + shift B p): one CSR matrix on the union of A's and B's patterns (B =
+// NULL is the identity), with A's and B's values kept per entry so that a new
+// shift costs one pass over the values.  Built once on the host from the
+// device copies.
+static int build_shift_op(Solver* s) {
+  const GcgeDevCsr& A = s->A->m;
+  const int n = A.n;
+  std::vector<int> arp(n + 1), aci(A.nnz), brp, bci;
+  std::vector<double> av(A.nnz), bv;
+  CU(cudaMemcpy(arp.data(), A.rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(aci.data(), A.ci, sizeof(int) * A.nnz, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(av.data(), A.v, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost));
+  if (s->B) {
+    const GcgeDevCsr& B = s->B->m;
+    brp.resize(n + 1);
+    bci.resize(B.nnz);
+    bv.resize(B.nnz);
+    CU(cudaMemcpy(brp.data(), B.rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(bci.data(), B.ci, sizeof(int) * B.nnz, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(bv.data(), B.v, sizeof(double) * B.nnz, cudaMemcpyDeviceToHost));
+  } else {
+    brp.resize(n + 1);
+    bci.resize(n);
+    bv.assign(n, 1.0);
+    for (int i = 0; i <= n; i++) brp[i] = i;
+    for (int i = 0; i < n; i++) bci[i] = i;
+  }
+  std::vector<int> urp(n + 1, 0), uci;
+  std::vector<double> ua, ub;
+  uci.reserve((size_t)A.nnz + n);
+  ua.reserve((size_t)A.nnz + n);
+  ub.reserve((size_t)A.nnz + n);
+  std::vector<std::pair<int, int>> row;  // (column, A entry e >= 0 or B entry -1-e)
+  for (int i = 0; i < n; i++) {
+    row.clear();
+    for (int e = arp[i]; e < arp[i + 1]; e++) row.push_back({aci[e], e});
+    for (int e = brp[i]; e < brp[i + 1]; e++) row.push_back({bci[e], -1 - e});
+    std::stable_sort(row.begin(), row.end(),
+                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+                       return x.first < y.first;
+                     });
+    for (size_t k = 0; k < row.size(); k++) {
+      if (k == 0 || row[k].first != row[k - 1].first) {
+        uci.push_back(row[k].first);
+        ua.push_back(0.0);
+        ub.push_back(0.0);
+      }
+      if (row[k].second >= 0) ua.back() += av[row[k].second];
+      else ub.back() += bv[-1 - row[k].second];
+    }
+    urp[i + 1] = (int)uci.size();
+  }
+  const size_t nz = uci.size();
+  GcgeDevCsr& M = s->ash;
+  M.n = n;
+  M.nnz = (int)nz;
+  CU(cudaMalloc(&M.rp, sizeof(int) * (n + 1)));
+  CU(cudaMalloc(&M.ci, sizeof(int) * nz));
+  CU(cudaMalloc(&M.v, sizeof(double) * nz));
+  CU(cudaMalloc(&s->ash_av, sizeof(double) * nz));
+  CU(cudaMalloc(&s->ash_bv, sizeof(double) * nz));
+  if (s->para.precision == 1) CU(cudaMalloc(&M.v32, sizeof(float) * nz));
+  CU(cudaMemcpy(M.rp, urp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(M.ci, uci.data(), sizeof(int) * nz, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->ash_av, ua.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->ash_bv, ub.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
+  s->ash_valid = false;
+  return GCGE_CUDA_OK;
+}
+
+static __global__ void k_shift_values(const double* __restrict__ av, const double* __restrict__ bv,
+                                      double sigma, double* __restrict__ v,
+                                      float* __restrict__ v32, int nnz) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += gridDim.x * blockDim.x) {
+    const double x = fma(sigma, bv[e], av[e]);
+    v[e] = x;
+    if (v32) v32[e] = (float)x;
+  }
 }
 
 // GCGE_SOLVER_Setup = PARA_Setup + OPS_Setup + WORKSPACE_Setup
@@ -541,6 +662,7 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   s->bcg.acol = s->bcg_mem + 6 * GCGE_MAXCOLS;
   s->bcg.mask = s->bcg_int + GCGE_MAXCOLS + 1;
   CU(cudaStreamSynchronize(s->st));
+  if (p.use_shift == 1 || p.if_shift == 1) CHK(build_shift_op(s));
   (void)add;
   s->setup_done = true;
   return GCGE_CUDA_OK;
@@ -774,16 +896,48 @@ static int compute_subspace_matrix(Solver* s) {
                            0.0, s->sub_mat + (size_t)dim_x * ldm + dim_x, ldm, s->st));
     KL(gcge::set_diag(s->sub_mat, ldm, s->d_eval, dim_x, s->st));
   }
-  return vtaw(s, dim_xp, s->num_soft_locked, ldm, s->sub_mat + (size_t)dim_xp * ldm);
+  CHK(vtaw(s, dim_xp, s->num_soft_locked, ldm, s->sub_mat + (size_t)dim_xp * ldm));
+  if (s->if_shift_run == 1) KL(gcge::add_diag(s->sub_mat, ldm, s->shift_run, ldm, s->st));  // :181-189
+  return GCGE_CUDA_OK;
+}
+
+// GCGE_SortByMagnitude (src/gcge_rayleighritz.c:842-874): quicksort of
+// a[left..right] by |a| with the first element as pivot, carrying idx.  Kept
+// as the reference's partition scheme so that ties order the same way.
+static void sort_by_magnitude(double* a, int* idx, int left, int right) {
+  if (left > right) return;
+  int i = left, j = right;
+  const int pidx = idx[left];
+  const double piv = a[left], pm = fabs(a[left]);
+  while (i != j) {
+    while (fabs(a[j]) >= pm && j > i) j--;
+    if (j > i) {
+      idx[i] = idx[j];
+      a[i++] = a[j];
+    }
+    while (fabs(a[i]) <= pm && j > i) i++;
+    if (j > i) {
+      idx[j] = idx[i];
+      a[j--] = a[i];
+    }
+  }
+  a[i] = piv;
+  idx[i] = pidx;
+  sort_by_magnitude(a, idx, left, i - 1);
+  sort_by_magnitude(a, idx, i + 1, right);
 }
 
 // GCGE_ComputeSubspaceEigenpairs (src/gcge_rayleighritz.c:507-805), serial
-// branch, eval_type "sa", no shift.
+// branch.  eval_type "sm" computes all pairs and moves the smallest |lambda|
+// first (:748-769); a shift is taken off the Ritz values and the diagonal
+// afterwards (:771-783).
 static int compute_subspace_eigenpairs(Solver* s) {
   const int ldm = s->dim_xpw;
   const int sl = s->unlock[0];
   s->num_soft_locked = sl;
-  const int iu = (s->max_dim_x < ldm) ? s->max_dim_x : ldm;
+  const bool sm = s->para.eval_type == 1;
+  const int iu_sa = (s->max_dim_x < ldm) ? s->max_dim_x : ldm;
+  const int iu = sm ? ldm : iu_sa;
   const int nw = s->dim_xpw - s->dim_xp;
   if (sl > 0 && nw > 0)
     CU(cudaMemset2DAsync(s->sub_mat + (size_t)s->dim_xp * ldm, sizeof(double) * ldm, 0,
@@ -799,6 +953,29 @@ static int compute_subspace_eigenpairs(Solver* s) {
                      s->st));
   CHK(sync(s));
   if (status < 0) return set_err(GCGE_CUDA_ERR_NUMERIC, "subspace Jacobi did not converge");
+  if (sm) {
+    std::vector<int> ord(nrows);
+    for (int i = 0; i < nrows; i++) ord[i] = i;
+    sort_by_magnitude(s->eval.data() + sl, ord.data(), 0, nrows - 1);
+    const int len = iu_sa - sl;
+    if (len > 0) {
+      IntList idx;
+      for (int i = 0; i < len; i++) idx.v[i] = ord[i];
+      double* blk = s->sub_evec + (size_t)sl * ldm;
+      KL(gcge::gather_cols(blk, ldm, sl, nrows, idx, len, s->sub_tmp, ldm, s->st));
+      CU(cudaMemcpy2DAsync(blk + sl, sizeof(double) * ldm, s->sub_tmp, sizeof(double) * ldm,
+                           sizeof(double) * nrows, len, cudaMemcpyDeviceToDevice, s->st));
+    }
+  }
+  if (s->if_shift_run == 1) {
+    for (int i = sl; i < iu; i++) s->eval[i] -= s->shift_run;
+    KL(gcge::add_diag(s->sub_mat, ldm, -s->shift_run, ldm, s->st));
+  }
+  if (sm || s->if_shift_run == 1) {
+    CU(cudaMemcpyAsync(s->d_eval + sl, s->eval.data() + sl, sizeof(double) * (iu - sl),
+                       cudaMemcpyHostToDevice, s->st));
+    CHK(sync(s));
+  }
   return GCGE_CUDA_OK;
 }
 
@@ -817,18 +994,33 @@ static int compute_w(Solver* s) {
   if (wl <= 0) return GCGE_CUDA_OK;
   ColList<double> X, Wc, R = cols(s->V_tmp, 0, wl);
   std::vector<double> rs(wl), wsc(wl);
+  // the reference adds para->shift to lambda here whether or not if_shift is
+  // set (src/gcge_xpw.c:158,166)
+  const double sh = s->shift_run;
   for (int i = 0; i < wl; i++) {
     const int xi = s->unlock[i];
     X.p[i] = s->V[xi];
     Wc.p[i] = s->V[ws + i];
     const double lam = s->eval[xi];
     if (fabs(lam) <= 1.0) {
-      rs[i] = lam;
+      rs[i] = lam + sh;
       wsc[i] = 1.0;
     } else {
       rs[i] = 1.0;
-      wsc[i] = 1.0 / lam;
+      wsc[i] = 1.0 / (lam + sh);
     }
+  }
+  // the block-CG operator: A, or A + shift B
+  const GcgeDevCsr* Aop = &s->A->m;
+  if (s->if_shift_run == 1) {
+    if (!s->ash.rp) return set_err(GCGE_CUDA_ERR_STATE, "shift active without a shifted operator");
+    if (!s->ash_valid || s->ash_sigma != sh) {
+      KL((k_shift_values<<<4 * 152, 256, 0, s->st>>>(s->ash_av, s->ash_bv, sh, s->ash.v,
+                                                      s->ash.v32, s->ash.nnz)));
+      s->ash_sigma = sh;
+      s->ash_valid = true;
+    }
+    Aop = &s->ash;
   }
   KL(gcge::apply_b_f64(Bptr(s), X, R, wl, s->n, s->st));
   dim3 g((s->n + 255) / 256, wl);
@@ -842,7 +1034,7 @@ static int compute_w(Solver* s) {
     return GCGE_CUDA_OK;
   }
   if (s->para.precision == 0) {
-    steps = gcge::bcg_run<double>(s->A->m.rp, s->A->m.ci, s->A->m.v, s->n, R, Wc,
+    steps = gcge::bcg_run<double>(Aop->rp, Aop->ci, Aop->v, s->n, R, Wc,
                                   cols(s->CG_p, 0, wl), cols(s->evec, 0, wl), wl,
                                   s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
                                   &launches);
@@ -853,7 +1045,7 @@ static int compute_w(Solver* s) {
     // matters near convergence, where w0 = x/lambda carries the eigenvector
     // and the useful correction is as small as the eigen-residual.
     ColList<double> AW = cols(s->evec, 0, wl);
-    KL(gcge::spmm_f64(s->A->m, Wc, AW, wl, s->st));
+    KL(gcge::spmm_f64(*Aop, Wc, AW, wl, s->st));
     KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
     if (wl <= 32) {
       // row-interleaved FP32 vectors: one contiguous row per SpMM gather
@@ -864,7 +1056,7 @@ static int compute_w(Solver* s) {
       float* Wr = Pr + blk;
       KL(gcge::cols_to_rows_f32(R, wl, Rr, s->n, s->st));
       CU(cudaMemsetAsync(Xr, 0, sizeof(float) * blk, s->st));
-      steps = gcge::bcg_run_rows_f32(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, Rr, Xr, Pr, Wr,
+      steps = gcge::bcg_run_rows_f32(Aop->rp, Aop->ci, Aop->v32, s->n, Rr, Xr, Pr, Wr,
                                      wl, s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial,
                                      s->st, &launches);
       KL(gcge::rows_add_to_cols_f64(Xr, wl, Wc, s->n, s->st));
@@ -873,7 +1065,7 @@ static int compute_w(Solver* s) {
       KL(gcge::convert_f64_to_f32(R, fr, wl, s->n, s->st));
       for (int i = 0; i < wl; i++)
         CU(cudaMemsetAsync(fx.p[i], 0, sizeof(float) * s->n, s->st));
-      steps = gcge::bcg_run<float>(s->A->m.rp, s->A->m.ci, s->A->m.v32, s->n, fr, fx,
+      steps = gcge::bcg_run<float>(Aop->rp, Aop->ci, Aop->v32, s->n, fr, fx,
                                    colsf(s->f_p, 0, wl), colsf(s->f_w, 0, wl), wl,
                                    s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
                                    &launches);
@@ -1004,6 +1196,10 @@ static int check_convergence(Solver* s) {
     }
   }
   if (ncc < nev && unlock[0] < ncc) ncc = unlock[0];
+  if (p.use_shift == 1) {  // src/gcge_eigsol.c:827-831
+    s->if_shift_run = 1;
+    s->shift_run = (eval[s->dim_x - 1] - 100.0 * eval[0]) / 99.0;
+  }
   if (nu > p.block_size) nu = p.block_size;
   s->num_unlock = nu;
   s->num_conv_continuous = ncc;
@@ -1060,6 +1256,8 @@ extern "C" int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* s) {
   s->num_soft_locked = 0;
   s->num_iter = 0;
   s->num_conv_continuous = 0;
+  s->if_shift_run = p.if_shift;
+  s->shift_run = p.shift;
   CU(cudaMemsetAsync(s->d_eval, 0, sizeof(double) * s->mx, s->st));
   CU(cudaMemsetAsync(s->sub_mat, 0, sizeof(double) * (size_t)s->mx * s->mx, s->st));
   CU(cudaMemsetAsync(s->sub_evec, 0, sizeof(double) * (size_t)s->mx * s->mx, s->st));

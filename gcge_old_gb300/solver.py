@@ -72,7 +72,8 @@ class GCGESolver:
     """
 
     INT_PARAMS = {"nev", "ev_max_it", "block_size", "num_init_evec", "cg_max_it",
-                  "max_reorth_time", "print_level", "gemm"}
+                  "max_reorth_time", "print_level", "gemm", "use_shift", "if_shift",
+                  "eval_type"}
 
     def __init__(self, A, B=None, nev: int = 1, **params):
         self._lib = L.load()
@@ -91,6 +92,9 @@ class GCGESolver:
             if k == "precision":
                 v = {"fp64": 0, "mixed": 1}.get(v, v)
                 L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"precision", int(v)), k)
+            elif k == "eval_type":
+                v = {"sa": 0, "sm": 1}.get(v, v)
+                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"eval_type", int(v)), k)
             elif k == "gemm":
                 v = {"fp64": 0, "ozaki": 1}.get(v, v)
                 L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"gemm", int(v)), k)

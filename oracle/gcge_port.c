@@ -33,6 +33,11 @@ typedef struct {
 typedef struct {
   int nev, block_size, ev_max_it, cg_max_it, max_reorth_time;
   double ev_tol, cg_rate, orth_zero_tol, reorth_tol, scbgs_reorth_tol, multi_tol_for_lock;
+  /* shift (src/gcge_para.h:90-92): use_shift recomputes if_shift/shift after
+   * every convergence check; if_shift/shift set by hand give a fixed shift.
+   * eval_sm: eval_type "sm" (smallest magnitude) instead of "sa". */
+  int use_shift, if_shift, eval_sm;
+  double shift;
 } port_para;
 
 typedef struct {
@@ -43,6 +48,7 @@ typedef struct {
   double *sub_mat, *sub_evec, *sub_dtmp, *eval, *res;
   int *unlock, *itmp;
   int num_iter, num_unlock, num_conv_continuous;
+  double* Bx; /* B x of the shifted block-CG operator */
   port_para p;
   const port_csr *A, *B;
   long long spmv_count;
@@ -418,8 +424,35 @@ static void compute_subspace_matrix(port_ws* w) {
   }
   int start_V = w->num_soft_locked_in_last_iter; /* opt_rr_eig_partly */
   vtaw(w, dim_xp, start_V, ldm, sm + dim_xp * ldm);
+  if (w->p.if_shift == 1) /* :181-189 */
+    for (int i = 0; i < ldm; i++) sm[i * ldm + i] += w->p.shift;
 }
-/* GCGE_ComputeSubspaceEigenpairs, :507-805 (serial, no shift, "sa"). */
+
+/* GCGE_SortByMagnitude (src/gcge_rayleighritz.c:842-874): in-place quicksort
+ * of a[left..right] by |a| with the first element as pivot, carrying idx. */
+static void sort_by_magnitude(double* a, int* idx, int left, int right) {
+  if (left > right) return;
+  int i = left, j = right;
+  const int pidx = idx[left];
+  const double piv = a[left], pm = fabs(a[left]);
+  while (i != j) {
+    while (fabs(a[j]) >= pm && j > i) j--;
+    if (j > i) {
+      idx[i] = idx[j];
+      a[i++] = a[j];
+    }
+    while (fabs(a[i]) <= pm && j > i) i++;
+    if (j > i) {
+      idx[j] = idx[i];
+      a[j--] = a[i];
+    }
+  }
+  a[i] = piv;
+  idx[i] = pidx;
+  sort_by_magnitude(a, idx, left, i - 1);
+  sort_by_magnitude(a, idx, i + 1, right);
+}
+/* GCGE_ComputeSubspaceEigenpairs, :507-805 (serial branch). */
 static void compute_subspace_eigenpairs(port_ws* w) {
   int ldm = w->dim_xpw;
   double* tmp = w->sub_dtmp;
@@ -427,12 +460,27 @@ static void compute_subspace_eigenpairs(port_ws* w) {
   int il = s + 1;
   w->num_soft_locked_in_last_iter = s;
   int iu = (w->max_dim_x < ldm) ? w->max_dim_x : ldm;
+  if (w->p.eval_sm) iu = ldm; /* :748-751: all pairs, then the smallest |lambda| */
   for (int i = 0; i < w->dim_xpw - w->dim_xp; i++)
     memset(w->sub_mat + (w->dim_xp + i) * ldm, 0, sizeof(double) * s);
   memcpy(tmp, w->sub_mat, sizeof(double) * ldm * ldm);
   int nrows = ldm - s;
   dense_eig(tmp + s * ldm + s, ldm, nrows, w->eval + s, w->sub_evec + s * ldm + s, ldm, il - s,
             iu - s);
+  if (w->p.eval_sm) { /* :753-769 */
+    int* ord = w->itmp;
+    for (int i = 0; i < nrows; i++) ord[i] = i;
+    sort_by_magnitude(w->eval + s, ord, 0, nrows - 1);
+    int len = ((w->max_dim_x < ldm) ? w->max_dim_x : ldm) - s;
+    double* start = w->sub_evec + s * ldm + s;
+    for (int i = 0; i < len; i++)
+      memcpy(tmp + (size_t)i * ldm, start + (size_t)ord[i] * ldm, sizeof(double) * nrows);
+    memcpy(start, tmp, sizeof(double) * ((size_t)(len - 1) * ldm + nrows));
+  }
+  if (w->p.if_shift == 1) { /* :771-783 */
+    for (int i = s; i < iu; i++) w->eval[i] -= w->p.shift;
+    for (int i = 0; i < ldm; i++) w->sub_mat[i * ldm + i] -= w->p.shift;
+  }
 }
 
 /* ---------------- X, P, W (src/gcge_xpw.c) ------------------------------ */
@@ -444,6 +492,18 @@ static void compute_x(port_ws* w, int size_x, int size_v) { /* :47-76 */
 /* GCGE_BCG, src/gcge_cg.c:302-501, including its index bookkeeping: after a
  * column locks out, rho/ptw are addressed by the compacted index "id" in
  * places and by the column index "idx" in others (:411 vs :451,465,474). */
+/* y += shift * (B x or x) when a shift is active (src/gcge_cg.c:348-360,
+ * 420-432): the block CG then solves (A + shift B) w = rhs. */
+static void shift_term(port_ws* w, const double* x, double* y) {
+  if (w->p.if_shift != 1) return;
+  if (w->B) {
+    spmv(w->B, x, w->Bx, w);
+    axpby(w->n, w->p.shift, w->Bx, 1.0, y);
+  } else {
+    axpby(w->n, w->p.shift, x, 1.0, y);
+  }
+}
+
 static void bcg(port_ws* w, double** RHS, double** X, int s0, int s1, int len, double** P,
                 double** Wv) {
   const int n = w->n;
@@ -456,6 +516,7 @@ static void bcg(port_ws* w, double** RHS, double** X, int s0, int s1, int len, d
   int nu = 0;
   for (int idx = 0; idx < len; idx++) {
     spmv(w->A, X[s1 + idx], Wv[idx], w);
+    shift_term(w, X[s1 + idx], Wv[idx]);
     axpby(n, -1.0, Wv[idx], 1.0, RHS[s0 + idx]);
     rho2[idx] = dot(n, RHS[s0 + idx], RHS[s0 + idx]);
   }
@@ -471,6 +532,7 @@ static void bcg(port_ws* w, double** RHS, double** X, int s0, int s1, int len, d
       if (niter == 1) axpby(n, 1.0, RHS[s0 + idx], 0.0, P[idx]);
       else axpby(n, 1.0, RHS[s0 + idx], rho2[idx] / rho1[idx], P[idx]);
       spmv(w->A, P[idx], Wv[idx], w);
+      shift_term(w, P[idx], Wv[idx]);
       ptw[id] = dot(n, P[idx], Wv[idx]);
     }
     for (int id = 0; id < nu; id++) {
@@ -502,11 +564,12 @@ static void compute_w(port_ws* w) { /* :118-260 */
     double* wc = w->V[ws + idx];
     apply_b(w, x, rhs);
     double lam = w->eval[xi];
+    /* the reference adds para->shift here whether or not if_shift is set */
     if (fabs(lam) <= 1.0) {
-      axpby(n, 0.0, rhs, lam, rhs);
+      axpby(n, 0.0, rhs, lam + w->p.shift, rhs);
       axpby(n, 1.0, x, 0.0, wc);
     } else {
-      axpby(n, 1.0 / lam, x, 0.0, wc);
+      axpby(n, 1.0 / (lam + w->p.shift), x, 0.0, wc);
     }
   }
   bcg(w, w->V_tmp, w->V, 0, ws, wl, w->CG_p, w->evec);
@@ -600,6 +663,10 @@ static void check_convergence(port_ws* w) {
     }
   }
   if (ncc < nev && unlock[0] < ncc) ncc = unlock[0];
+  if (w->p.use_shift == 1) { /* src/gcge_eigsol.c:827-831 */
+    w->p.if_shift = 1;
+    w->p.shift = (eval[w->dim_x - 1] - 100.0 * eval[0]) / 99.0;
+  }
   if (nu > w->p.block_size) nu = w->p.block_size;
   w->num_unlock = nu;
   w->num_conv_continuous = ncc;
@@ -637,6 +704,10 @@ void gcge_port_default_para(port_para* p, int nev) {
   p->reorth_tol = 0.75;
   p->scbgs_reorth_tol = 1e-16;
   p->multi_tol_for_lock = 1e-6;
+  p->use_shift = 0;
+  p->if_shift = 0;
+  p->eval_sm = 0;
+  p->shift = 0.0;
 }
 
 /* Solve A x = lambda B x for the nev smallest pairs from the initial block x0
@@ -682,6 +753,7 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
   w->sub_mat = (double*)calloc((size_t)mx * mx, sizeof(double));
   w->unlock = (int*)calloc(w->max_dim_x, sizeof(int));
   w->res = (double*)calloc(nev, sizeof(double));
+  w->Bx = (double*)calloc(n, sizeof(double));
   for (int i = 0; i < nev; i++) w->res[i] = 1.0;
   for (int i = 0; i < w->max_dim_x; i++) w->unlock[i] = i;
   w->dim_x = nev;
@@ -764,6 +836,7 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
   free(w->sub_mat);
   free(w->unlock);
   free(w->res);
+  free(w->Bx);
   return 0;
 }
 

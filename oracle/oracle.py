@@ -31,7 +31,9 @@ class PortPara(C.Structure):
                 ("cg_max_it", C.c_int), ("max_reorth_time", C.c_int),
                 ("ev_tol", C.c_double), ("cg_rate", C.c_double),
                 ("orth_zero_tol", C.c_double), ("reorth_tol", C.c_double),
-                ("scbgs_reorth_tol", C.c_double), ("multi_tol_for_lock", C.c_double)]
+                ("scbgs_reorth_tol", C.c_double), ("multi_tol_for_lock", C.c_double),
+                ("use_shift", C.c_int), ("if_shift", C.c_int), ("eval_sm", C.c_int),
+                ("shift", C.c_double)]
 
 
 def build_port(force: bool = False) -> str:

@@ -47,6 +47,16 @@ int ref_gcge_solve(int n, const int* a_rowptr, const int* a_col, const double* a
   }
   GCGE_SOLVER* s = GCGE_CSR_Solver_Init(&A, Bp, nev, argc, argv);
   if (!s) return 1;
+  /* "-ref_fixed_shift <sigma>" (a flag of this driver, skipped by the
+   * reference's own parser): sets the public fields para->if_shift = 1 and
+   * para->shift = sigma (src/gcge_para.h:90-92), which the reference reads in
+   * GCGE_ComputeW / GCGE_BCG / Rayleigh-Ritz; -gcge_use_shift recomputes them
+   * every iteration instead. */
+  for (int i = 0; i + 1 < argc; i++)
+    if (!strcmp(argv[i], "-ref_fixed_shift")) {
+      s->para->if_shift = 1;
+      s->para->shift = atof(argv[i + 1]);
+    }
   CSR_VEC** ev = (CSR_VEC**)s->evec;
   for (int j = 0; j < nev; j++) memcpy(ev[j]->Entries, x0 + (size_t)j * n, sizeof(double) * n);
   double t0 = wall_seconds();

@@ -28,7 +28,11 @@ def load_golden(name):
     flags = {}
     for f in d["flags"]:
         k, v = str(f).split("=")
-        flags[k.replace("-gcge_", "")] = float(v)
+        k = k.replace("-gcge_", "").replace("-ref_", "")  # -ref_fixed_shift: oracle driver flag
+        try:
+            flags[k] = float(v)
+        except ValueError:
+            flags[k] = v  # eval_type
     d["flags_dict"] = flags
     return A, B, int(d["nev"]), d["x0"], d
 

@@ -67,9 +67,38 @@ def main():
          {"-gcge_ev_tol": 1e-13, "-gcge_block_size": 20, "-gcge_ev_max_it": 100},
          keep_vecs=False)
 
+    shifted()
+
+
+def shifted():
+    """The shift options (use_shift, a fixed if_shift/shift) and eval_type "sm"
+    on indefinite problems A - c B; c is off the midpoint of two eigenvalues so
+    no two |lambda - c| tie.  "-ref_fixed_shift" is a flag of
+    oracle/ref_driver.c that sets para->if_shift = 1, para->shift = value."""
+    import scipy.linalg as sla
+    import scipy.sparse as sp
+    A, B = M.diffusion27(10, seed=2)
+    base = {"-gcge_ev_tol": 1e-11, "-gcge_ev_max_it": 150}
+    x0 = M.initial_block(A.n, 10, seed=4)
+    save("ref_diff27_m10_nev10_useshift", A, B, 10, x0, {**base, "-gcge_use_shift": 1})
+    ev = sla.eigh(A.to_scipy().toarray(), B.to_scipy().toarray(), eigvals_only=True)
+    c = 0.5 * (ev[2] + ev[3]) + 0.37
+    Ac = M.CSRMatrix.from_scipy(A.to_scipy() - c * B.to_scipy())
+    save("ref_diff27c_m10_nev10_fixedshift", Ac, B, 10, x0, {**base, "-ref_fixed_shift": 2 * c})
+    save("ref_diff27c_m10_nev10_sm", Ac, B, 10, x0, {**base, "-gcge_eval_type": "sm"})
+    L = M.laplace2d(32).to_scipy()
+    Lc = M.CSRMatrix.from_scipy(L - 0.1 * sp.identity(L.shape[0]))
+    base = {"-gcge_ev_tol": 1e-10, "-gcge_ev_max_it": 150}
+    x0 = M.initial_block(Lc.n, 10, seed=4)
+    save("ref_lap2dc_m32_nev10_useshift", Lc, None, 10, x0, {**base, "-gcge_use_shift": 1})
+    save("ref_lap2dc_m32_nev10_sm", Lc, None, 10, x0, {**base, "-gcge_eval_type": "sm"})
+
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["shifted"]:
+        shifted()
+    else:
+        main()
 
 
 def make_cfg2_summary(out_path=os.path.join(OUT, "cfg2_reference_summary.json")):

@@ -60,6 +60,16 @@ def test_solver_parameter_surface_without_gpu():
             b"mixed"]
     argv = (C.c_char_p * len(args))(*args)
     assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, len(args), argv) == 0
+    # shift and eval_type (GCGE_PARA use_shift / if_shift / shift / eval_type)
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"use_shift", 1) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamDouble(s, b"shift", 2.5) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"eval_type", 1) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"eval_type", 2) == 1
+    for flag in ([b"-gcge_eval_type", b"sm"], [b"-gcge_use_shift", b"0"]):
+        argv = (C.c_char_p * 2)(*flag)
+        assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, 2, argv) == 0
+    argv = (C.c_char_p * 2)(b"-gcge_eval_type", b"lm")
+    assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, 2, argv) == 1
     bad = [b"-gcge_precision", b"half"]
     argv = (C.c_char_p * 2)(*bad)
     assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, 2, argv) == 1

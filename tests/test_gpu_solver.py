@@ -19,7 +19,12 @@ EV_RTOL = 1e-10
 def gpu_params(flags, precision):
     p = {"precision": precision}
     for k, v in flags.items():
-        p[k] = int(v) if k in ("block_size", "ev_max_it", "cg_max_it") else float(v)
+        if k == "fixed_shift":
+            p["if_shift"], p["shift"] = 1, float(v)
+        elif k == "eval_type":
+            p[k] = v
+        else:
+            p[k] = int(v) if k in ("block_size", "ev_max_it", "cg_max_it", "use_shift") else float(v)
     return p
 
 

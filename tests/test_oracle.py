@@ -15,8 +15,12 @@ def para_for(nev, flags):
     for k, v in flags.items():
         if k in ("ev_tol", "cg_rate"):
             kw[k] = float(v)
-        elif k in ("block_size", "ev_max_it", "cg_max_it"):
+        elif k in ("block_size", "ev_max_it", "cg_max_it", "use_shift"):
             kw[k] = int(v)
+        elif k == "eval_type":
+            kw["eval_sm"] = int(v == "sm")
+        elif k == "fixed_shift":
+            kw["if_shift"], kw["shift"] = 1, float(v)
     return O.default_para(nev, **kw)
 
 
