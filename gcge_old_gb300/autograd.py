@@ -11,6 +11,18 @@ by grad[ij] + grad[ji].  Simple (non-repeated) eigenvalues are assumed.
 
     lam = eigvals_csr(a_val, A_pattern, nev, x0, b_val=b_val, B_pattern=B_pattern)
     (w * lam).sum().backward()
+
+eigpairs_csr also returns the eigenvectors (rows of X, B-normalised, each
+signed so that its entry of largest magnitude is positive) for losses that
+use them.  Their adjoint (GCGE_CUDA_EigvecAdjointSolve + GCGE_CUDA_EigGradCSR2)
+solves, for each eigenvector the loss touches, the projected system
+(A - lambda_k B) mu_k = g_k - B x_k (x_k^T g_k) with mu_k B-orthogonal to x_k,
+and gives dL/dA_ij = -mu_k[i] x_k[j], dL/dB_ij = lambda_k mu_k[i] x_k[j]
+- 1/2 (g_k^T x_k) x_k[i] x_k[j].  It needs lambda_k < lambda_{nev+1}, which
+holds for every returned pair.
+
+    lam, X = eigpairs_csr(a_val, A_pattern, nev, x0, b_val=b_val, B_pattern=B_pattern)
+    ((X[0] * mask) ** 2).sum().backward()
 """
 from __future__ import annotations
 
@@ -82,3 +94,99 @@ def eigvals_csr(a_val: torch.Tensor, A_pattern: CSRMatrix, nev: int, x0: np.ndar
     if (b_val is None) != (B_pattern is None):
         raise ValueError("b_val and B_pattern go together")
     return _EigvalsCSR.apply(a_val, b_val, A_pattern, B_pattern, nev, x0, params)
+
+
+def _signed(vec: np.ndarray) -> np.ndarray:
+    """Each row flipped so that its entry of largest magnitude is positive."""
+    idx = np.abs(vec).argmax(axis=1)
+    sgn = np.sign(vec[np.arange(len(vec)), idx])
+    sgn[sgn == 0] = 1.0
+    return vec * sgn[:, None]
+
+
+def _cols(t: torch.Tensor):
+    return (C.c_void_p * t.shape[0])(*[C.c_void_p(t[j].data_ptr()) for j in range(t.shape[0])])
+
+
+class _EigpairsCSR(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, a_val, b_val, A_pattern, B_pattern, nev, x0, params, adj):
+        A = _with_values(A_pattern, a_val)
+        B = _with_values(B_pattern, b_val) if b_val is not None else None
+        s = GCGESolver(A, B, nev, **params)
+        try:
+            ev, vec = s.solve(x0)
+        finally:
+            s.close()
+        vec = _signed(vec)
+        ctx.A, ctx.B = A, B
+        ctx.ev, ctx.vec, ctx.adj = ev, vec, adj
+        ctx.has_b = b_val is not None
+        dev = a_val.device
+        return torch.from_numpy(ev.copy()).to(dev), torch.from_numpy(vec.copy()).to(dev)
+
+    @staticmethod
+    def backward(ctx, g_lam, g_vec):
+        lib = L.load()
+        ev, nev = ctx.ev, len(ctx.ev)
+        gl = (g_lam.detach().to("cpu", torch.float64).numpy() if g_lam is not None
+              else np.zeros(nev))
+        X = torch.from_numpy(np.ascontiguousarray(ctx.vec)).to("cuda")
+        xp = _cols(X)
+        mu = None
+        gx = np.zeros(nev)
+        want = np.zeros(nev, dtype=bool)
+        dA = DeviceMatrix(ctx.A)
+        dB = DeviceMatrix(ctx.B) if ctx.B is not None else None
+        try:
+            if g_vec is not None:
+                G = g_vec.detach().to("cuda", torch.float64).contiguous()
+                want = (G.abs().amax(dim=1) > 0).cpu().numpy()
+            if want.any():
+                mu = torch.zeros_like(X)
+                gp = (C.c_void_p * nev)(*[C.c_void_p(G[j].data_ptr()) if want[j] else None
+                                          for j in range(nev)])
+                it = C.c_int(0)
+                L.check(lib.GCGE_CUDA_EigvecAdjointSolve(
+                    dA.handle, dB.handle if dB else None, xp, _dptr(ev), nev, gp, _cols(mu),
+                    _dptr(gx), int(ctx.adj["max_it"]), float(ctx.adj["tol"]), C.byref(it)),
+                    "EigvecAdjointSolve")
+                ctx.adjoint_steps = it.value
+            mp = _cols(mu) if mu is not None else None
+            ga = gb = None
+            if ctx.needs_input_grad[0]:
+                ga = torch.zeros(ctx.A.nnz, dtype=torch.float64, device="cuda")
+                a = np.ascontiguousarray(gl)
+                b = np.where(want, -1.0, 0.0)
+                L.check(lib.GCGE_CUDA_EigGradCSR2(dA.handle, xp, mp, _dptr(a), _dptr(b), nev,
+                                                  C.c_void_p(ga.data_ptr())), "EigGradCSR2")
+            if ctx.has_b and ctx.needs_input_grad[1]:
+                gb = torch.zeros(ctx.B.nnz, dtype=torch.float64, device="cuda")
+                a = np.ascontiguousarray(-ev * gl - 0.5 * gx)
+                b = np.where(want, ev, 0.0)
+                L.check(lib.GCGE_CUDA_EigGradCSR2(dB.handle, xp, mp, _dptr(a), _dptr(b), nev,
+                                                  C.c_void_p(gb.data_ptr())), "EigGradCSR2")
+        finally:
+            dA.close()
+            if dB:
+                dB.close()
+        dev = (g_lam if g_lam is not None else g_vec).device
+        return (ga.to(dev) if ga is not None else None, gb.to(dev) if gb is not None else None,
+                None, None, None, None, None, None)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(L.c_double_p)
+
+
+def eigpairs_csr(a_val: torch.Tensor, A_pattern: CSRMatrix, nev: int, x0: np.ndarray,
+                 b_val: torch.Tensor | None = None, B_pattern: CSRMatrix | None = None,
+                 adjoint_tol: float = 1e-10, adjoint_max_it: int = 100000, **params):
+    """(lambda, X): the nev smallest eigenpairs of A x = lambda B x, X of shape
+    (nev, n) with B-normalised rows, differentiable in a_val / b_val for losses
+    of both.  adjoint_tol / adjoint_max_it: stopping rule of the projected CG of
+    the eigenvector adjoint (relative residual per column)."""
+    if (b_val is None) != (B_pattern is None):
+        raise ValueError("b_val and B_pattern go together")
+    adj = {"tol": adjoint_tol, "max_it": adjoint_max_it}
+    return _EigpairsCSR.apply(a_val, b_val, A_pattern, B_pattern, nev, x0, params, adj)

@@ -88,6 +88,11 @@ SIGNATURES = {
     "GCGE_CUDA_SOLVER_SetMultiLinearSolver": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "GCGE_CUDA_JacobiPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                       C.c_void_p]),
+    "GCGE_CUDA_EigvecAdjointSolve": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_double_p, C.c_int,
+                                              c_pp, c_pp, c_double_p, C.c_int, C.c_double,
+                                              c_int_p]),
+    "GCGE_CUDA_EigGradCSR2": (C.c_int, [C.c_void_p, c_pp, c_pp, c_double_p, c_double_p, C.c_int,
+                                        C.c_void_p]),
     "GCGE_CUDA_EigGradCSR": (C.c_int, [C.c_void_p, c_pp, C.c_void_p, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MatDotRowsF32Async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                                C.c_void_p]),

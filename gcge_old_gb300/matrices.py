@@ -150,6 +150,73 @@ def diffusion27(m: int = 160, seed: int = 0):
     return a, b
 
 
+def aniso2d(m: int = 512, seed: int = 0, ratio: float = 10.0):
+    """2D anisotropic diffusion, 5-point, on the m x m interior nodes of an
+    (m+1) x (m+1) cell grid with per-cell kappa ~ U(0.5, 2): the conductance of
+    an edge is the mean kappa of the two cells beside it, times ``ratio`` for
+    y-edges; edges to the Dirichlet boundary only add to the diagonal.
+    B = diag(h^2 (1 + U(-0.1, 0.1))), h = 1/(m+1).
+
+    Returns (A, B, S, kappa) with A.val = S @ kappa: S (nnz x (m+1)^2, CSR) is
+    the linear map from cell coefficients to the stored values of A, for
+    gradients with respect to kappa."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    nc = m + 1
+    kappa = rng.uniform(0.5, 2.0, nc * nc)
+    n = m * m
+    node = lambda a, b: a * m + b          # interior node (row a, column b), 0-based
+    cell = lambda a, b: a * nc + b         # cell with lower-left corner at grid point (a, b)
+    # edge list: (i, j or -1 for boundary, [cells], weight)
+    er, ec, ev = [], [], []                # S triplets, keyed by (row, col) of A
+    entries = {}
+
+    def add(i, j, cells, w):
+        key = (i, j)
+        for c in cells:
+            entries.setdefault(key, {})
+            entries[key][c] = entries[key].get(c, 0.0) + w / len(cells)
+
+    for a in range(m + 1):      # grid rows 0..m of nodes 0..m+1 (grid point g = interior + 1)
+        for b in range(m + 1):
+            # x-edge between grid points (a+1, b) and (a+1, b+1), cells (a, b) and (a+1, b)
+            if a < m:
+                i = node(a, b - 1) if b >= 1 else -1
+                j = node(a, b) if b < m else -1
+                cells = [cell(a, b), cell(a + 1, b)]
+                for p_, q_ in ((i, j), (j, i)):
+                    if p_ >= 0:
+                        add(p_, p_, cells, 1.0)
+                        if q_ >= 0:
+                            add(p_, q_, cells, -1.0)
+            # y-edge between grid points (a, b+1) and (a+1, b+1), cells (a, b) and (a, b+1)
+            if b < m:
+                i = node(a - 1, b) if a >= 1 else -1
+                j = node(a, b) if a < m else -1
+                cells = [cell(a, b), cell(a, b + 1)]
+                for p_, q_ in ((i, j), (j, i)):
+                    if p_ >= 0:
+                        add(p_, p_, cells, ratio)
+                        if q_ >= 0:
+                            add(p_, q_, cells, -ratio)
+    keys = sorted(entries)
+    rows = np.array([k[0] for k in keys], dtype=np.int64)
+    cols = np.array([k[1] for k in keys], dtype=np.int64)
+    for e, k in enumerate(keys):
+        for c, w in entries[k].items():
+            er.append(e)
+            ec.append(c)
+            ev.append(w)
+    S = sp.csr_matrix((ev, (er, ec)), shape=(len(keys), nc * nc))
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rowptr, rows + 1, 1)
+    rowptr = np.cumsum(rowptr)
+    A = CSRMatrix(n, rowptr.astype(np.int32), cols.astype(np.int32), S @ kappa)
+    h = 1.0 / (m + 1)
+    B = diag_matrix(h * h * (1.0 + rng.uniform(-0.1, 0.1, n)))
+    return A, B, S, kappa
+
+
 def initial_block(n: int, nev: int, seed: int = 0) -> np.ndarray:
     """Seeded N(0,1) initial block, column-major n x nev (shape (nev, n) in C
     order, so column j is ``x0[j]``)."""

@@ -70,6 +70,31 @@ int GCGE_CUDA_MatDestroy(GCGE_CUDA_MAT** mat);
 /* Rows (= columns) and stored entries of a device matrix. */
 int GCGE_CUDA_MatGetSize(const GCGE_CUDA_MAT* mat, int* n, int* nnz);
 
+/* ---------------------------------------------------------------- eigenvector adjoint
+ * For eigenvector losses: with g_k = dL/dx_k (device columns, G[k] = NULL for
+ * columns the loss does not touch) solves, for each requested k,
+ *   (A - lambda_k B) mu_k = g_k - B x_k (x_k^T g_k),  mu_k B-orthogonal to x_k,
+ * writing mu_k to MU[k] (device column of length n), and gx[k] = g_k^T x_k
+ * (host array, may be NULL).  X holds the nev B-orthonormal eigenvectors and
+ * eval (host) their eigenvalues, all simple; B = NULL is the identity.  mu_k
+ * is the sum of its components on the other computed pairs,
+ * x_j (x_j^T g_k) / (lambda_j - lambda_k), and a part in the B-orthogonal
+ * complement of X found by a Jacobi-preconditioned projected CG (positive
+ * definite there when lambda_k < lambda_{nev+1}), run until every column's
+ * residual is below tol times its initial value (at most max_it steps;
+ * GCGE_CUDA_ERR_NUMERIC if a column does not get there).  The gradient then is
+ *   dL/dA_ij = -mu_k[i] x_k[j],
+ *   dL/dB_ij = lambda_k mu_k[i] x_k[j] - 1/2 (g_k^T x_k) x_k[i] x_k[j],
+ * which GCGE_CUDA_EigGradCSR2 assembles over a CSR pattern. */
+int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT* B, double* const* X,
+                                 const double* eval, int nev, double* const* G, double* const* MU,
+                                 double* gx, int max_it, double tol, int* iters);
+/* grad[e] = sum_k (a[k] x_k[i] + b[k] mu_k[i]) x_k[j] over the stored entries
+ * e = (i, j) of M (device output of M's nnz doubles); MU may be NULL (then b
+ * is ignored) and MU[k] may be NULL for columns without an eigenvector term. */
+int GCGE_CUDA_EigGradCSR2(const GCGE_CUDA_MAT* M, double* const* X, double* const* MU,
+                          const double* a, const double* b, int k, double* grad);
+
 /* ---------------------------------------------------------------- matrix files
  * Text: the reference's CSR file (CSR_ReadMatFile, app/csr/gcge_app_csr.c:185-236):
  * nrow, ncol, nnz, rowptr[nrow+1], col[nnz], val[nnz], whitespace separated,
