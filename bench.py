@@ -29,6 +29,15 @@ once in each precision: 27-point Q1 variable-coefficient diffusion (per-cell
 kappa = exp(N(0,1))) with its consistent mass on a 160^3 grid (n = 4,096,000,
 nnz = 109,215,352), nev = 100, and reports both times and the per-pair
 difference of the mixed result from the FP64 one (not the default line).
+
+--config 4 runs the differentiation configuration: 2D anisotropic diffusion
+(5-point, per-cell kappa ~ U(0.5, 2), y-edges weighted 10) on a 512 x 512
+grid with diagonal mass, nev = 32, loss = sum_k w_k lambda_k
++ ||x_1 * mask||^2; it times the forward solve and the backward pass (the
+eigenvalue and eigenvector adjoints), checks the gradients with respect to
+kappa and to A's and B's values against central differences of the solver,
+and the same on a 64 x 64 copy against adjoints from a dense generalized
+eigendecomposition.
 """
 from __future__ import annotations
 
@@ -369,6 +378,107 @@ def run_config3(args):
     return 0
 
 
+def _config4_grad(torch, M, m, nev, seed, ev_tol):
+    """Forward + backward of the config-4 loss; returns the problem, tensors and times."""
+    from gcge_old_gb300.autograd import eigpairs_csr
+    A, B, Smap, kappa = M.aniso2d(m, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    w = rng.uniform(0.0, 1.0, nev)
+    mask = (rng.uniform(size=A.n) < 0.5).astype(np.float64)
+    x0 = M.initial_block(A.n, nev, seed=seed)
+    S = Smap.tocoo()
+    St = torch.sparse_coo_tensor(np.vstack([S.row, S.col]), S.data, S.shape)
+    kap = torch.tensor(kappa, requires_grad=True)
+    b = torch.tensor(B.val, requires_grad=True)
+    params = dict(ev_tol=ev_tol, ev_max_it=5000, precision="fp64")
+    torch.cuda.synchronize()
+    t0 = time.time()
+    a = torch.sparse.mm(St, kap[:, None])[:, 0]
+    a.retain_grad()
+    lam, X = eigpairs_csr(a, A, nev, x0, b_val=b, B_pattern=B, **params)
+    t1 = time.time()
+    wt, mt = torch.from_numpy(w), torch.from_numpy(mask)
+    loss = (wt * lam).sum() + ((X[0] * mt) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    t2 = time.time()
+
+    def f(kv, bv):
+        with torch.no_grad():
+            l, Y = eigpairs_csr(torch.from_numpy(Smap @ kv), A, nev, x0,
+                                b_val=torch.from_numpy(bv), B_pattern=B, **params)
+        return float((w * l.numpy()).sum() + ((Y[0].numpy() * mask) ** 2).sum())
+
+    return dict(A=A, B=B, S=Smap, kappa=kappa, w=w, mask=mask, lam=lam.detach().numpy(),
+                X=X.detach().numpy(), ga=a.grad.numpy(), gb=b.grad.numpy(),
+                gk=kap.grad.numpy(), f=f, t_fwd=t1 - t0, t_bwd=t2 - t1)
+
+
+def run_config4(args):
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    import scipy.linalg as sla
+    from gcge_old_gb300 import matrices as M
+    nev = 32
+    r = _config4_grad(torch, M, 512, nev, 0, 1e-12)
+    kappa, Bv, gk, gb, ga = r["kappa"], r["B"].val, r["gk"], r["gb"], r["ga"]
+    rng = np.random.default_rng(3)
+    checks = []
+
+    def fd(kv_p, kv_m, bv_p, bv_m, h):
+        return (r["f"](kv_p, bv_p) - r["f"](kv_m, bv_m)) / (2 * h)
+
+    top = np.argsort(-np.abs(gk))[:200]
+    for c in rng.choice(top, 3, replace=False):
+        h = 1e-4 * kappa[c]
+        kp, km = kappa.copy(), kappa.copy()
+        kp[c] += h
+        km[c] -= h
+        v = fd(kp, km, Bv, Bv, h)
+        checks.append({"param": "kappa[%d]" % c, "fd": v, "adjoint": float(gk[c]),
+                       "rel": abs(v - gk[c]) / abs(gk[c])})
+    topb = np.argsort(-np.abs(gb))[:200]
+    for e in rng.choice(topb, 2, replace=False):
+        h = 1e-4 * Bv[e]
+        bp, bm = Bv.copy(), Bv.copy()
+        bp[e] += h
+        bm[e] -= h
+        v = fd(kappa, kappa, bp, bm, h)
+        checks.append({"param": "B[%d]" % e, "fd": v, "adjoint": float(gb[e]),
+                       "rel": abs(v - gb[e]) / abs(gb[e])})
+    # 64 x 64 copy against dense generalized-eigendecomposition adjoints
+    s = _config4_grad(torch, M, 64, nev, 0, 1e-12)
+    A, B = s["A"], s["B"]
+    ev, V = sla.eigh(A.to_scipy().toarray(), B.to_scipy().toarray())
+    V = V.T.copy()
+    idx = np.abs(V[:nev]).argmax(axis=1)
+    V[:nev] *= np.sign(V[np.arange(nev), idx])[:, None]
+    g0 = 2 * s["mask"] ** 2 * V[0]
+    d = ev - ev[0]
+    d[0] = np.inf
+    mu0 = ((V @ g0) / d) @ V
+    Asp, Bsp = A.to_scipy().tocoo(), B.to_scipy().tocoo()
+    w = s["w"]
+    gA = sum(w[k] * V[k][Asp.row] * V[k][Asp.col] for k in range(nev)) - mu0[Asp.row] * V[0][Asp.col]
+    gB = (sum(-w[k] * ev[k] * V[k][Bsp.row] * V[k][Bsp.col] for k in range(nev))
+          + ev[0] * mu0[Bsp.row] * V[0][Bsp.col] - 0.5 * (g0 @ V[0]) * V[0][Bsp.row] * V[0][Bsp.col])
+    dense = {"n": A.n, "eigenvalue_rel_max": float(np.max(np.abs(s["lam"] - ev[:nev]) / ev[:nev])),
+             "gradA_rel_max": float(np.abs(s["ga"] - gA).max() / np.abs(gA).max()),
+             "gradB_rel_max": float(np.abs(s["gb"] - gB).max() / np.abs(gB).max()),
+             "gradKappa_rel_max": float(np.abs(s["gk"] - s["S"].T @ gA).max()
+                                        / np.abs(s["S"].T @ gA).max())}
+    out = {"metric": "eigenvalue + eigenvector loss gradient (adjoint) vs finite differences",
+           "config": {"workload": "aniso2d_5pt_512x512_kappa_U(0.5,2)_ratio10_diag_mass_nev32",
+                      "n": int(r["A"].n), "nnz_A": int(r["A"].nnz), "nev": nev,
+                      "loss": "sum w_k lambda_k + ||x_1 * mask||^2"},
+           "forward_s": r["t_fwd"], "backward_s": r["t_bwd"],
+           "fd_checks": checks, "fd_rel_max": max(c["rel"] for c in checks),
+           "dense_64x64": dense, "data": "synthetic (seeded generator)"}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -377,13 +487,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="48^3 grid (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
-                    help="3: the 160^3 27-point mixed-precision configuration (one solve each)")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4],
+                    help="3: the 160^3 27-point mixed-precision configuration (one solve each); "
+                         "4: the 512^2 differentiation configuration (gradient checks)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
     if args.config == 3:
         return run_config3(args)
+    if args.config == 4:
+        return run_config4(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

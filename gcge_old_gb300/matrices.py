@@ -165,53 +165,42 @@ def aniso2d(m: int = 512, seed: int = 0, ratio: float = 10.0):
     nc = m + 1
     kappa = rng.uniform(0.5, 2.0, nc * nc)
     n = m * m
-    node = lambda a, b: a * m + b          # interior node (row a, column b), 0-based
-    cell = lambda a, b: a * nc + b         # cell with lower-left corner at grid point (a, b)
-    # edge list: (i, j or -1 for boundary, [cells], weight)
-    er, ec, ev = [], [], []                # S triplets, keyed by (row, col) of A
-    entries = {}
-
-    def add(i, j, cells, w):
-        key = (i, j)
-        for c in cells:
-            entries.setdefault(key, {})
-            entries[key][c] = entries[key].get(c, 0.0) + w / len(cells)
-
-    for a in range(m + 1):      # grid rows 0..m of nodes 0..m+1 (grid point g = interior + 1)
-        for b in range(m + 1):
-            # x-edge between grid points (a+1, b) and (a+1, b+1), cells (a, b) and (a+1, b)
-            if a < m:
-                i = node(a, b - 1) if b >= 1 else -1
-                j = node(a, b) if b < m else -1
-                cells = [cell(a, b), cell(a + 1, b)]
-                for p_, q_ in ((i, j), (j, i)):
-                    if p_ >= 0:
-                        add(p_, p_, cells, 1.0)
-                        if q_ >= 0:
-                            add(p_, q_, cells, -1.0)
-            # y-edge between grid points (a, b+1) and (a+1, b+1), cells (a, b) and (a, b+1)
-            if b < m:
-                i = node(a - 1, b) if a >= 1 else -1
-                j = node(a, b) if a < m else -1
-                cells = [cell(a, b), cell(a, b + 1)]
-                for p_, q_ in ((i, j), (j, i)):
-                    if p_ >= 0:
-                        add(p_, p_, cells, ratio)
-                        if q_ >= 0:
-                            add(p_, q_, cells, -ratio)
-    keys = sorted(entries)
-    rows = np.array([k[0] for k in keys], dtype=np.int64)
-    cols = np.array([k[1] for k in keys], dtype=np.int64)
-    for e, k in enumerate(keys):
-        for c, w in entries[k].items():
-            er.append(e)
-            ec.append(c)
-            ev.append(w)
-    S = sp.csr_matrix((ev, (er, ec)), shape=(len(keys), nc * nc))
+    # edges between grid points; interior node (r, c) is grid point (r+1, c+1),
+    # index r*m + c; cell (a, b) has its lower-left corner at grid point (a, b)
+    A_, B_ = np.meshgrid(np.arange(m), np.arange(m + 1), indexing="ij")
+    # x-edges: grid row a+1, grid columns b -> b+1; cells (a, b) and (a+1, b)
+    xi = np.where(B_ >= 1, A_ * m + B_ - 1, -1)
+    xj = np.where(B_ < m, A_ * m + B_, -1)
+    xc1, xc2 = A_ * nc + B_, (A_ + 1) * nc + B_
+    # y-edges: grid rows a -> a+1, grid column b+1; cells (a, b) and (a, b+1)
+    Ay, By = np.meshgrid(np.arange(m + 1), np.arange(m), indexing="ij")
+    yi = np.where(Ay >= 1, (Ay - 1) * m + By, -1)
+    yj = np.where(Ay < m, Ay * m + By, -1)
+    yc1, yc2 = Ay * nc + By, Ay * nc + By + 1
+    ei = np.concatenate([xi.ravel(), yi.ravel()])
+    ej = np.concatenate([xj.ravel(), yj.ravel()])
+    c1 = np.concatenate([xc1.ravel(), yc1.ravel()])
+    c2 = np.concatenate([xc2.ravel(), yc2.ravel()])
+    w = np.concatenate([np.ones(xi.size), np.full(yi.size, ratio)]) / 2.0
+    rows, cols, cells, vals = [], [], [], []
+    for p_, q_ in ((ei, ej), (ej, ei)):
+        d = p_ >= 0                      # diagonal of each interior endpoint
+        o = d & (q_ >= 0)                # coupling of two interior endpoints
+        for c in (c1, c2):
+            rows += [p_[d], p_[o]]
+            cols += [p_[d], q_[o]]
+            cells += [c[d], c[o]]
+            vals += [w[d], -w[o]]
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    key, ent = np.unique(rows * n + cols, return_inverse=True)
+    S = sp.csr_matrix((np.concatenate(vals), (ent, np.concatenate(cells))),
+                      shape=(len(key), nc * nc))
+    S.sum_duplicates()
+    r = key // n
     rowptr = np.zeros(n + 1, dtype=np.int64)
-    np.add.at(rowptr, rows + 1, 1)
+    np.add.at(rowptr, r + 1, 1)
     rowptr = np.cumsum(rowptr)
-    A = CSRMatrix(n, rowptr.astype(np.int32), cols.astype(np.int32), S @ kappa)
+    A = CSRMatrix(n, rowptr.astype(np.int32), (key % n).astype(np.int32), S @ kappa)
     h = 1.0 / (m + 1)
     B = diag_matrix(h * h * (1.0 + rng.uniform(-0.1, 0.1, n)))
     return A, B, S, kappa
