@@ -445,15 +445,23 @@ def run_config4(args):
     R.sort_indices()
     assert R.nnz == len(Av) and (R.indptr == Asp.indptr).all() and (R.indices == Asp.indices).all()
     dA = R.data * np.abs(Av)
+    # edge-wise direction: random relative change of each off-diagonal pair with
+    # the diagonal moved so that row sums stay as they are (a conductance change)
+    coo = Asp.tocoo()
+    off = coo.row != coo.col
+    E = Asp.copy()
+    E.data = np.where(off, R.data * np.abs(Av), 0.0)
+    dE = E.data - np.where(~off, np.asarray(E.sum(axis=1)).ravel()[coo.row], 0.0)
     dk = rng.standard_normal(len(kappa)) * kappa
     dB = rng.standard_normal(len(Bv)) * Bv
     dirs = [("kappa", Smap @ dk, np.zeros_like(Bv), float(r["gk"] @ dk),
              float(r["ga_ev"] @ (Smap @ dk))),
             ("A_values", dA, np.zeros_like(Bv), float(r["ga"] @ dA), float(r["ga_ev"] @ dA)),
+            ("A_edges", dE, np.zeros_like(Bv), float(r["ga"] @ dE), float(r["ga_ev"] @ dE)),
             ("B_values", np.zeros_like(Av), dB, float(r["gb"] @ dB), float(r["gb_ev"] @ dB))]
     checks = {"eigenvalue_loss": [], "full_loss": []}
     for name, da, db, adj_full, adj_ev in dirs:
-        for eps in (1e-4, 1e-3):
+        for eps in ((1e-6, 1e-5, 1e-4) if name.startswith("A_") else (1e-4, 1e-3)):
             fp, fm = r["f"](Av + eps * da, Bv + eps * db), r["f"](Av - eps * da, Bv - eps * db)
             for i, key, adj in ((0, "eigenvalue_loss", adj_ev), (1, "full_loss", adj_full)):
                 v = (fp[i] - fm[i]) / (2 * eps)
@@ -488,10 +496,10 @@ def run_config4(args):
            "fd_checks": checks,
            "fd_rel_best_eigenvalue_loss": {d: min(c["rel"] for c in checks["eigenvalue_loss"]
                                                   if c["direction"] == d)
-                                           for d in ("kappa", "A_values", "B_values")},
+                                           for d in ("kappa", "A_values", "A_edges", "B_values")},
            "fd_rel_best_full_loss": {d: min(c["rel"] for c in checks["full_loss"]
                                             if c["direction"] == d)
-                                     for d in ("kappa", "A_values", "B_values")},
+                                     for d in ("kappa", "A_values", "A_edges", "B_values")},
            "fd_noise_floor": noise,
            "dense_64x64": dense, "data": "synthetic (seeded generator)"}
     print(json.dumps(out))
