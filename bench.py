@@ -415,7 +415,9 @@ def _config4_grad(torch, M, m, nev, seed, ev_tol):
         le = float((w * l.numpy()).sum())
         return le, le + float(((Y[0].numpy() * mask) ** 2).sum())
 
-    return dict(A=A, B=B, S=Smap, kappa=kappa, w=w, mask=mask, lam=lam.detach().numpy(),
+    from gcge_old_gb300.autograd import last_adjoint
+    adj = dict(last_adjoint)
+    return dict(A=A, B=B, S=Smap, kappa=kappa, w=w, mask=mask, lam=lam.detach().numpy(), adj=adj,
                 X=X.detach().numpy(), ga=ga, gb=b.grad.numpy(), gk=kap.grad.numpy(),
                 ga_ev=ga_ev.numpy(), gb_ev=gb_ev.numpy(), f=f, t_fwd=t1 - t0, t_bwd=t2 - t1)
 
@@ -493,6 +495,8 @@ def run_config4(args):
                       "n": int(r["A"].n), "nnz_A": int(r["A"].nnz), "nev": nev,
                       "loss": "sum w_k lambda_k + ||x_1 * mask||^2"},
            "forward_s": r["t_fwd"], "backward_s": r["t_bwd"],
+           "eigenvector_adjoint": {"columns": r["adj"]["columns"], "cg_steps": r["adj"]["steps"],
+                                   "tol": 1e-10},
            "fd_checks": checks,
            "fd_rel_best_eigenvalue_loss": {d: min(c["rel"] for c in checks["eigenvalue_loss"]
                                                   if c["direction"] == d)

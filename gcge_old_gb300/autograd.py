@@ -96,6 +96,10 @@ def eigvals_csr(a_val: torch.Tensor, A_pattern: CSRMatrix, nev: int, x0: np.ndar
     return _EigvalsCSR.apply(a_val, b_val, A_pattern, B_pattern, nev, x0, params)
 
 
+# step count and column count of the last eigenvector-adjoint solve
+last_adjoint = {"steps": 0, "columns": 0}
+
+
 def _signed(vec: np.ndarray) -> np.ndarray:
     """Each row flipped so that its entry of largest magnitude is positive."""
     idx = np.abs(vec).argmax(axis=1)
@@ -151,7 +155,8 @@ class _EigpairsCSR(torch.autograd.Function):
                     dA.handle, dB.handle if dB else None, xp, _dptr(ev), nev, gp, _cols(mu),
                     _dptr(gx), int(ctx.adj["max_it"]), float(ctx.adj["tol"]), C.byref(it)),
                     "EigvecAdjointSolve")
-                ctx.adjoint_steps = it.value
+                last_adjoint["steps"] = it.value
+                last_adjoint["columns"] = int(want.sum())
             mp = _cols(mu) if mu is not None else None
             ga = gb = None
             if ctx.needs_input_grad[0]:
