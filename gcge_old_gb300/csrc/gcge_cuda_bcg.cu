@@ -317,7 +317,9 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
                                                   const int* __restrict__ ci,
                                                   const float* __restrict__ val,
                                                   const float* __restrict__ X, float* R, int len,
-                                                  double* __restrict__ partial) {
+                                                  double* __restrict__ partial,
+                                                  const int* __restrict__ hidx,
+                                                  const float* __restrict__ hb) {
   __shared__ double sh[(kT / 32) * 32];
   float acc2[KW];
 #pragma unroll
@@ -326,13 +328,18 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
     float ax[KW];
 #pragma unroll
     for (int c = 0; c < KW; c++) ax[c] = 0.f;
-    for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
-      const int col = __ldg(ci + j);
-      const float a = __ldg(val + j);
-      float xv[KW];
-      load_row<KW>(X, col, xv);
+    const int h = hidx ? __ldg(hidx + r) : -1;
+    if (h >= 0) {
+      load_row<KW>(hb, h, ax);
+    } else {
+      for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+        const int col = __ldg(ci + j);
+        const float a = __ldg(val + j);
+        float xv[KW];
+        load_row<KW>(X, col, xv);
 #pragma unroll
-      for (int c = 0; c < KW; c++) ax[c] = fmaf(a, xv[c], ax[c]);
+        for (int c = 0; c < KW; c++) ax[c] = fmaf(a, xv[c], ax[c]);
+      }
     }
     float rv[KW];
     load_row<KW>(R, r, rv);
@@ -375,7 +382,9 @@ __global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ r
                                                 const int* __restrict__ ci,
                                                 const float* __restrict__ val,
                                                 const float* __restrict__ P, float* W, int len,
-                                                BcgScalars s, double* __restrict__ partial) {
+                                                BcgScalars s, double* __restrict__ partial,
+                                                const int* __restrict__ hidx,
+                                                const float* __restrict__ hb) {
   __shared__ double sh[(kT / 32) * 32];
   if (*s.nu == 0) return;
   bool on[KW];
@@ -388,13 +397,18 @@ __global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ r
     float ap[KW];
 #pragma unroll
     for (int c = 0; c < KW; c++) ap[c] = 0.f;
-    for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
-      const int col = __ldg(ci + j);
-      const float a = __ldg(val + j);
-      float pv[KW];
-      load_row<KW>(P, col, pv);
+    const int h = hidx ? __ldg(hidx + r) : -1;
+    if (h >= 0) {
+      load_row<KW>(hb, h, ap);
+    } else {
+      for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+        const int col = __ldg(ci + j);
+        const float a = __ldg(val + j);
+        float pv[KW];
+        load_row<KW>(P, col, pv);
 #pragma unroll
-      for (int c = 0; c < KW; c++) ap[c] = fmaf(a, pv[c], ap[c]);
+        for (int c = 0; c < KW; c++) ap[c] = fmaf(a, pv[c], ap[c]);
+      }
     }
     store_row<KW>(W, r, ap);
     float pr[KW];
@@ -529,12 +543,20 @@ template <int KW>
 __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__ rp,
                                                   const int* __restrict__ ci,
                                                   const float* __restrict__ val,
-                                                  const float* __restrict__ X, float* Y) {
+                                                  const float* __restrict__ X, float* Y,
+                                                  const int* __restrict__ hidx,
+                                                  const float* __restrict__ hb) {
   const int r = blockIdx.x * kT + threadIdx.x;
   if (r >= n) return;
   float acc[KW];
 #pragma unroll
   for (int c = 0; c < KW; c++) acc[c] = 0.f;
+  const int h = hidx ? __ldg(hidx + r) : -1;
+  if (h >= 0) {
+    load_row<KW>(hb, h, acc);
+    store_row<KW>(Y, r, acc);
+    return;
+  }
   for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
     const int col = __ldg(ci + j);
     const float a = __ldg(val + j);
@@ -570,12 +592,16 @@ __global__ void k_rows_add(const float* __restrict__ Xr, int len, ColList<double
 template <int KW>
 int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, float* X, float* P,
              float* W, int len, int max_it, double rate, const BcgScalars& s, double* partial,
-             cudaStream_t st, int* launches) {
+             cudaStream_t st, int* launches, const GcgeDevCsr* M) {
+  const bool hv = M && M->nheavy > 0;
+  const int* hidx = hv ? M->hidx : nullptr;
   // four CTAs of 8 warps per SM for the row-streaming kernels (two from 20
   // columns up, where the update kernel holds over 100 registers a thread)
   const int nb = min((n + kT - 1) / kT, (KW <= 16 ? 4 : 2) * 152);
   int nl = 0;
-  k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial);
+  if (hv) heavy_rows_f32(*M, val, X, KW, nullptr, st);
+  k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial, hidx,
+                                     hv ? M->hb32 : nullptr);
   k_rows_init_ctrl<<<1, 1024, 0, st>>>(partial, nb, len, s);
   nl += 2;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
@@ -585,7 +611,9 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
     const int batch = (max_it - niter) < kBatch ? (max_it - niter) : kBatch;
     for (int j = 0; j < batch; j++) {
       k_rows_p<KW><<<nb, kT, 0, st>>>(n, R, P, s, niter + j == 1 ? 1 : 0);
-      k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial);
+      if (hv) heavy_rows_f32(*M, val, P, KW, s.nu, st);
+      k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial, hidx,
+                                       hv ? M->hb32 : nullptr);
       k_rows_alpha<<<1, 1024, 0, st>>>(partial, nb, len, s);
       k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
       k_rows_step<<<1, 1024, 0, st>>>(partial, nb, len, s, rate, j);
@@ -606,33 +634,37 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
 
 int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, float* R, float* X,
                      float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
-                     double* partial, cudaStream_t st, int* launches) {
+                     double* partial, cudaStream_t st, int* launches, const GcgeDevCsr* M) {
   if (len <= 0) return 0;
   switch (bcg_rows_width(len)) {
-    case 4: return rows_run<4>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 8: return rows_run<8>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 12: return rows_run<12>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 20: return rows_run<20>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 24: return rows_run<24>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 28: return rows_run<28>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
-    case 32: return rows_run<32>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches);
+    case 4: return rows_run<4>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 8: return rows_run<8>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 12: return rows_run<12>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 20: return rows_run<20>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 24: return rows_run<24>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 28: return rows_run<28>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 32: return rows_run<32>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
   }
   return -1;
 }
 
 void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
-                   float* Y, int k, cudaStream_t st) {
+                   float* Y, int k, cudaStream_t st, const GcgeDevCsr* M) {
   const int g = (n + kT - 1) / kT;
+  const bool hv = M && M->nheavy > 0;
+  if (hv) heavy_rows_f32(*M, val, X, bcg_rows_width(k), nullptr, st);
+  const int* hidx = hv ? M->hidx : nullptr;
+  const float* hb = hv ? M->hb32 : nullptr;
   switch (bcg_rows_width(k)) {
-    case 4: k_rows_spmm<4><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 20: k_rows_spmm<20><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 24: k_rows_spmm<24><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 28: k_rows_spmm<28><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
-    case 32: k_rows_spmm<32><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y); break;
+    case 4: k_rows_spmm<4><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 20: k_rows_spmm<20><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 24: k_rows_spmm<24><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 28: k_rows_spmm<28><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 32: k_rows_spmm<32><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
   }
 }
 

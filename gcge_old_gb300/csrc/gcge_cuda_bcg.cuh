@@ -35,13 +35,16 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
 // gathers one contiguous KW-float row per nonzero and every vector kernel
 // streams whole rows.  Same steps, scalars and reductions (same order) as
 // bcg_run<float>; s.acol and s.mask must be set.  Returns niter or -1.
+// M (optional): the matrix whose heavy-row chunks (GcgeDevCsr::nheavy) rp / ci
+// / val describe; its heavy rows are then multiplied chunk-wise.
 int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, float* R, float* X,
                      float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
-                     double* partial, cudaStream_t st, int* launches);
+                     double* partial, cudaStream_t st, int* launches,
+                     const GcgeDevCsr* M = nullptr);
 inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
 // Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 32).
 void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
-                   float* Y, int k, cudaStream_t st);
+                   float* Y, int k, cudaStream_t st, const GcgeDevCsr* M = nullptr);
 // Rr (n x KW rows) <- FP64 columns R[0:len] (zero-padded); Y[c] += Xr[:, c].
 void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st);
 void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,

@@ -26,11 +26,22 @@ template <typename T, int KC>
 __global__ void __launch_bounds__(kThreads) k_spmm(int n, const int* __restrict__ rp,
                                                    const int* __restrict__ ci,
                                                    const T* __restrict__ val, ColList<T> X,
-                                                   ColList<T> Y, int k) {
+                                                   ColList<T> Y, int k,
+                                                   const int* __restrict__ hidx,
+                                                   const T* __restrict__ hb) {
   const int row = blockIdx.x * kThreads + threadIdx.x;
   if (row >= n) return;
   const int c0 = blockIdx.y * KC;
   const int kc = min(KC, k - c0);
+  if (hidx) {  // a heavy row: its products were formed chunk by chunk
+    const int h = __ldg(hidx + row);
+    if (h >= 0) {
+#pragma unroll
+      for (int c = 0; c < KC; c++)
+        if (c < kc) Y.p[c0 + c][row] = hb[(size_t)h * k + c0 + c];
+      return;
+    }
+  }
   T acc[KC];
 #pragma unroll
   for (int c = 0; c < KC; c++) acc[c] = T(0);
@@ -317,7 +328,11 @@ __global__ void __launch_bounds__(kThreads) k_residual(int n, const int* __restr
                                                        const double* __restrict__ bv,
                                                        ColList<double> X,
                                                        const double* __restrict__ lam,
-                                                       double* __restrict__ partial) {
+                                                       double* __restrict__ partial,
+                                                       const int* __restrict__ ahidx,
+                                                       const double* __restrict__ ahb,
+                                                       const int* __restrict__ bhidx,
+                                                       const double* __restrict__ bhb, int k) {
   __shared__ double sh[32];
   const int c = blockIdx.y;
   const double* x = X.p[c];
@@ -325,9 +340,16 @@ __global__ void __launch_bounds__(kThreads) k_residual(int n, const int* __restr
   double rs = 0.0, xs = 0.0;
   for (int r = blockIdx.x * kThreads + threadIdx.x; r < n; r += gridDim.x * kThreads) {
     double ax = 0.0;
-    for (int j = __ldg(arp + r); j < __ldg(arp + r + 1); j++) ax = fma(__ldg(av + j), x[__ldg(aci + j)], ax);
+    const int ha = ahidx ? __ldg(ahidx + r) : -1;
+    if (ha >= 0)
+      ax = ahb[(size_t)ha * k + c];
+    else
+      for (int j = __ldg(arp + r); j < __ldg(arp + r + 1); j++) ax = fma(__ldg(av + j), x[__ldg(aci + j)], ax);
     double bx;
-    if (brp) {
+    const int hb_ = bhidx ? __ldg(bhidx + r) : -1;
+    if (hb_ >= 0) {
+      bx = bhb[(size_t)hb_ * k + c];
+    } else if (brp) {
       bx = 0.0;
       for (int j = __ldg(brp + r); j < __ldg(brp + r + 1); j++) bx = fma(__ldg(bv + j), x[__ldg(bci + j)], bx);
     } else {
@@ -363,7 +385,9 @@ void spmm_f64(const GcgeDevCsr& A, const ColList<double>& X, const ColList<doubl
   if (k <= 0 || A.n <= 0) return;
   constexpr int KC = 8;
   dim3 g((A.n + kThreads - 1) / kThreads, (k + KC - 1) / KC);
-  k_spmm<double, KC><<<g, kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v, X, Y, k);
+  heavy_cols_f64(A, X, k, st);
+  k_spmm<double, KC><<<g, kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v, X, Y, k,
+                                             A.nheavy ? A.hidx : nullptr, A.hb64);
 }
 
 void spmm_f32(const GcgeDevCsr& A, const ColList<float>& X, const ColList<float>& Y, int k,
@@ -371,7 +395,7 @@ void spmm_f32(const GcgeDevCsr& A, const ColList<float>& X, const ColList<float>
   if (k <= 0 || A.n <= 0) return;
   constexpr int KC = 8;
   dim3 g((A.n + kThreads - 1) / kThreads, (k + KC - 1) / KC);
-  k_spmm<float, KC><<<g, kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v32, X, Y, k);
+  k_spmm<float, KC><<<g, kThreads, 0, st>>>(A.n, A.rp, A.ci, A.v32, X, Y, k, nullptr, nullptr);
 }
 
 void apply_b_f64(const GcgeDevCsr* B, const ColList<double>& X, const ColList<double>& Y, int k,
@@ -468,9 +492,13 @@ void residual_f64(const GcgeDevCsr& A, const GcgeDevCsr* B, const ColList<double
   if (k <= 0) return;
   const int n = A.n;
   const int nb = row_blocks(n);
+  heavy_cols_f64(A, X, k, st);
+  const bool bh = B && B->nheavy;
+  if (bh) heavy_cols_f64(*B, X, k, st);
   k_residual<<<dim3(nb, k), kThreads, 0, st>>>(n, A.rp, A.ci, A.v, B ? B->rp : nullptr,
                                                 B ? B->ci : nullptr, B ? B->v : nullptr, X, lam,
-                                                partial);
+                                                partial, A.nheavy ? A.hidx : nullptr, A.hb64,
+                                                bh ? B->hidx : nullptr, bh ? B->hb64 : nullptr, k);
   // partial holds 2k rows of nb entries: reduce into a scratch pair array
   double* pr = partial + (size_t)2 * k * nb;
   k_reduce_rows<<<2 * k, 256, 0, st>>>(partial, nb, 2 * k, pr);

@@ -283,7 +283,7 @@ extern "C" int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, fl
       k_val_to_f32<<<(A->m.nnz + 255) / 256, 256, 0, (cudaStream_t)stream>>>(A->m.v, A->m.v32,
                                                                              A->m.nnz);
   }
-  gcge::spmm_rows_f32(A->m.rp, A->m.ci, A->m.v32, A->m.n, x, y, k, (cudaStream_t)stream);
+  gcge::spmm_rows_f32(A->m.rp, A->m.ci, A->m.v32, A->m.n, x, y, k, (cudaStream_t)stream, &A->m);
   return cudaGetLastError() == cudaSuccess ? GCGE_CUDA_OK : GCGE_CUDA_ERR_CUDA;
 }
 

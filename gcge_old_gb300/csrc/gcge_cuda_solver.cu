@@ -110,6 +110,11 @@ static int mat_finish(GCGE_CUDA_MAT_* M, const int* h_rp, const int* h_ci) {
     diag = false;
   }
   if (diag) M->m.diag = M->m.v;
+  if (h_rp) {
+    const int e = gcge::heavy_setup(M->m, h_rp);
+    if (e) return set_err(GCGE_CUDA_ERR_ALLOC, "heavy-row chunks: %s",
+                          cudaGetErrorString((cudaError_t)e));
+  }
   return GCGE_CUDA_OK;
 }
 
@@ -157,7 +162,12 @@ extern "C" int GCGE_CUDA_MatCreate(GCGE_CUDA_MAT** mat, int n, const int* rowptr
     CU(cudaMemcpy(M->m.ci, col, sizeof(int) * nnz, kind));
     CU(cudaMemcpy(M->m.v, val, sizeof(double) * nnz, kind));
   }
-  mat_finish(M, rp_h, ci_h);
+  const int rc = mat_finish(M, rp_h, ci_h);
+  if (rc) {
+    GCGE_CUDA_MAT* tmp = M;
+    GCGE_CUDA_MatDestroy(&tmp);
+    return rc;
+  }
   *mat = M;
   return GCGE_CUDA_OK;
 }
@@ -178,6 +188,7 @@ extern "C" int GCGE_CUDA_MatGetSize(const GCGE_CUDA_MAT* mat, int* n, int* nnz) 
 extern "C" int GCGE_CUDA_MatDestroy(GCGE_CUDA_MAT** mat) {
   if (!mat || !*mat) return GCGE_CUDA_OK;
   GcgeDevCsr& m = (*mat)->m;
+  gcge::heavy_free(m);
   cudaFree(m.rp);
   cudaFree(m.ci);
   cudaFree(m.v);
@@ -462,6 +473,7 @@ static void free_ws(Solver* s) {
   cudaFree(s->bcg_mem);
   cudaFree(s->bcg_int);
   if (s->h_pinned_int) cudaFreeHost(s->h_pinned_int);
+  gcge::heavy_free(s->ash);
   cudaFree(s->ash.rp);
   cudaFree(s->ash.ci);
   cudaFree(s->ash.v);
@@ -547,6 +559,10 @@ static int build_shift_op(Solver* s) {
   CU(cudaMemcpy(M.ci, uci.data(), sizeof(int) * nz, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(s->ash_av, ua.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(s->ash_bv, ub.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
+  {
+    const int e = gcge::heavy_setup(M, urp.data());
+    if (e) return set_err(GCGE_CUDA_ERR_ALLOC, "heavy-row chunks of the shifted operator");
+  }
   s->ash_valid = false;
   return GCGE_CUDA_OK;
 }
@@ -1058,7 +1074,7 @@ static int compute_w(Solver* s) {
       CU(cudaMemsetAsync(Xr, 0, sizeof(float) * blk, s->st));
       steps = gcge::bcg_run_rows_f32(Aop->rp, Aop->ci, Aop->v32, s->n, Rr, Xr, Pr, Wr,
                                      wl, s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial,
-                                     s->st, &launches);
+                                     s->st, &launches, Aop);
       KL(gcge::rows_add_to_cols_f64(Xr, wl, Wc, s->n, s->st));
     } else {
       ColList<float> fr = colsf(s->f_rhs, 0, wl), fx = colsf(s->f_x, 0, wl);

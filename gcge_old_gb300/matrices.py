@@ -206,6 +206,60 @@ def aniso2d(m: int = 512, seed: int = 0, ratio: float = 10.0):
     return A, B, S, kappa
 
 
+def chung_lu(n: int = 8_000_000, mean_deg: float = 16.0, gamma: float = 2.5, seed: int = 0,
+             shift: float = 1e-3):
+    """Shifted graph Laplacian of a seeded Chung-Lu power-law graph.
+
+    Expected degrees w_i = c (n / (i + 1))^(1 / (gamma - 1)); mean_deg - 2 of
+    the mean degree comes from n (mean_deg - 2) / 2 edges whose endpoints are
+    drawn with probability proportional to w (self-loops dropped, repeated
+    pairs merged), the other 2 from a random recursive tree (node i joins a
+    uniform earlier node), which keeps the graph connected so that B = D is
+    positive definite.  Node labels are then shuffled.  Edge weights
+    U(0.5, 1.5).  A = L + shift I (L = D - W), B = D.
+
+    Returns (A, B, edges) with edges = (i, j, w, pos) for the undirected edges
+    i < j: pos = (A index of (i, j), of (j, i), of (i, i), of (j, j), B index of
+    i, of j), for gradients with respect to the edge weights."""
+    rng = np.random.default_rng(seed)
+    t = 1.0 / (gamma - 1.0)
+    w = (n / np.arange(1, n + 1, dtype=np.float64)) ** t
+    w *= (mean_deg - 2.0) * n / w.sum()
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    m = int(round(n * (mean_deg - 2.0) / 2.0))
+    a = np.searchsorted(cdf, rng.random(m), side="right")
+    b = np.searchsorted(cdf, rng.random(m), side="right")
+    np.minimum(a, n - 1, out=a)
+    np.minimum(b, n - 1, out=b)
+    tree_child = np.arange(1, n, dtype=np.int64)
+    tree_parent = np.floor(rng.random(n - 1) * tree_child).astype(np.int64)
+    i = np.concatenate([np.minimum(a, b), np.minimum(tree_child, tree_parent)])
+    j = np.concatenate([np.maximum(a, b), np.maximum(tree_child, tree_parent)])
+    keep = i != j
+    key = np.sort(i[keep] * n + j[keep])
+    key = key[np.concatenate([[True], key[1:] != key[:-1]])]
+    perm = rng.permutation(n)
+    i, j = perm[key // n], perm[key % n]
+    i, j = np.minimum(i, j), np.maximum(i, j)
+    wt = rng.uniform(0.5, 1.5, len(i))
+    deg = np.bincount(i, weights=wt, minlength=n) + np.bincount(j, weights=wt, minlength=n)
+    m = len(i)
+    rows = np.concatenate([i, j, np.arange(n)])
+    cols = np.concatenate([j, i, np.arange(n)])
+    vals = np.concatenate([-wt, -wt, deg + shift])
+    order = np.argsort(rows * n + cols, kind="stable")
+    inv = np.empty_like(order)
+    inv[order] = np.arange(len(order))
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    rowptr[1:] = np.cumsum(np.bincount(rows, minlength=n))
+    Ac = CSRMatrix(n, rowptr.astype(np.int32), cols[order].astype(np.int32), vals[order])
+    B = diag_matrix(deg)
+    p_ij, p_ji, p_d = inv[:m], inv[m:2 * m], inv[2 * m:]
+    p_ii, p_jj = p_d[i], p_d[j]
+    return Ac, B, (i, j, wt, (p_ij, p_ji, p_ii, p_jj, i, j))
+
+
 def initial_block(n: int, nev: int, seed: int = 0) -> np.ndarray:
     """Seeded N(0,1) initial block, column-major n x nev (shape (nev, n) in C
     order, so column j is ``x0[j]``)."""

@@ -1,0 +1,108 @@
+"""Uneven rows: products and solves on a shifted power-law graph Laplacian
+(seeded Chung-Lu graph, rows from 1 to thousands of entries), where rows of
+more than 64 entries go through the chunked warp pass (gcge_cuda_heavy.cu)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gcge_old_gb300 import matrices as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def graph():
+    A, B, edges = M.chung_lu(50_000, seed=1)
+    d = np.diff(A.rowptr)
+    assert d.max() > 1000 and (d > 64).sum() > 100  # heavy rows present
+    return A, B, edges
+
+
+def test_spmm_f64_heavy_rows(cuda_lib, graph):
+    import torch
+    from gcge_old_gb300.solver import DeviceMatrix
+    A = graph[0]
+    rng = np.random.default_rng(0)
+    k = 13
+    X = torch.from_numpy(rng.standard_normal((k, A.n))).cuda()
+    Y = torch.zeros_like(X)
+    dA = DeviceMatrix(A)
+    xp = (C.c_void_p * k)(*[C.c_void_p(X[j].data_ptr()) for j in range(k)])
+    yp = (C.c_void_p * k)(*[C.c_void_p(Y[j].data_ptr()) for j in range(k)])
+    assert cuda_lib.GCGE_CUDA_MatDotMultiVec(dA.handle, xp, yp, k) == 0
+    ref = (A.to_scipy() @ X.cpu().numpy().T).T
+    err = np.abs(Y.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err < 1e-13, err
+    dA.close()
+
+
+@pytest.mark.parametrize("k", [4, 13, 28])
+def test_spmm_rows_f32_heavy_rows(cuda_lib, graph, k):
+    import torch
+    from gcge_old_gb300.solver import DeviceMatrix
+    A = graph[0]
+    kw = (k + 3) // 4 * 4
+    rng = np.random.default_rng(k)
+    Xc = rng.standard_normal((A.n, k)).astype(np.float32)
+    Xr = np.zeros((A.n, kw), np.float32)
+    Xr[:, :k] = Xc
+    X = torch.from_numpy(Xr).cuda()
+    Y = torch.zeros_like(X)
+    dA = DeviceMatrix(A)
+    assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(X.data_ptr()),
+                                                 C.c_void_p(Y.data_ptr()), k, None) == 0
+    torch.cuda.synchronize()
+    ref = A.to_scipy() @ Xc.astype(np.float64)
+    scale = np.abs(A.to_scipy()) @ np.abs(Xc.astype(np.float64))
+    err = (np.abs(Y.cpu().numpy()[:, :k] - ref) / np.maximum(scale, 1e-30)).max()
+    assert err < 1e-5, err
+    dA.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_power_law_graph(cuda_lib, precision):
+    from gcge_old_gb300 import solver as S
+    A, B, _ = M.chung_lu(20_000, seed=2)
+    nev = 16
+    x0 = M.initial_block(A.n, nev, seed=3)
+    ev, vec, st = S.solve(A, B, nev, x0, ev_tol=1e-10, ev_max_it=500, precision=precision)
+    ref = O.port_solve(A, B, nev, x0, O.default_para(nev, ev_tol=1e-10, ev_max_it=500),
+                       threads=4)
+    assert np.max(np.abs(ev - ref["eval"]) / np.abs(ref["eval"])) < 1e-9
+    assert O.true_residuals(A, B, ev, vec).max() < 1e-9
+
+
+def test_edge_weight_gradient(cuda_lib):
+    """dlambda_k / dw_e = (x_i - x_j)^2 - lambda_k (x_i^2 + x_j^2) on an edge (i, j)
+    (A = L + shift I, B = D), assembled from the CSR-value adjoints of A and B."""
+    import torch
+    from gcge_old_gb300.autograd import eigvals_csr
+    A, B, (i, j, w, pos) = M.chung_lu(3_000, seed=4)
+    nev = 8
+    x0 = M.initial_block(A.n, nev, seed=5)
+    a = torch.tensor(A.val, requires_grad=True)
+    b = torch.tensor(B.val, requires_grad=True)
+    lam = eigvals_csr(a, A, nev, x0, b_val=b, B_pattern=B, ev_tol=1e-12, ev_max_it=2000,
+                      precision="fp64")
+    lam[nev - 1].backward()
+    p_ij, p_ji, p_ii, p_jj, bi, bj = pos
+    ga, gb = a.grad.numpy(), b.grad.numpy()
+    gw = -ga[p_ij] - ga[p_ji] + ga[p_ii] + ga[p_jj] + gb[bi] + gb[bj]
+    rng = np.random.default_rng(6)
+    for e in rng.choice(len(w), 3, replace=False):
+        h = 1e-4 * w[e]
+
+        def lam_at(dw):
+            av, bv = A.val.copy(), B.val.copy()
+            av[[p_ij[e], p_ji[e]]] -= dw
+            av[[p_ii[e], p_jj[e]]] += dw
+            bv[[bi[e], bj[e]]] += dw
+            with torch.no_grad():
+                l = eigvals_csr(torch.from_numpy(av), A, nev, x0, b_val=torch.from_numpy(bv),
+                                B_pattern=B, ev_tol=1e-12, ev_max_it=2000, precision="fp64")
+            return float(l[nev - 1])
+
+        fd = (lam_at(h) - lam_at(-h)) / (2 * h)
+        assert abs(fd - gw[e]) <= 1e-6 * max(abs(gw[e]), 1e-3 * np.abs(gw).max()), (e, fd, gw[e])
