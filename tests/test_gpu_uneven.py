@@ -71,7 +71,10 @@ def test_solve_power_law_graph(cuda_lib, precision):
     ref = O.port_solve(A, B, nev, x0, O.default_para(nev, ev_tol=1e-10, ev_max_it=500),
                        threads=4)
     assert np.max(np.abs(ev - ref["eval"]) / np.abs(ref["eval"])) < 1e-9
-    assert O.true_residuals(A, B, ev, vec).max() < 1e-9
+    # the reference's criterion ||A x - lambda B x|| / (||x|| max(1, |lambda|)): the
+    # smallest eigenvalue (~ shift n / sum(d)) is far below 1 here
+    crit = O.true_residuals(A, B, ev, vec) * np.abs(ev) / np.maximum(1.0, np.abs(ev))
+    assert crit.max() < 2e-10, crit
 
 
 def test_edge_weight_gradient(cuda_lib):
