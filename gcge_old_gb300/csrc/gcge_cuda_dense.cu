@@ -318,10 +318,13 @@ __global__ void __launch_bounds__(256) k_sub_mgs(double* __restrict__ V, int ldV
 __global__ void __launch_bounds__(256) k_chol_drop(int k, const double* __restrict__ G, int ldg,
                                                    double tol2, double* __restrict__ T,
                                                    int* __restrict__ kept,
-                                                   int* __restrict__ nk_out) {
+                                                   int* __restrict__ nk_out,
+                                                   double* __restrict__ gwork) {
   extern __shared__ double sm[];
-  double* M = sm;              // k x k working copy
-  double* R = sm + k * k;      // k x k upper factor (rows of kept pivots)
+  // k x k working copy and k x k upper factor (rows of kept pivots): in shared
+  // memory, or in gwork when 2 k^2 doubles do not fit
+  double* M = gwork ? gwork : sm;
+  double* R = M + k * k;
   __shared__ int keep[GCGE_MAXCOLS];
   __shared__ int pos[GCGE_MAXCOLS];
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -562,10 +565,14 @@ void sub_mgs(double* V, int ldV, int nrows, int start, int end, double tol, int*
 }
 
 void chol_drop(int k, const double* G, int ldg, double tol, double* T, int* kept, int* nk,
-               cudaStream_t st) {
+               double* work, cudaStream_t st) {
   const size_t sm = sizeof(double) * 2 * (size_t)k * k;
+  if (sm > 200 * 1024) {
+    k_chol_drop<<<1, 256, 0, st>>>(k, G, ldg, tol * tol, T, kept, nk, work);
+    return;
+  }
   if (sm > 48 * 1024) cudaFuncSetAttribute(k_chol_drop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_chol_drop<<<1, 256, sm, st>>>(k, G, ldg, tol * tol, T, kept, nk);
+  k_chol_drop<<<1, 256, sm, st>>>(k, G, ldg, tol * tol, T, kept, nk, nullptr);
 }
 
 void gather_cols(const double* src, int lds, int r0, int rows, const IntList& idx, int ncols,

@@ -21,8 +21,9 @@ void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec,
                 int iu, double* work, int* status, cudaStream_t st);
 void sub_mgs(double* V, int ldV, int nrows, int start, int end, double tol, int* end_out,
              cudaStream_t st);
+// work: 2 k^2 doubles of device scratch, used when they do not fit in shared memory
 void chol_drop(int k, const double* G, int ldg, double tol, double* T, int* kept, int* nk,
-               cudaStream_t st);
+               double* work, cudaStream_t st);
 void gather_cols(const double* src, int lds, int r0, int rows, const IntList& idx, int ncols,
                  double* dst, int ldd, cudaStream_t st);
 void set_diag(double* M, int ld, const double* d, int k, cudaStream_t st);

@@ -800,7 +800,8 @@ static int cholqr2(Solver* s, std::vector<double*>& V, int start, int* end,
     KL(gram(s, W, k, BW, k, s->sub_tmp2, k, true));
     int* kept = s->d_int;
     int* nk = s->d_int + GCGE_MAXCOLS;
-    KL(gcge::chol_drop(k, s->sub_tmp2, k, s->para.orth_zero_tol, s->sub_tmp, kept, nk, s->st));
+    KL(gcge::chol_drop(k, s->sub_tmp2, k, s->para.orth_zero_tol, s->sub_tmp, kept, nk,
+                       s->jac_work, s->st));
     int h[GCGE_MAXCOLS + 1];
     CU(cudaMemcpyAsync(h, s->d_int, sizeof(int) * (GCGE_MAXCOLS + 1), cudaMemcpyDeviceToHost, s->st));
     CHK(sync(s));

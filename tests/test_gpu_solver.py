@@ -160,3 +160,19 @@ def test_solver_headline_workload_matches_reference(cuda_lib, precision):
     assert O.true_residuals(A, B, ev, vec).max() <= 1e-10
     assert b_orthonormality(B, vec) < 1e-9
     assert abs(st["num_iter"] - ref["iters"]) <= 5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solver_nev128_analytic(cuda_lib, precision):
+    """nev = 128 (a 198-column basis: the projected matrices and the Cholesky
+    of the initial block no longer fit in one CTA's shared memory) on the 2D
+    Laplacian, whose eigenvalues are known in closed form."""
+    m, nev = 100, 128
+    A = M.laplace2d(m)
+    t = 2.0 - 2.0 * np.cos(np.arange(1, m + 1) * np.pi / (m + 1))
+    exact = np.sort((t[:, None] + t[None, :]).ravel())[:nev]
+    x0 = M.initial_block(A.n, nev, seed=11)
+    ev, vec, st = S.solve(A, None, nev, x0, ev_tol=1e-10, ev_max_it=400, precision=precision)
+    np.testing.assert_allclose(ev, exact, rtol=1e-9)
+    crit = O.true_residuals(A, None, ev, vec) * np.abs(ev) / np.maximum(1.0, np.abs(ev))
+    assert crit.max() < 2e-10
