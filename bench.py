@@ -552,7 +552,7 @@ def run_config5(args):
         st = s.stats()
     finally:
         s.close()
-    tr = true_residuals_gpu(torch, A, B, ev2, vec)
+    tr = true_residuals_gpu(torch, A, B, ev2, torch.from_numpy(vec).to("cuda"))
     ref_crit = tr * np.abs(ev2) / np.maximum(1.0, np.abs(ev2))
     del vec
     # directional finite difference along a random relative change of the edge weights
