@@ -42,9 +42,12 @@ eigendecomposition.
 --config 5 runs the uneven-row configuration: the shifted graph Laplacian
 A = L + 1e-3 I of a seeded Chung-Lu power-law graph (n = 8M, mean degree 16,
 exponent 2.5, edge weights U(0.5, 1.5)) with B = D, nev = 128, in mixed
-precision; it reports the solve, both residual criteria per pair, and the
-gradient of sum_k w_k lambda_k with respect to the edge weights with a
-directional finite-difference check (two more solves).
+precision, capped at --c5it GCG iterations (the reference's method converges
+slowly on this clustered spectrum: its oracle port leaves 23 of 128 pairs above
+1e-10 after 300 iterations at n = 20,000); it reports the time per iteration,
+the converged pairs, and the gradient of sum_k w_k lambda_k over the leading
+converged pairs (up to 8) with respect to the edge weights, with a directional
+finite-difference check (two more solves).
 """
 from __future__ import annotations
 
@@ -522,6 +525,7 @@ def run_config5(args):
     import __graft_entry__ as g
     g.build()
     from gcge_old_gb300 import matrices as M
+    from gcge_old_gb300 import solver as S
     from gcge_old_gb300.autograd import eigvals_csr
     n, nev = args.c5n, 128
     t0 = time.time()
@@ -529,33 +533,37 @@ def run_config5(args):
     gen_s = time.time() - t0
     rows = np.diff(A.rowptr)
     x0 = M.initial_block(n, nev, seed=0)
-    params = dict(ev_tol=1e-10, ev_max_it=1000, precision="mixed")
+    params = dict(ev_tol=1e-10, ev_max_it=args.c5it, precision="mixed")
+    s = S.GCGESolver(A, B, nev, **params)
+    try:
+        ev, vec = s.solve(x0)
+        st = s.stats()
+    finally:
+        s.close()
+    vec_d = torch.from_numpy(vec).to("cuda")
+    del vec
+    tr = true_residuals_gpu(torch, A, B, ev, vec_d)
+    del vec_d
+    torch.cuda.empty_cache()
+    crit = tr * np.abs(ev) / np.maximum(1.0, np.abs(ev))
+    nconv = int(np.argmax(crit >= 1e-10)) if (crit >= 1e-10).any() else nev
+    # gradient of sum_k w_k lambda_k over the leading converged pairs (at most 8)
+    # with respect to the edge weights, and a directional finite difference
+    kl = min(8, nconv)
+    wl = np.zeros(nev)
+    wl[:kl] = np.random.default_rng(1).uniform(0.0, 1.0, kl)
+    wl_t = torch.from_numpy(wl)
     a = torch.tensor(A.val, requires_grad=True)
     b = torch.tensor(B.val, requires_grad=True)
-    wl = torch.from_numpy(np.random.default_rng(1).uniform(0.0, 1.0, nev))
-    torch.cuda.synchronize()
     t1 = time.time()
     lam = eigvals_csr(a, A, nev, x0, b_val=b, B_pattern=B, **params)
     t2 = time.time()
-    (wl * lam).sum().backward()
+    (wl_t * lam).sum().backward()
     torch.cuda.synchronize()
     t3 = time.time()
     p_ij, p_ji, p_ii, p_jj, bi, bj = pos
     ga, gb = a.grad.numpy(), b.grad.numpy()
     gw = -ga[p_ij] - ga[p_ji] + ga[p_ii] + ga[p_jj] + gb[bi] + gb[bj]
-    ev = lam.detach().numpy()
-    # residuals from a plain solve (the autograd path keeps no vectors for the caller)
-    from gcge_old_gb300 import solver as S
-    s = S.GCGESolver(A, B, nev, **params)
-    try:
-        ev2, vec = s.solve(x0)
-        st = s.stats()
-    finally:
-        s.close()
-    tr = true_residuals_gpu(torch, A, B, ev2, torch.from_numpy(vec).to("cuda"))
-    ref_crit = tr * np.abs(ev2) / np.maximum(1.0, np.abs(ev2))
-    del vec
-    # directional finite difference along a random relative change of the edge weights
     d = np.random.default_rng(2).standard_normal(len(ew)) * ew
     eps = 1e-6
 
@@ -570,24 +578,29 @@ def run_config5(args):
         with torch.no_grad():
             l = eigvals_csr(torch.from_numpy(av), A, nev, x0, b_val=torch.from_numpy(bv),
                             B_pattern=B, **params)
-        return float((wl * l).sum())
+        return float((wl_t * l).sum())
 
     fd = (lam_sum(1) - lam_sum(-1)) / (2 * eps)
     adj = float(gw @ d)
-    out = {"metric": "s to nev eigenpairs @1e-10 (uneven rows, mixed) + edge-weight gradient",
+    out = {"metric": "s per GCG iteration and pairs converged @1e-10 (uneven rows, mixed) "
+                     "+ edge-weight gradient",
            "config": {"workload": "chung_lu_n%d_deg16_gamma2.5_shift1e-3_B=D_nev%d" % (n, nev),
                       "n": n, "nnz_A": int(A.nnz), "max_row": int(rows.max()),
                       "rows_over_64": int((rows > 64).sum()),
-                      "entries_in_rows_over_64": float(rows[rows > 64].sum() / A.nnz)},
-           "solve_s": st["seconds"], "forward_s_autograd": t2 - t1, "backward_s": t3 - t2,
-           "gcg_iterations": st["num_iter"], "bcg_steps": st["bcg_steps"],
+                      "entries_in_rows_over_64": float(rows[rows > 64].sum() / A.nnz),
+                      "ev_max_it": args.c5it},
+           "solve_s": st["seconds"], "gcg_iterations": st["num_iter"],
+           "s_per_iteration": st["seconds"] / max(1, st["num_iter"]),
+           "bcg_steps": st["bcg_steps"],
            "phase_s": {k: round(v, 3) for k, v in st.items() if k.startswith("t_")},
-           "eigenvalues_min_max": [float(ev2.min()), float(ev2.max())],
-           "reference_criterion_max": float(ref_crit.max()),
-           "relative_residual_max": float(tr.max()),
-           "relative_residual_max_pairs_2_on": float(tr[1:].max()),
-           "edge_gradient_directional_fd": {"fd": fd, "adjoint": adj,
-                                            "rel": abs(fd - adj) / abs(adj), "eps": eps},
+           "pairs_converged_leading": nconv,
+           "pairs_converged_total": int((crit < 1e-10).sum()),
+           "reference_criterion_max": float(crit.max()),
+           "eigenvalues_first_last": [float(ev[0]), float(ev[-1])],
+           "gradient": {"loss": "sum_{k<%d} w_k lambda_k" % kl, "forward_s": t2 - t1,
+                        "backward_s": t3 - t2,
+                        "directional_fd": {"fd": fd, "adjoint": adj,
+                                           "rel": abs(fd - adj) / abs(adj), "eps": eps}},
            "generator_s": gen_s, "data": "synthetic (seeded generator)"}
     print(json.dumps(out))
     return 0
@@ -602,6 +615,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="48^3 grid (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--c5n", type=int, default=8_000_000, help="graph size of --config 5")
+    ap.add_argument("--c5it", type=int, default=100, help="GCG iteration cap of --config 5")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
                     help="3: the 160^3 27-point mixed-precision configuration (one solve each); "
                          "4: the 512^2 differentiation configuration (gradient checks)")
