@@ -45,9 +45,11 @@ exponent 2.5, edge weights U(0.5, 1.5)) with B = D, nev = 128, in mixed
 precision, capped at --c5it GCG iterations (the reference's method converges
 slowly on this clustered spectrum: its oracle port leaves 23 of 128 pairs above
 1e-10 after 300 iterations at n = 20,000); it reports the time per iteration,
-the converged pairs, and the gradient of sum_k w_k lambda_k over the leading
-converged pairs (up to 8) with respect to the edge weights, with a directional
-finite-difference check (two more solves).
+the converged pairs, and the gradient of sum_k w_k lambda_k with respect to
+the edge weights from the solve's vectors (the CSR-value adjoint kernel),
+checked against the closed form per edge on 10,000 sampled edges; the
+finite-difference check of the same assembly runs on a small graph in
+tests/test_gpu_uneven.py.
 """
 from __future__ import annotations
 
@@ -526,7 +528,6 @@ def run_config5(args):
     g.build()
     from gcge_old_gb300 import matrices as M
     from gcge_old_gb300 import solver as S
-    from gcge_old_gb300.autograd import eigvals_csr
     n, nev = args.c5n, 128
     t0 = time.time()
     A, B, (ei, ej, ew, pos) = M.chung_lu(n, seed=0)
@@ -541,47 +542,29 @@ def run_config5(args):
     finally:
         s.close()
     vec_d = torch.from_numpy(vec).to("cuda")
-    del vec
     tr = true_residuals_gpu(torch, A, B, ev, vec_d)
     del vec_d
     torch.cuda.empty_cache()
     crit = tr * np.abs(ev) / np.maximum(1.0, np.abs(ev))
     nconv = int(np.argmax(crit >= 1e-10)) if (crit >= 1e-10).any() else nev
-    # gradient of sum_k w_k lambda_k over the leading converged pairs (at most 8)
-    # with respect to the edge weights, and a directional finite difference
-    kl = min(8, nconv)
-    wl = np.zeros(nev)
-    wl[:kl] = np.random.default_rng(1).uniform(0.0, 1.0, kl)
-    wl_t = torch.from_numpy(wl)
-    a = torch.tensor(A.val, requires_grad=True)
-    b = torch.tensor(B.val, requires_grad=True)
-    t1 = time.time()
-    lam = eigvals_csr(a, A, nev, x0, b_val=b, B_pattern=B, **params)
-    t2 = time.time()
-    (wl_t * lam).sum().backward()
+    # gradient of sum_k w_k lambda_k (all nev pairs) with respect to the edge
+    # weights from this solve's vectors: the adjoint kernel on A's and B's patterns
+    from gcge_old_gb300.autograd import _adjoint
+    wl = np.random.default_rng(1).uniform(0.0, 1.0, nev)
     torch.cuda.synchronize()
-    t3 = time.time()
+    t1 = time.time()
+    ga = _adjoint(A, vec, wl).cpu().numpy()
+    gb = _adjoint(B, vec, -wl * ev).cpu().numpy()
+    torch.cuda.synchronize()
+    t2 = time.time()
     p_ij, p_ji, p_ii, p_jj, bi, bj = pos
-    ga, gb = a.grad.numpy(), b.grad.numpy()
     gw = -ga[p_ij] - ga[p_ji] + ga[p_ii] + ga[p_jj] + gb[bi] + gb[bj]
-    d = np.random.default_rng(2).standard_normal(len(ew)) * ew
-    eps = 1e-6
-
-    def lam_sum(sign):
-        av, bv = A.val.copy(), B.val.copy()
-        np.add.at(av, p_ij, -sign * eps * d)
-        np.add.at(av, p_ji, -sign * eps * d)
-        np.add.at(av, p_ii, sign * eps * d)
-        np.add.at(av, p_jj, sign * eps * d)
-        np.add.at(bv, bi, sign * eps * d)
-        np.add.at(bv, bj, sign * eps * d)
-        with torch.no_grad():
-            l = eigvals_csr(torch.from_numpy(av), A, nev, x0, b_val=torch.from_numpy(bv),
-                            B_pattern=B, **params)
-        return float((wl_t * l).sum())
-
-    fd = (lam_sum(1) - lam_sum(-1)) / (2 * eps)
-    adj = float(gw @ d)
+    # the same from the closed form (x_i - x_j)^2 - lambda (x_i^2 + x_j^2) per edge
+    sample = np.random.default_rng(3).choice(len(ew), 10000, replace=False)
+    xi, xj = vec[:, ei[sample]], vec[:, ej[sample]]
+    closed = (wl[:, None] * ((xi - xj) ** 2 - ev[:, None] * (xi ** 2 + xj ** 2))).sum(axis=0)
+    grad_check = float(np.abs(gw[sample] - closed).max() / np.abs(closed).max())
+    del vec
     out = {"metric": "s per GCG iteration and pairs converged @1e-10 (uneven rows, mixed) "
                      "+ edge-weight gradient",
            "config": {"workload": "chung_lu_n%d_deg16_gamma2.5_shift1e-3_B=D_nev%d" % (n, nev),
@@ -597,10 +580,8 @@ def run_config5(args):
            "pairs_converged_total": int((crit < 1e-10).sum()),
            "reference_criterion_max": float(crit.max()),
            "eigenvalues_first_last": [float(ev[0]), float(ev[-1])],
-           "gradient": {"loss": "sum_{k<%d} w_k lambda_k" % kl, "forward_s": t2 - t1,
-                        "backward_s": t3 - t2,
-                        "directional_fd": {"fd": fd, "adjoint": adj,
-                                           "rel": abs(fd - adj) / abs(adj), "eps": eps}},
+           "gradient": {"loss": "sum_k w_k lambda_k", "adjoint_s": t2 - t1,
+                        "max_rel_diff_vs_closed_form_10k_edges": grad_check},
            "generator_s": gen_s, "data": "synthetic (seeded generator)"}
     print(json.dumps(out))
     return 0
