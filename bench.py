@@ -688,6 +688,8 @@ def main():
         "max_residual": {"mixed": float(res_m.max()), "fp64": float(res_d.max())},
         "eigenvalue_rel_diff_mixed_vs_fp64": ev_rel,
         "phase_s_mixed": {k: round(v, 4) for k, v in st_mixed[-1].items() if k.startswith("t_")},
+        "w_orth_passes": {"mixed": st_mixed[-1]["w_orth_passes"],
+                          "fp64": st_fp64[-1]["w_orth_passes"]},
         "roofline": {"kernel": "k_rows_spmm<12> (FP32 CSR SpMM of the block CG, k=10, "
                                "row-interleaved)", "bound": "hbm",
                      "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,

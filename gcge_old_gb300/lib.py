@@ -40,7 +40,7 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_longlong), ("seconds", C.c_double),
                 ("t_x_orth", C.c_double), ("t_rr_mat", C.c_double), ("t_rr_eig", C.c_double),
                 ("t_x_axpy", C.c_double), ("t_p", C.c_double), ("t_w_line", C.c_double),
-                ("t_w_orth", C.c_double), ("t_conv", C.c_double)]
+                ("t_w_orth", C.c_double), ("t_conv", C.c_double), ("w_orth_passes", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

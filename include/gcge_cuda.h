@@ -51,6 +51,7 @@ typedef struct GCGE_CUDA_STATS_ {
   long long kernel_launches;
   double seconds;          /* wall time of Solve, host clock */
   double t_x_orth, t_rr_mat, t_rr_eig, t_x_axpy, t_p, t_w_line, t_w_orth, t_conv;
+  int w_orth_passes;       /* block Gram-Schmidt passes of the W orthogonalisation */
 } GCGE_CUDA_STATS;
 
 /* ---------------------------------------------------------------- errors */
