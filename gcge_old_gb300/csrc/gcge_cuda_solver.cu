@@ -856,27 +856,21 @@ static int w_orth(Solver* s, int start, int* end) {
         KL(gcge::apply_b_f64(Bptr(s), W, T, l2, s->n, s->st));
         KL(gram(s, V1, start, T, l2, s->sub_tmp2, start, false));
       }
+      if (ozl) {
+        // W <- W - V1 G
+        KL(gcge::lincomb_oz(V1, start, s->sub_tmp2, start, W, l2, 1.0, s->n, s->oz_scratch, s->st,
+                            false, true));
+      } else {
+        KL(lincomb(s, V1, start, s->sub_tmp2, start, T, l2, 0.0));
+        KL(gcge::axpby_f64(-1.0, T, 1.0, W, l2, s->n, s->st));
+      }
+      // ||G||_F is an absolute measure (W is not normalised yet), so the update
+      // of the last pass is kept even when ||G||_F is below the tolerance
       KL((k_frob<<<1, 256, 0, s->st>>>(s->sub_tmp2, start, l2, s->d_small)));
       double h = 0.0;
       CU(cudaMemcpyAsync(&h, s->d_small, sizeof(double), cudaMemcpyDeviceToHost, s->st));
       CHK(sync(s));
       vi = h;
-      // The reference applies W <- W - V1 G on every pass, then stops once
-      // ||G||_F <= scbgs_reorth_tol.  On that last pass the coupling V1^T B W is
-      // already within the tolerance (||G||_F <= 1e-16 + eps: a change of W at
-      // its own rounding level), so the update is skipped: one tall-skinny
-      // product less per GCG iteration, same stopping rule.
-      const bool last = !(vi > p.scbgs_reorth_tol + 2.220446049250313e-16);
-      if (!last) {
-        if (ozl) {
-          // W <- W - V1 G
-          KL(gcge::lincomb_oz(V1, start, s->sub_tmp2, start, W, l2, 1.0, s->n, s->oz_scratch,
-                              s->st, false, true));
-        } else {
-          KL(lincomb(s, V1, start, s->sub_tmp2, start, T, l2, 0.0));
-          KL(gcge::axpby_f64(-1.0, T, 1.0, W, l2, s->n, s->st));
-        }
-      }
       s->stats.w_orth_passes++;
       if (it >= p.max_reorth_time) break;
     }
