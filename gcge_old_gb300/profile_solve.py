@@ -9,6 +9,15 @@ launches, five FP32 column launches, five FP32 row-interleaved launches), for
 traffic counters of those kernels:
 
     python -m gcge_old_gb300.profile_solve --grid 96 --spmm 10
+
+--graph N solves the shifted Laplacian of an N-node Chung-Lu graph with B = D
+instead (uneven rows); --aniso M --adjoint K solves the 2D anisotropic problem
+on an M x M grid and then runs K steps of the eigenvector adjoint's projected
+CG for the first eigenvector (a bounded launch sequence: the adjoint stops
+there whether or not it converged):
+
+    python -m gcge_old_gb300.profile_solve --graph 1000000 --nev 128 --iters 3
+    python -m gcge_old_gb300.profile_solve --aniso 512 --nev 32 --adjoint 200
 """
 import argparse
 
@@ -45,6 +54,32 @@ def spmm_only(A, k):
     print("spmm n=%d nnz=%d k=%d done" % (A.n, A.nnz, k))
 
 
+def adjoint_steps(A, B, nev, steps):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from . import lib as L
+    lib = L.load()
+    x0 = M.initial_block(A.n, nev, seed=0)
+    ev, vec, _ = S.solve(A, B, nev, x0, ev_tol=1e-12, ev_max_it=2000, precision="fp64")
+    X = torch.from_numpy(vec).cuda()
+    G = torch.zeros_like(X)
+    G[0] = torch.randn(A.n, dtype=torch.float64, device="cuda")
+    MU = torch.zeros_like(X)
+    cols = lambda t, on: (C.c_void_p * nev)(*[C.c_void_p(t[j].data_ptr()) if on(j) else None
+                                              for j in range(nev)])
+    dA, dB = S.DeviceMatrix(A), S.DeviceMatrix(B)
+    it = C.c_int(0)
+    rc = lib.GCGE_CUDA_EigvecAdjointSolve(dA.handle, dB.handle, cols(X, lambda j: True),
+                                          ev.ctypes.data_as(L.c_double_p), nev,
+                                          cols(G, lambda j: j == 0), cols(MU, lambda j: j == 0),
+                                          None, steps, 1e-10, C.byref(it))
+    torch.cuda.synchronize()
+    print("adjoint n=%d nev=%d steps=%d rc=%d" % (A.n, nev, it.value, rc))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--grid", type=int, default=96)
@@ -53,8 +88,19 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--gemm", default="ozaki", choices=["ozaki", "fp64"])
     ap.add_argument("--spmm", type=int, default=0, help="only K-column SpMMs")
+    ap.add_argument("--graph", type=int, default=0, help="Chung-Lu graph with this many nodes")
+    ap.add_argument("--aniso", type=int, default=0, help="2D anisotropic grid size")
+    ap.add_argument("--adjoint", type=int, default=0, help="eigenvector-adjoint CG steps")
     a = ap.parse_args()
-    A, B = M.laplace3d_mass(a.grid, seed=0)
+    if a.graph:
+        A, B, _ = M.chung_lu(a.graph, seed=0)
+    elif a.aniso:
+        A, B, _, _ = M.aniso2d(a.aniso, seed=0)
+    else:
+        A, B = M.laplace3d_mass(a.grid, seed=0)
+    if a.adjoint:
+        adjoint_steps(A, B, a.nev, a.adjoint)
+        return
     if a.spmm:
         spmm_only(A, a.spmm)
         return
