@@ -414,6 +414,191 @@ size_t jacobi_smem_bytes(int nrows) {
   return sizeof(double) * 2 * (size_t)mp * mp;
 }
 
+// Final stage of jacobi_eig.  After the refinement, S = X^T A X is diagonal
+// up to couplings below 1e-14 ||A||_F except between pairs the refinement
+// marked as clustered.  Rather than sweeping all m(m-1)/2 pairs (m - 1 rounds
+// of block-wide barriers per sweep), the clusters -- connected components of
+// the marked pairs and of any coupling still above 1e-14 ||A||_F -- are solved
+// independently, one warp each, by cyclic FP64 Jacobi on their principal
+// submatrix; Z is block diagonal.  Same rotation formula, thresholds and
+// output order as k_jacobi (mode 0): eigenvalues il..iu ascending (NaN last,
+// ties by index), eigenvector columns signed so the largest-magnitude entry is
+// positive.  work: 2 m^2 doubles (each cluster of size c > 1 takes 2 c^2:
+// its submatrix and its eigenvectors).  One CTA; status[0] = sweeps of the
+// slowest cluster, or -1 if a cluster did not converge.
+__global__ void __launch_bounds__(1024, 1)
+    k_cluster_jacobi(int m, const double* __restrict__ S, const unsigned char* __restrict__ mask,
+                     const double* __restrict__ normA, double* __restrict__ eval,
+                     double* __restrict__ Z, int ldz, int il, int iu, double* __restrict__ work,
+                     int* __restrict__ status, double tol, int max_sweeps) {
+  __shared__ int label[256], order[256], cstart[257], rank_of[256], cl[256], cpos[256];
+  __shared__ size_t coff[257];
+  __shared__ int ncl, worst;
+  __shared__ double d[256];
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  const double thr = 1e-14 * normA[0];
+  for (int i = tid; i < m; i += nt) label[i] = i;
+  if (tid == 0) worst = 0;
+  __syncthreads();
+  // connected components by min-label propagation (at most m rounds; the
+  // exit test is a block-wide vote, so every thread leaves the loop together)
+  for (int round = 0; round < m; round++) {
+    int mine = 0;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e % m, j = e / m;
+      if (i >= j) continue;
+      if (!(mask[e] || fabs(S[e]) > thr)) continue;
+      const int a = label[i], b = label[j];
+      if (a != b) {
+        const int l = a < b ? a : b;
+        atomicMin(&label[i], l);
+        atomicMin(&label[j], l);
+        mine = 1;
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += nt) {  // pointer jumping
+      int l = label[i];
+      while (label[l] != l) l = label[l];
+      label[i] = l;
+    }
+    if (!__syncthreads_or(mine)) break;
+  }
+  // group the members of each cluster, in index order (serial: m <= 256)
+  if (tid == 0) {
+    int nc = 0, pos = 0;
+    size_t off = 0;
+    for (int r = 0; r < m; r++) {
+      if (label[r] != r) continue;
+      cstart[nc] = pos;
+      coff[nc] = off;
+      for (int i = r; i < m; i++)
+        if (label[i] == r) {
+          cl[i] = nc;
+          cpos[i] = pos - cstart[nc];
+          order[pos++] = i;
+        }
+      const size_t sz = (size_t)(pos - cstart[nc]);
+      if (sz > 1) off += 2 * sz * sz;
+      nc++;
+    }
+    cstart[nc] = pos;
+    coff[nc] = off;
+    ncl = nc;
+  }
+  __syncthreads();
+  for (int i = tid; i < m; i += nt) d[i] = S[i + (size_t)i * m];
+  // one warp per cluster of size > 1
+  for (int c = warp; c < ncl; c += nt >> 5) {
+    const int b0 = cstart[c], sz = cstart[c + 1] - b0;
+    if (sz == 1) continue;
+    // this cluster's submatrix (from the upper triangle) and eigenvectors
+    double* A = work + coff[c];
+    double* V = A + (size_t)sz * sz;
+    for (int e = lane; e < sz * sz; e += 32) {
+      const int a = e % sz, b = e / sz;
+      const int ia = order[b0 + a], ib = order[b0 + b];
+      A[e] = (ia <= ib) ? S[ia + (size_t)ib * m] : S[ib + (size_t)ia * m];
+      V[e] = (a == b) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    int sweep = 0;
+    bool conv = false;
+    for (; sweep < max_sweeps; sweep++) {
+      int did = 0;
+      for (int p = 0; p < sz - 1; p++)
+        for (int q = p + 1; q < sz; q++) {
+          const double apq = A[p + q * sz], app = A[p + p * sz], aqq = A[q + q * sz];
+          if (!(fabs(apq) > 1e-300 && fabs(apq) > tol * sqrt(fabs(app) * fabs(aqq)))) continue;
+          const double theta = (aqq - app) / (2.0 * apq);
+          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+          did = 1;
+          __syncwarp();
+          for (int j = lane; j < sz; j += 32) {  // rows p, q
+            const double x = A[p + j * sz], y = A[q + j * sz];
+            A[p + j * sz] = cs * x - sn * y;
+            A[q + j * sz] = sn * x + cs * y;
+          }
+          __syncwarp();
+          for (int i = lane; i < sz; i += 32) {  // columns p, q of A and V
+            const double x = A[i + p * sz], y = A[i + q * sz];
+            A[i + p * sz] = cs * x - sn * y;
+            A[i + q * sz] = sn * x + cs * y;
+            const double v1 = V[i + p * sz], v2 = V[i + q * sz];
+            V[i + p * sz] = cs * v1 - sn * v2;
+            V[i + q * sz] = sn * v1 + cs * v2;
+          }
+          __syncwarp();
+          if (lane == 0) {
+            A[q + p * sz] = 0.0;
+            A[p + q * sz] = 0.0;
+          }
+          __syncwarp();
+        }
+      if (!did) {
+        conv = true;
+        break;
+      }
+    }
+    for (int a = lane; a < sz; a += 32) d[order[b0 + a]] = A[a + a * sz];
+    if (lane == 0) atomicMax(&worst, conv ? sweep : 1 << 20);
+  }
+  __syncthreads();
+  // ascending order by rank (NaN as +inf, ties by index)
+  for (int i = tid; i < m; i += nt) {
+    double di = d[i];
+    if (di != di) di = INFINITY;
+    int rk = 0;
+    for (int j = 0; j < m; j++) {
+      double dj = d[j];
+      if (dj != dj) dj = INFINITY;
+      if (dj < di || (dj == di && j < i)) rk++;
+    }
+    rank_of[rk] = i;
+  }
+  __syncthreads();
+  const int nout = iu - il + 1;
+  for (int kk = tid; kk < nout; kk += nt) eval[kk] = d[rank_of[il - 1 + kk]];
+  // eigenvector of index c: column cpos[c] of its cluster's V on the
+  // cluster's rows (e_c for a singleton), zero elsewhere
+  auto zval = [&](int i, int c) -> double {
+    const int k = cl[c];
+    if (cl[i] != k) return 0.0;
+    const int sz = cstart[k + 1] - cstart[k];
+    if (sz == 1) return 1.0;
+    const double* V = work + coff[k] + (size_t)sz * sz;
+    return V[cpos[i] + (size_t)cpos[c] * sz];
+  };
+  for (int kk = warp; kk < nout; kk += nt >> 5) {
+    const int c = rank_of[il - 1 + kk];
+    double best = -1.0, bv = 0.0;
+    int bi = m;
+    for (int i = lane; i < m; i += 32) {
+      const double v = zval(i, c);
+      if (fabs(v) > best || (fabs(v) == best && i < bi)) {
+        best = fabs(v);
+        bv = v;
+        bi = i;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const double ov = __shfl_down_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bv = ov;
+        bi = oi;
+      }
+    }
+    bv = __shfl_sync(0xffffffffu, bv, 0);
+    const double sg = bv < 0 ? -1.0 : 1.0;
+    for (int i = lane; i < m; i += 32) Z[i + (size_t)kk * ldz] = sg * zval(i, c);
+  }
+  if (tid == 0) status[0] = worst >= (1 << 20) ? -1 : worst;
+}
+
 template <typename T>
 static void launch_jacobi(int nrows, const double* a, int lda, double* eval, double* evec, int lde,
                           int il, int iu, T* work, int* status, int mode, double tol,
@@ -548,8 +733,8 @@ void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec,
   }
   dgemm_small(false, false, true, m, m, m, 1.0, a, lda, X, m, 0.0, AX, m, st);
   dgemm_small(true, false, false, m, m, m, 1.0, X, m, AX, m, 0.0, S, m, st);
-  launch_jacobi<double>(m, S, m, eval, Z, m, il, iu, (double*)jw, status, 0, 1e-15, 60, st, mask,
-                        normA_dev);
+  k_cluster_jacobi<<<1, 1024, 0, st>>>(m, S, mask, normA_dev, eval, Z, m, il, iu, (double*)jw,
+                                       status, 1e-15, 60);
   const int nout = iu - il + 1;
   dgemm_small(false, false, false, m, nout, m, 1.0, X, m, Z, m, 0.0, evec, lde, st);
 }

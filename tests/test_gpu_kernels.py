@@ -104,7 +104,7 @@ def test_axpby(cuda_lib):
 
 
 @pytest.mark.parametrize("m,il,iu", [(12, 1, 12), (80, 1, 40), (91, 3, 70), (150, 1, 150),
-                                     (2, 1, 2), (1, 1, 1)])
+                                     (2, 1, 2), (1, 1, 1), (198, 1, 148), (256, 5, 256)])
 def test_dense_eigensolver(cuda_lib, m, il, iu):
     rng = np.random.default_rng(m)
     Q, _ = np.linalg.qr(rng.standard_normal((m, m)))
@@ -261,7 +261,8 @@ def test_ozaki_lincomb_unbalanced_columns(cuda_lib):
     assert np.abs(got - ref).max() < 1e-15 * np.abs(ref).max() * 10
 
 
-@pytest.mark.parametrize("m,kind", [(60, "near"), (90, "many"), (120, "graded"), (30, "near")])
+@pytest.mark.parametrize("m,kind", [(60, "near"), (90, "many"), (120, "graded"), (30, "near"),
+                                    (198, "many"), (256, "near")])
 def test_dense_eigensolver_clusters(cuda_lib, m, kind):
     """Near-degenerate and graded spectra (the FP32 stage cannot separate
     them; the refinement and the clustered-pair Jacobi must)."""
