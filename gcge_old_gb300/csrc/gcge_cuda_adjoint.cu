@@ -82,6 +82,33 @@ void dots(const ColList<double>& X, const ColList<double>& Y, int m, int n, doub
   k_dots_sum<<<m, 32, 0, st>>>(partial, m, out);
 }
 
+// partial[(j + k1 * c) * gridDim.x + b] = block b's share of X_j . U_c: one
+// block row per (j, c) pair, so a k1 x m Gram with m small keeps every SM busy
+__global__ void k_pair_dots(ColList<double> X, int k1, ColList<double> U, int n,
+                            double* __restrict__ partial) {
+  __shared__ double sh[256];
+  const int pr = blockIdx.y, j = pr % k1, c = pr / k1;
+  const double* __restrict__ x = X.p[j];
+  const double* __restrict__ u = U.p[c];
+  double s = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    s = fma(x[r], u[r], s);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(size_t)pr * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// G[j + c * k1] = X_j . U_c (j < k1, c < m), fixed summation order
+void pair_gram(const ColList<double>& X, int k1, const ColList<double>& U, int m, int n,
+               double* partial, double* G, cudaStream_t st) {
+  k_pair_dots<<<dim3(kDotBlocks, k1 * m), 256, 0, st>>>(X, k1, U, n, partial);
+  k_dots_sum<<<k1 * m, 32, 0, st>>>(partial, k1 * m, G);
+}
+
 __global__ void k_diag_inv(int n, const int* __restrict__ rp, const int* __restrict__ ci,
                            const double* __restrict__ v, double* __restrict__ dinv) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -253,11 +280,9 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
   double* pu = q + 2 * GCGE_MAXCOLS;
   double* rr = q + 3 * GCGE_MAXCOLS;
   int* active = reinterpret_cast<int*>(q + 4 * GCGE_MAXCOLS);
-  // Gram partials: per row block either k1 * k2 values or whole 64 x 64 tiles
-  const size_t tiles = (size_t)((nev + 63) / 64) * ((m + 63) / 64);
+  // Gram partials: kDotBlocks per (column of X, column of U) pair
   double* gp = nullptr;
-  if (cudaMalloc(&gp, sizeof(double) * gcge::kRowBlocks *
-                          std::max<size_t>((size_t)nev * m, tiles * 64 * 64)) != cudaSuccess)
+  if (cudaMalloc(&gp, sizeof(double) * kDotBlocks * (size_t)nev * m) != cudaSuccess)
     return gcge_record_error(GCGE_CUDA_ERR_ALLOC, "EigvecAdjointSolve: device memory");
   struct Free {
     double* p;
@@ -273,7 +298,7 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
   k_diag_inv<<<(n + 255) / 256, 256, 0, st>>>(n, A->m.rp, A->m.ci, A->m.v, dinv);
   gcge::apply_b_f64(Bm, Xl, BX, nev, n, st);
   // x_j^T g_k (nev x m) to the host: the coefficients over the computed pairs
-  gcge::gram_f64(Xl, nev, Gl, m, n, Gm, nev, false, gp, st);
+  pair_gram(Xl, nev, Gl, m, n, gp, Gm, st);
   std::vector<double> hg((size_t)nev * m), hc((size_t)nev * m, 0.0);
   if (cudaMemcpyAsync(hg.data(), Gm, sizeof(double) * nev * m, cudaMemcpyDeviceToHost, st) !=
       cudaSuccess)
@@ -297,7 +322,7 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
   // Z = Q D^-1 R = D^-1 R - X (BX^T D^-1 R); P = Z
   auto precond = [&]() {
     k_precond<<<gcol, 256, 0, st>>>(R, Z, dinv, n);
-    gcge::gram_f64(BX, nev, Z, m, n, Gm, nev, false, gp, st);
+    pair_gram(BX, nev, Z, m, n, gp, Gm, st);
     k_sub_lincomb<<<nb_rows, 256, shm, st>>>(Z, Xl, Gm, nev, nev, m, n);
   };
   precond();
@@ -325,7 +350,7 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
     } else {
       k_shift_sub<<<gcol, 256, 0, st>>>(U, P, lam, n);
     }
-    gcge::gram_f64(Xl, nev, U, m, n, Gm, nev, false, gp, st);
+    pair_gram(Xl, nev, U, m, n, gp, Gm, st);
     k_sub_lincomb<<<nb_rows, 256, shm, st>>>(U, BX, Gm, nev, nev, m, n);
     dots(P, U, m, n, partial, pu, st);
     k_step<<<gcol, 256, 0, st>>>(Ml, R, P, U, rz, pu, active, n);
