@@ -311,6 +311,20 @@ __device__ __forceinline__ void store_row(float* base, size_t r, const float* v)
   for (int q = 0; q < KW / 4; q++) p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
+// v = the product of heavy row h: its chunk partials in chunk order
+template <int KW>
+__device__ __forceinline__ void heavy_row_sum(const int* __restrict__ hch,
+                                              const float* __restrict__ cb, int h, float* v) {
+#pragma unroll
+  for (int c = 0; c < KW; c++) v[c] = 0.f;
+  for (int q = __ldg(hch + h); q < __ldg(hch + h + 1); q++) {
+    float t[KW];
+    load_row<KW>(cb, q, t);
+#pragma unroll
+    for (int c = 0; c < KW; c++) v[c] += t[c];
+  }
+}
+
 // r = rhs - A x and partial ||r_c||^2 (c < len)
 template <int KW>
 __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__ rp,
@@ -319,6 +333,7 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
                                                   const float* __restrict__ X, float* R, int len,
                                                   double* __restrict__ partial,
                                                   const int* __restrict__ hidx,
+                                                  const int* __restrict__ hch,
                                                   const float* __restrict__ hb) {
   __shared__ double sh[(kT / 32) * 32];
   float acc2[KW];
@@ -330,7 +345,7 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
     for (int c = 0; c < KW; c++) ax[c] = 0.f;
     const int h = hidx ? __ldg(hidx + r) : -1;
     if (h >= 0) {
-      load_row<KW>(hb, h, ax);
+      heavy_row_sum<KW>(hch, hb, h, ax);
     } else {
       for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
         const int col = __ldg(ci + j);
@@ -384,6 +399,7 @@ __global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ r
                                                 const float* __restrict__ P, float* W, int len,
                                                 BcgScalars s, double* __restrict__ partial,
                                                 const int* __restrict__ hidx,
+                                                const int* __restrict__ hch,
                                                 const float* __restrict__ hb) {
   __shared__ double sh[(kT / 32) * 32];
   if (*s.nu == 0) return;
@@ -399,7 +415,7 @@ __global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ r
     for (int c = 0; c < KW; c++) ap[c] = 0.f;
     const int h = hidx ? __ldg(hidx + r) : -1;
     if (h >= 0) {
-      load_row<KW>(hb, h, ap);
+      heavy_row_sum<KW>(hch, hb, h, ap);
     } else {
       for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
         const int col = __ldg(ci + j);
@@ -545,6 +561,7 @@ __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__
                                                   const float* __restrict__ val,
                                                   const float* __restrict__ X, float* Y,
                                                   const int* __restrict__ hidx,
+                                                  const int* __restrict__ hch,
                                                   const float* __restrict__ hb) {
   const int r = blockIdx.x * kT + threadIdx.x;
   if (r >= n) return;
@@ -553,7 +570,7 @@ __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__
   for (int c = 0; c < KW; c++) acc[c] = 0.f;
   const int h = hidx ? __ldg(hidx + r) : -1;
   if (h >= 0) {
-    load_row<KW>(hb, h, acc);
+    heavy_row_sum<KW>(hch, hb, h, acc);
     store_row<KW>(Y, r, acc);
     return;
   }
@@ -601,7 +618,7 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
   int nl = 0;
   if (hv) heavy_rows_f32(*M, val, X, KW, nullptr, st);
   k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial, hidx,
-                                     hv ? M->hb32 : nullptr);
+                                     hv ? M->hch : nullptr, hv ? M->cb32 : nullptr);
   k_rows_init_ctrl<<<1, 1024, 0, st>>>(partial, nb, len, s);
   nl += 2;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
@@ -613,7 +630,7 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
       k_rows_p<KW><<<nb, kT, 0, st>>>(n, R, P, s, niter + j == 1 ? 1 : 0);
       if (hv) heavy_rows_f32(*M, val, P, KW, s.nu, st);
       k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial, hidx,
-                                       hv ? M->hb32 : nullptr);
+                                       hv ? M->hch : nullptr, hv ? M->cb32 : nullptr);
       k_rows_alpha<<<1, 1024, 0, st>>>(partial, nb, len, s);
       k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
       k_rows_step<<<1, 1024, 0, st>>>(partial, nb, len, s, rate, j);
@@ -655,16 +672,17 @@ void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const 
   const bool hv = M && M->nheavy > 0;
   if (hv) heavy_rows_f32(*M, val, X, bcg_rows_width(k), nullptr, st);
   const int* hidx = hv ? M->hidx : nullptr;
-  const float* hb = hv ? M->hb32 : nullptr;
+  const int* hch = hv ? M->hch : nullptr;
+  const float* hb = hv ? M->cb32 : nullptr;
   switch (bcg_rows_width(k)) {
-    case 4: k_rows_spmm<4><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 20: k_rows_spmm<20><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 24: k_rows_spmm<24><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 28: k_rows_spmm<28><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
-    case 32: k_rows_spmm<32><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hb); break;
+    case 4: k_rows_spmm<4><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 20: k_rows_spmm<20><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 24: k_rows_spmm<24><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 28: k_rows_spmm<28><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 32: k_rows_spmm<32><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
   }
 }
 

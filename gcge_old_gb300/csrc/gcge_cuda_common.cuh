@@ -30,7 +30,8 @@ struct GcgeDevCsr {
   // Rows of more than gcge::kHeavyRow entries ("heavy", e.g. the hubs of a
   // power-law graph), cut into chunks of up to gcge::kHeavyChunk entries that a
   // warp each multiplies before the thread-per-row kernels run; those kernels
-  // then read the heavy rows' products (hb64 / hb32) instead of walking them.
+  // then read the heavy rows' products (hb64, or the chunk sums of cb32)
+  // instead of walking them.
   int nheavy = 0, nchunk = 0;
   int* hidx = nullptr;     // per row: index among the heavy rows, or -1
   int* hch = nullptr;      // nheavy + 1: heavy row h owns chunks hch[h] .. hch[h+1]-1
@@ -38,8 +39,7 @@ struct GcgeDevCsr {
   int* che = nullptr;      // per chunk: one past the last entry
   double* hb64 = nullptr;  // nheavy x GCGE_MAXCOLS products (FP64 columns), [h * k + c]
   double* cb64 = nullptr;  // nchunk x kHeavyGroup chunk partials
-  float* hb32 = nullptr;   // nheavy x 32 products (FP32 row-interleaved), [h * KW + c]
-  float* cb32 = nullptr;   // nchunk x 32 chunk partials
+  float* cb32 = nullptr;   // nchunk x KW chunk partials (FP32 row-interleaved), [q * KW + c]
 };
 
 
@@ -61,8 +61,10 @@ int heavy_setup(GcgeDevCsr& M, const int* h_rp);
 void heavy_free(GcgeDevCsr& M);
 // M.hb64[h * k + c] = (M X_c)[heavy row h] for c < k.
 void heavy_cols_f64(const GcgeDevCsr& M, const ColList<double>& X, int k, cudaStream_t st);
-// M.hb32[h * KW + c] = (M X)[heavy row h][c] for the row-interleaved n x KW block
-// X with M's FP32 values val; skipped on the device when nu != null and *nu == 0.
+// M.cb32[q * KW + c] = chunk q's share of (M X)[its row][c] for the row-interleaved
+// n x KW block X with M's FP32 values val (a heavy row's product is the sum of
+// its chunks hch[h] .. hch[h+1]-1, in that order); skipped on the device when
+// nu != null and *nu == 0.
 void heavy_rows_f32(const GcgeDevCsr& M, const float* val, const float* X, int KW, const int* nu,
                     cudaStream_t st);
 

@@ -4,9 +4,10 @@
 // stalls its whole launch.  Rows of more than kHeavyRow entries are therefore
 // cut at matrix creation into chunks of up to kHeavyChunk entries; before a
 // row kernel runs, one warp per chunk multiplies its chunk (lanes stride the
-// entries, then a fixed xor-shuffle tree), a second pass adds the chunks of each
-// heavy row in chunk order, and the row kernel takes those rows' products from
-// the result instead of walking them.  Every sum has a fixed order, so the
+// entries, then a fixed xor-shuffle tree); the chunks of each heavy row are
+// then added in chunk order (by a second pass for FP64 columns, by the row
+// kernel itself for the FP32 row-interleaved blocks), and the row kernel takes
+// those rows' products instead of walking them.  Every sum has a fixed order, so the
 // products are deterministic.
 #include <vector>
 
@@ -85,21 +86,8 @@ __global__ void k_heavy_rows(int nchunk, const int* __restrict__ chb, const int*
     for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
   if (lane == 0) {
 #pragma unroll
-    for (int c = 0; c < KW; c++) cb[(size_t)warp * 32 + c] = acc[c];
+    for (int c = 0; c < KW; c++) cb[(size_t)warp * KW + c] = acc[c];
   }
-}
-
-template <int KW>
-__global__ void k_heavy_sum_rows(int nheavy, const int* __restrict__ hch,
-                                 const float* __restrict__ cb, float* __restrict__ hb,
-                                 const int* __restrict__ nu) {
-  if (nu && *nu == 0) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nheavy * KW) return;
-  const int h = t / KW, c = t % KW;
-  float s = 0.f;
-  for (int q = __ldg(hch + h); q < __ldg(hch + h + 1); q++) s += cb[(size_t)q * 32 + c];
-  hb[(size_t)h * KW + c] = s;
 }
 
 template <int KW>
@@ -108,8 +96,6 @@ void heavy_rows_kw(const GcgeDevCsr& M, const float* val, const float* X, const 
   const int threads = 32 * kWarpsPerBlock;
   k_heavy_rows<KW><<<(M.nchunk + kWarpsPerBlock - 1) / kWarpsPerBlock, threads, 0, st>>>(
       M.nchunk, M.chb, M.che, M.ci, val, X, M.cb32, nu);
-  k_heavy_sum_rows<KW><<<(M.nheavy * KW + 255) / 256, 256, 0, st>>>(M.nheavy, M.hch, M.cb32,
-                                                                    M.hb32, nu);
 }
 
 }  // namespace
@@ -140,7 +126,6 @@ int heavy_setup(GcgeDevCsr& M, const int* h_rp) {
   alloc((void**)&M.che, sizeof(int) * nchunk);
   alloc((void**)&M.hb64, sizeof(double) * nheavy * (size_t)GCGE_MAXCOLS);
   alloc((void**)&M.cb64, sizeof(double) * nchunk * (size_t)kHeavyGroup);
-  alloc((void**)&M.hb32, sizeof(float) * nheavy * (size_t)32);
   alloc((void**)&M.cb32, sizeof(float) * nchunk * (size_t)32);
   if (err == cudaSuccess)
     err = cudaMemcpy(M.hidx, hidx.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
@@ -166,11 +151,10 @@ void heavy_free(GcgeDevCsr& M) {
   cudaFree(M.che);
   cudaFree(M.hb64);
   cudaFree(M.cb64);
-  cudaFree(M.hb32);
   cudaFree(M.cb32);
   M.hidx = M.hch = M.chb = M.che = nullptr;
   M.hb64 = M.cb64 = nullptr;
-  M.hb32 = M.cb32 = nullptr;
+  M.cb32 = nullptr;
   M.nheavy = M.nchunk = 0;
 }
 
