@@ -68,6 +68,7 @@ def main():
          keep_vecs=False)
 
     shifted()
+    more_structures()
 
 
 def shifted():
@@ -94,9 +95,23 @@ def shifted():
     save("ref_lap2dc_m32_nev10_sm", Lc, None, 10, x0, {**base, "-gcge_eval_type": "sm"})
 
 
+def more_structures():
+    """Small instances of the anisotropic (per-cell kappa, diagonal mass) and the
+    power-law graph (A = L + 1e-3 I, B = D, rows of very different lengths)
+    problem families."""
+    A, B, _, _ = M.aniso2d(24, seed=5)
+    save("ref_aniso2d_m24_nev10", A, B, 10, M.initial_block(A.n, 10, seed=6),
+         {"-gcge_ev_tol": 1e-11, "-gcge_ev_max_it": 150})
+    A, B, _ = M.chung_lu(3000, seed=7)
+    save("ref_chunglu_n3000_nev10", A, B, 10, M.initial_block(A.n, 10, seed=8),
+         {"-gcge_ev_tol": 1e-10, "-gcge_ev_max_it": 300})
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["shifted"]:
         shifted()
+    elif sys.argv[1:] == ["structures"]:
+        more_structures()
     else:
         main()
 
