@@ -71,8 +71,9 @@ __device__ inline double block_sum1024(double v, double* sh) {
 //         entry is positive;
 // mode 1: all nrows eigenvectors, unsorted, to evec (lde) (a preconditioning
 //         basis for the FP64 pass).
-// work: global scratch of 2*mp*mp T when the matrix does not fit in shared
-// memory.  status[0] = sweeps used (or -1 if not converged).
+// work: global scratch of 2*mp*mp T.  use_smem 1: M and Q in shared memory;
+// 2: M in shared memory, Q in work; 0: both in work.  status[0] = sweeps used
+// (or -1 if not converged).
 template <typename T>
 __global__ void __launch_bounds__(1024, 1)
     k_jacobi(int nrows, const double* __restrict__ a, int lda, double* __restrict__ eval,
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(1024, 1)
   const int m = nrows;
   const int mp = (m % 2) ? m + 1 : m;  // padded player count
   T* M = use_smem ? reinterpret_cast<T*>(dyn_raw) : work;
-  T* Q = M + (size_t)mp * mp;
+  T* Q = use_smem == 2 ? work : M + (size_t)mp * mp;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < mp * mp; e += nt) {
     const int i = e % mp, j = e / mp;
@@ -605,12 +606,16 @@ static void launch_jacobi(int nrows, const double* a, int lda, double* eval, dou
                           int max_sweeps, cudaStream_t st, const unsigned char* mask = nullptr,
                           const double* norm_ptr = nullptr) {
   const int mp = (nrows % 2) ? nrows + 1 : nrows;
-  const size_t sm = sizeof(T) * 2 * (size_t)mp * mp;
-  const int use_smem = sm <= 200 * 1024 ? 1 : 0;
+  // the rotated matrix in shared memory whenever it fits (its rows and columns
+  // are read every round), the eigenvector accumulator too if there is room
+  constexpr size_t kCap = 220 * 1024;  // dynamic shared memory left beside the static arrays
+  const size_t one = sizeof(T) * (size_t)mp * mp;
+  const int use_smem = 2 * one <= kCap ? 1 : (one <= kCap ? 2 : 0);
   if (use_smem) {
+    const size_t sm = use_smem == 1 ? 2 * one : one;
     cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_jacobi<T><<<1, 1024, sm, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, 1, status, mode,
-                                     tol, max_sweeps, mask, norm_ptr);
+    k_jacobi<T><<<1, 1024, sm, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, use_smem,
+                                     status, mode, tol, max_sweeps, mask, norm_ptr);
   } else {
     k_jacobi<T><<<1, 1024, 0, st>>>(nrows, a, lda, eval, evec, lde, il, iu, work, 0, status, mode,
                                     tol, max_sweeps, mask, norm_ptr);
