@@ -630,9 +630,9 @@ static void launch_jacobi(int nrows, const double* a, int lda, double* eval, dou
 //        = r_ij / 2                          otherwise (and on the diagonal),
 // after which X <- X + X E.  Frobenius norms stand in for 2-norms (larger
 // delta: safe); ||A|| is read from device memory.  Pairs within delta are
-// "clustered"; delta shrinks as the basis improves, so a later step keeps a
-// pair clustered only if it is still within the new delta (the mask only
-// loses pairs); the final FP64 stage rotates the pairs left.  One CTA.
+// "clustered": on the first step the mask records them and later steps keep
+// treating them as clustered; the final FP64 Jacobi rotates exactly those
+// pairs.  One CTA.
 __global__ void __launch_bounds__(1024) k_oa_step_dev(int m, const double* __restrict__ S,
                                                       const double* __restrict__ R,
                                                       const double* __restrict__ normA, int first,
@@ -687,11 +687,13 @@ __global__ void __launch_bounds__(1024) k_oa_step_dev(int m, const double* __res
     if (i == j) {
       v = 0.5 * R[e];
     } else {
-      // pairs within delta are clustered; delta shrinks with the basis error,
-      // and a pair once separated stays separated
-      bool clustered = !(fabs(lam[i] - lam[j]) > delta);  // NaN -> clustered
-      if (!first) clustered = clustered && mask[e] != 0;
-      mask[e] = clustered ? 1 : 0;
+      bool clustered;
+      if (first) {
+        clustered = !(fabs(lam[i] - lam[j]) > delta);  // NaN -> clustered
+        mask[e] = clustered ? 1 : 0;
+      } else {
+        clustered = mask[e] != 0;
+      }
       v = clustered ? 0.5 * R[e] : (S[e] + lam[j] * R[e]) / (lam[j] - lam[i]);
     }
     E[e] = v;
@@ -721,9 +723,7 @@ void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec,
   double* nrm = Z + mm;                                         // 8 doubles
   unsigned char* mask = reinterpret_cast<unsigned char*>(nrm + 8);  // m*m bytes
   void* jw = nrm + 8 + (mm + 7) / 8;                            // Jacobi scratch
-  // the FP32 basis only seeds the refinement, which doubles its digits each
-  // step: 1e-4 is enough for three steps to reach FP64 and takes fewer sweeps
-  launch_jacobi<float>(m, a, lda, eval, X, m, 1, m, (float*)jw, status, 1, 1e-4, 20, st);
+  launch_jacobi<float>(m, a, lda, eval, X, m, 1, m, (float*)jw, status, 1, 2e-7, 20, st);
   k_frob_sym<<<1, 1024, 0, st>>>(m, a, lda, nrm);
   double* normA_dev = nrm;
   for (int it = 0; it < 3; it++) {
