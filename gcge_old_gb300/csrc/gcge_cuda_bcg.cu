@@ -311,6 +311,47 @@ __device__ __forceinline__ void store_row(float* base, size_t r, const float* v)
   for (int q = 0; q < KW / 4; q++) p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
+// acc = (A X)[r] for the row-interleaved block X (acc zeroed here).  With
+// G > 1 the entries are taken in groups of G: first the group's column
+// indices and values, then its G row gathers, then the FMAs in entry order, so
+// G gathers are in flight per thread and the sums are the same as one entry
+// at a time.  G is chosen per kernel to stay inside its register budget.
+template <int KW, int G>
+__device__ __forceinline__ void row_gather(const int* __restrict__ rp, const int* __restrict__ ci,
+                                           const float* __restrict__ val,
+                                           const float* __restrict__ X, int r, float* acc) {
+#pragma unroll
+  for (int c = 0; c < KW; c++) acc[c] = 0.f;
+  const int e = __ldg(rp + r + 1);
+  int j = __ldg(rp + r);
+  if (G > 1) {
+    for (; j + G <= e; j += G) {
+      int col[G];
+      float a[G];
+#pragma unroll
+      for (int u = 0; u < G; u++) {
+        col[u] = __ldg(ci + j + u);
+        a[u] = __ldg(val + j + u);
+      }
+      float xv[G][KW];
+#pragma unroll
+      for (int u = 0; u < G; u++) load_row<KW>(X, col[u], xv[u]);
+#pragma unroll
+      for (int u = 0; u < G; u++)
+#pragma unroll
+        for (int c = 0; c < KW; c++) acc[c] = fmaf(a[u], xv[u][c], acc[c]);
+    }
+  }
+  for (; j < e; j++) {
+    const int col = __ldg(ci + j);
+    const float a = __ldg(val + j);
+    float xv[KW];
+    load_row<KW>(X, col, xv);
+#pragma unroll
+    for (int c = 0; c < KW; c++) acc[c] = fmaf(a, xv[c], acc[c]);
+  }
+}
+
 // v = the product of heavy row h: its chunk partials in chunk order
 template <int KW>
 __device__ __forceinline__ void heavy_row_sum(const int* __restrict__ hch,
@@ -566,22 +607,11 @@ __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__
   const int r = blockIdx.x * kT + threadIdx.x;
   if (r >= n) return;
   float acc[KW];
-#pragma unroll
-  for (int c = 0; c < KW; c++) acc[c] = 0.f;
   const int h = hidx ? __ldg(hidx + r) : -1;
-  if (h >= 0) {
+  if (h >= 0)
     heavy_row_sum<KW>(hch, hb, h, acc);
-    store_row<KW>(Y, r, acc);
-    return;
-  }
-  for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
-    const int col = __ldg(ci + j);
-    const float a = __ldg(val + j);
-    float xv[KW];
-    load_row<KW>(X, col, xv);
-#pragma unroll
-    for (int c = 0; c < KW; c++) acc[c] = fmaf(a, xv[c], acc[c]);
-  }
+  else
+    row_gather<KW, (KW <= 12 ? 4 : (KW <= 20 ? 2 : 1))>(rp, ci, val, X, r, acc);
   store_row<KW>(Y, r, acc);
 }
 
