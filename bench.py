@@ -10,7 +10,10 @@ all lambda > 1), seeded N(0,1) initial block.  A step is one complete solve.
 
 value: seconds per solve of the mixed-precision form (FP32 block CG, FP64
 everything else) with the matrices and the initial block resident in HBM,
-timed with CUDA events on the solver's stream; fp64_s: the all-FP64 form.
+timed with CUDA events on the solver's stream; fp64_s: the all-FP64 form
+(FP64 block CG; tall-skinny products FP64-accurate on the tensor cores in both
+forms); fp64_fma_products_s: one FP64 solve with those products on FP64 FMA
+units instead.
 e2e: the same solve through the C ABI with HOST buffers: matrix upload,
 initial block upload and eigenvector download inside the timed region.
 roofline: the SpMM of the mixed solve's block CG: FP32 CSR SpMM on
@@ -139,10 +142,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def time_solves(torch, S, L, dA, dB, nev, x0_dev, precision, warmup, steps):
+def time_solves(torch, S, L, dA, dB, nev, x0_dev, precision, warmup, steps, gemm="ozaki"):
     """Solves with device-resident inputs; returns (times_s, stats, eval, evec_dev)."""
     lib = L.load()
-    s = S.GCGESolver(dA, dB, nev, ev_tol=1e-10, ev_max_it=1000, precision=precision)
+    s = S.GCGESolver(dA, dB, nev, ev_tol=1e-10, ev_max_it=1000, precision=precision, gemm=gemm)
     evec_dev = torch.empty_like(x0_dev)
     L.check(lib.GCGE_CUDA_SOLVER_SetEigenvectorsDevice(s.handle, C.c_void_p(evec_dev.data_ptr())),
             "SetEigenvectorsDevice")
@@ -640,6 +643,11 @@ def main():
                                                          args.warmup, args.steps)
     t_fp64, st_fp64, ev_fp64, vec_fp64 = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64",
                                                      max(1, args.warmup // 3), max(1, args.steps // 2))
+    # the same FP64 solve with the tall-skinny products on FP64 FMA units instead of
+    # the FP64-accurate tensor-core products (one solve: what the tensor cores buy)
+    t_fma, st_fma, _, vec_fma = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64", 0, 1,
+                                            gemm="fp64")
+    del vec_fma
     torch.cuda.synchronize()
     clocks = sampler.stop()
     v_mixed = statistics.mean(t_mixed)
@@ -684,6 +692,7 @@ def main():
                    "nnz": A.nnz, "nev": nev, "block_size": 10, "parallelism": "replicas only",
                    "l2": "inputs larger than L2 (A 175 MB, basis 1.5 GB)"},
         "fp64_s": v_fp64, "mixed_s": v_mixed, "mixed_speedup_vs_fp64": v_fp64 / v_mixed,
+        "fp64_fma_products_s": t_fma[0],
         "gcg_iterations": {"mixed": st_mixed[-1]["num_iter"], "fp64": st_fp64[-1]["num_iter"]},
         "max_residual": {"mixed": float(res_m.max()), "fp64": float(res_d.max())},
         "eigenvalue_rel_diff_mixed_vs_fp64": ev_rel,
