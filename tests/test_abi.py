@@ -79,3 +79,26 @@ def test_solver_parameter_surface_without_gpu():
     assert lib.GCGE_CUDA_SOLVER_GetStream(s, C.byref(stream)) == 4
     assert lib.GCGE_CUDA_SOLVER_Free(C.byref(s)) == 0
     assert not s.value
+
+
+def test_new_entry_points_check_arguments_without_gpu():
+    """The W-step hook, the stock PCG, the eigenvector adjoint and the file
+    readers reject bad arguments before any device work."""
+    from gcge_old_gb300 import lib as L
+    lib = L.load(build_if_missing=True)
+    s = C.c_void_p()
+    assert lib.GCGE_CUDA_SOLVER_Create(C.byref(s)) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetMultiLinearSolver(s, C.cast(lib.GCGE_CUDA_JacobiPCG, C.c_void_p),
+                                                     None) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetMultiLinearSolver(s, None, None) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetMultiLinearSolver(None, None, None) == 1
+    assert lib.GCGE_CUDA_SOLVER_Free(C.byref(s)) == 0
+    assert lib.GCGE_CUDA_JacobiPCG(None, None, None, None, 1, 10, None) == 1
+    ev = np.array([1.0, 2.0])
+    assert lib.GCGE_CUDA_EigvecAdjointSolve(None, None, None, ev.ctypes.data_as(L.c_double_p), 2,
+                                            None, None, None, 10, 1e-8, None) == 1
+    a = np.ones(2)
+    assert lib.GCGE_CUDA_EigGradCSR2(None, None, None, a.ctypes.data_as(L.c_double_p), None, 2,
+                                     None) == 1
+    assert lib.GCGE_CUDA_MatGetSize(None, None, None) == 1
+    assert lib.GCGE_CUDA_MatCreateFromFile(None, b"x") == 1
