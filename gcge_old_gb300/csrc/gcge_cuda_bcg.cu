@@ -292,42 +292,23 @@ __device__ __forceinline__ void block_sum_cols(const float* acc, int len, double
   }
 }
 
-// One row of a row-interleaved block: KW floats (KW even) at base + r * KW,
-// moved as float4 when KW is a multiple of 4, as float2 otherwise.
 template <int KW>
 __device__ __forceinline__ void load_row(const float* __restrict__ base, size_t r, float* v) {
-  if constexpr (KW % 4 == 0) {
-    const float4* p = reinterpret_cast<const float4*>(base + r * KW);
+  const float4* p = reinterpret_cast<const float4*>(base + r * KW);
 #pragma unroll
-    for (int q = 0; q < KW / 4; q++) {
-      const float4 t = __ldg(p + q);
-      v[4 * q] = t.x;
-      v[4 * q + 1] = t.y;
-      v[4 * q + 2] = t.z;
-      v[4 * q + 3] = t.w;
-    }
-  } else {
-    const float2* p = reinterpret_cast<const float2*>(base + r * KW);
-#pragma unroll
-    for (int q = 0; q < KW / 2; q++) {
-      const float2 t = __ldg(p + q);
-      v[2 * q] = t.x;
-      v[2 * q + 1] = t.y;
-    }
+  for (int q = 0; q < KW / 4; q++) {
+    const float4 t = __ldg(p + q);
+    v[4 * q] = t.x;
+    v[4 * q + 1] = t.y;
+    v[4 * q + 2] = t.z;
+    v[4 * q + 3] = t.w;
   }
 }
 template <int KW>
 __device__ __forceinline__ void store_row(float* base, size_t r, const float* v) {
-  if constexpr (KW % 4 == 0) {
-    float4* p = reinterpret_cast<float4*>(base + r * KW);
+  float4* p = reinterpret_cast<float4*>(base + r * KW);
 #pragma unroll
-    for (int q = 0; q < KW / 4; q++)
-      p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-  } else {
-    float2* p = reinterpret_cast<float2*>(base + r * KW);
-#pragma unroll
-    for (int q = 0; q < KW / 2; q++) p[q] = make_float2(v[2 * q], v[2 * q + 1]);
-  }
+  for (int q = 0; q < KW / 4; q++) p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
 // acc = (A X)[r] for the row-interleaved block X (acc zeroed here).  With
@@ -702,10 +683,16 @@ int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, floa
                      float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
                      double* partial, cudaStream_t st, int* launches, const GcgeDevCsr* M) {
   if (len <= 0) return 0;
-#define GCGE_RR(W_) \
-  case W_: return rows_run<W_>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
-  switch (bcg_rows_width(len)) { GCGE_ROW_WIDTHS(GCGE_RR) }
-#undef GCGE_RR
+  switch (bcg_rows_width(len)) {
+    case 4: return rows_run<4>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 8: return rows_run<8>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 12: return rows_run<12>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 16: return rows_run<16>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 20: return rows_run<20>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 24: return rows_run<24>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 28: return rows_run<28>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+    case 32: return rows_run<32>(rp, ci, val, n, R, X, P, W, len, max_it, rate, s, partial, st, launches, M);
+  }
   return -1;
 }
 
@@ -717,27 +704,45 @@ void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const 
   const int* hidx = hv ? M->hidx : nullptr;
   const int* hch = hv ? M->hch : nullptr;
   const float* hb = hv ? M->cb32 : nullptr;
-#define GCGE_RS(W_) \
-  case W_: k_rows_spmm<W_><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
-  switch (bcg_rows_width(k)) { GCGE_ROW_WIDTHS(GCGE_RS) }
-#undef GCGE_RS
+  switch (bcg_rows_width(k)) {
+    case 4: k_rows_spmm<4><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 8: k_rows_spmm<8><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 12: k_rows_spmm<12><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 16: k_rows_spmm<16><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 20: k_rows_spmm<20><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 24: k_rows_spmm<24><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 28: k_rows_spmm<28><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+    case 32: k_rows_spmm<32><<<g, kT, 0, st>>>(n, rp, ci, val, X, Y, hidx, hch, hb); break;
+  }
 }
 
 void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st) {
   const int g = (n + 255) / 256;
-#define GCGE_CR(W_) \
-  case W_: k_cols_to_rows<W_><<<g, 256, 0, st>>>(R, len, Rr, n); break;
-  switch (bcg_rows_width(len)) { GCGE_ROW_WIDTHS(GCGE_CR) }
-#undef GCGE_CR
+  switch (bcg_rows_width(len)) {
+    case 4: k_cols_to_rows<4><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 8: k_cols_to_rows<8><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 12: k_cols_to_rows<12><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 16: k_cols_to_rows<16><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 20: k_cols_to_rows<20><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 24: k_cols_to_rows<24><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 28: k_cols_to_rows<28><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+    case 32: k_cols_to_rows<32><<<g, 256, 0, st>>>(R, len, Rr, n); break;
+  }
 }
 
 void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
                           cudaStream_t st) {
   const int g = (n + 255) / 256;
-#define GCGE_RA(W_) \
-  case W_: k_rows_add<W_><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-  switch (bcg_rows_width(len)) { GCGE_ROW_WIDTHS(GCGE_RA) }
-#undef GCGE_RA
+  switch (bcg_rows_width(len)) {
+    case 4: k_rows_add<4><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 8: k_rows_add<8><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 12: k_rows_add<12><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 16: k_rows_add<16><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 20: k_rows_add<20><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 24: k_rows_add<24><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 28: k_rows_add<28><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 32: k_rows_add<32><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+  }
 }
 
 }  // namespace gcge

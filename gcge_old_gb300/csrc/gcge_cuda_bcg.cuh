@@ -31,7 +31,7 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
 
 // The same FP32 block CG with the four vectors stored row-interleaved: R, X,
 // P, W are n x KW float arrays (element (r, c) at r*KW + c, KW = len rounded
-// up to even, rows 8-byte aligned) for len <= 32, so the SpMM
+// up to a multiple of 4, rows 16-byte aligned) for len <= 16, so the SpMM
 // gathers one contiguous KW-float row per nonzero and every vector kernel
 // streams whole rows.  Same steps, scalars and reductions (same order) as
 // bcg_run<float>; s.acol and s.mask must be set.  Returns niter or -1.
@@ -41,10 +41,7 @@ int bcg_run_rows_f32(const int* rp, const int* ci, const float* val, int n, floa
                      float* P, float* W, int len, int max_it, double rate, const BcgScalars& s,
                      double* partial, cudaStream_t st, int* launches,
                      const GcgeDevCsr* M = nullptr);
-inline int bcg_rows_width(int len) { return (len + 1) / 2 * 2; }
-// the row widths instantiated (every even width up to 32)
-#define GCGE_ROW_WIDTHS(X) \
-  X(2) X(4) X(6) X(8) X(10) X(12) X(14) X(16) X(18) X(20) X(22) X(24) X(26) X(28) X(30) X(32)
+inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
 // Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 32).
 void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
                    float* Y, int k, cudaStream_t st, const GcgeDevCsr* M = nullptr);

@@ -71,24 +71,14 @@ __global__ void k_heavy_rows(int nchunk, const int* __restrict__ chb, const int*
   for (int j = __ldg(chb + warp) + lane; j < e; j += 32) {
     const int col = __ldg(ci + j);
     const float a = __ldg(v + j);
-    if constexpr (KW % 4 == 0) {
-      const float4* p = reinterpret_cast<const float4*>(X + (size_t)col * KW);
+    const float4* p = reinterpret_cast<const float4*>(X + (size_t)col * KW);
 #pragma unroll
-      for (int q = 0; q < KW / 4; q++) {
-        const float4 t = __ldg(p + q);
-        acc[4 * q] = fmaf(a, t.x, acc[4 * q]);
-        acc[4 * q + 1] = fmaf(a, t.y, acc[4 * q + 1]);
-        acc[4 * q + 2] = fmaf(a, t.z, acc[4 * q + 2]);
-        acc[4 * q + 3] = fmaf(a, t.w, acc[4 * q + 3]);
-      }
-    } else {
-      const float2* p = reinterpret_cast<const float2*>(X + (size_t)col * KW);
-#pragma unroll
-      for (int q = 0; q < KW / 2; q++) {
-        const float2 t = __ldg(p + q);
-        acc[2 * q] = fmaf(a, t.x, acc[2 * q]);
-        acc[2 * q + 1] = fmaf(a, t.y, acc[2 * q + 1]);
-      }
+    for (int q = 0; q < KW / 4; q++) {
+      const float4 t = __ldg(p + q);
+      acc[4 * q] = fmaf(a, t.x, acc[4 * q]);
+      acc[4 * q + 1] = fmaf(a, t.y, acc[4 * q + 1]);
+      acc[4 * q + 2] = fmaf(a, t.z, acc[4 * q + 2]);
+      acc[4 * q + 3] = fmaf(a, t.w, acc[4 * q + 3]);
     }
   }
 #pragma unroll
@@ -185,21 +175,13 @@ void heavy_rows_f32(const GcgeDevCsr& M, const float* val, const float* X, int K
                     cudaStream_t st) {
   if (M.nheavy == 0) return;
   switch (KW) {
-    case 2: heavy_rows_kw<2>(M, val, X, nu, st); break;
     case 4: heavy_rows_kw<4>(M, val, X, nu, st); break;
-    case 6: heavy_rows_kw<6>(M, val, X, nu, st); break;
     case 8: heavy_rows_kw<8>(M, val, X, nu, st); break;
-    case 10: heavy_rows_kw<10>(M, val, X, nu, st); break;
     case 12: heavy_rows_kw<12>(M, val, X, nu, st); break;
-    case 14: heavy_rows_kw<14>(M, val, X, nu, st); break;
     case 16: heavy_rows_kw<16>(M, val, X, nu, st); break;
-    case 18: heavy_rows_kw<18>(M, val, X, nu, st); break;
     case 20: heavy_rows_kw<20>(M, val, X, nu, st); break;
-    case 22: heavy_rows_kw<22>(M, val, X, nu, st); break;
     case 24: heavy_rows_kw<24>(M, val, X, nu, st); break;
-    case 26: heavy_rows_kw<26>(M, val, X, nu, st); break;
     case 28: heavy_rows_kw<28>(M, val, X, nu, st); break;
-    case 30: heavy_rows_kw<30>(M, val, X, nu, st); break;
     case 32: heavy_rows_kw<32>(M, val, X, nu, st); break;
   }
 }

@@ -274,10 +274,8 @@ extern "C" int GCGE_CUDA_JacobiPCG(void* ctx, const GCGE_CUDA_MAT* A, double* co
 
 extern "C" int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k,
                                             void* stream) {
-  if (!A || !x || !y || k <= 0 || k > 32) return GCGE_CUDA_ERR_ARG;
-  // rows move as float4 when the width is a multiple of 4, as float2 otherwise
-  const uintptr_t am = gcge::bcg_rows_width(k) % 4 == 0 ? 15 : 7;
-  if (((uintptr_t)x & am) || ((uintptr_t)y & am)) return GCGE_CUDA_ERR_ARG;
+  if (!A || !x || !y || k <= 0 || k > 32 || ((uintptr_t)x & 15) || ((uintptr_t)y & 15))
+    return GCGE_CUDA_ERR_ARG;
   if (!A->m.v32) {
     if (cudaMalloc(&A->m.v32, sizeof(float) * (A->m.nnz > 0 ? A->m.nnz : 1)) != cudaSuccess)
       return GCGE_CUDA_ERR_ALLOC;

@@ -44,7 +44,7 @@ def spmm_only(A, k):
     for _ in range(5):
         L.check(lib.GCGE_CUDA_MatDotMultiVecF32Async(dA.handle, xp32, yp32, k, None), "spmm32")
     if k <= 16:  # the block CG's row-interleaved FP32 operator
-        kw = (k + 1) // 2 * 2
+        kw = (k + 3) // 4 * 4
         XR = torch.randn(A.n, kw, dtype=torch.float32, device="cuda")
         YR = torch.empty(A.n, kw, dtype=torch.float32, device="cuda")
         for _ in range(5):

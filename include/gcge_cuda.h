@@ -202,8 +202,8 @@ int GCGE_CUDA_MatDotMultiVecAsync(const GCGE_CUDA_MAT* A, double* const* x, doub
 int GCGE_CUDA_MatDotMultiVecF32Async(GCGE_CUDA_MAT* A, float* const* x, float* const* y, int k,
                                      void* stream);
 /* FP32 y = A x on row-interleaved blocks: x and y are device arrays of
- * n x w floats, w = k rounded up to even (element (r, c) at r*w + c; 8-byte
- * aligned, 16-byte when w is a multiple of 4), k <= 32.  The operator of the mixed-precision block CG
+ * n x round_up(k, 4) floats (element (r, c) at r*round_up(k,4) + c, 16-byte
+ * aligned), k <= 32.  The operator of the mixed-precision block CG
  * (GCGE_BCG, src/gcge_cg.c:429-445, on FP32 copies), whose gathers read one
  * contiguous row per nonzero; asynchronous on the given cudaStream_t. */
 int GCGE_CUDA_MatDotRowsF32Async(GCGE_CUDA_MAT* A, const float* x, float* y, int k, void* stream);

@@ -38,7 +38,7 @@ def test_rows_spmm_matches_column_spmm(cuda_lib, k):
     column by column (FP32 sums of the same products in the same order)."""
     import torch
     A = M.laplace3d_mass(14, seed=1)[0]
-    kw = (k + 1) // 2 * 2
+    kw = (k + 3) // 4 * 4
     rng = np.random.default_rng(k)
     X = rng.standard_normal((A.n, kw)).astype(np.float32)
     X[:, k:] = 0.0

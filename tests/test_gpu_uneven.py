@@ -43,7 +43,7 @@ def test_spmm_rows_f32_heavy_rows(cuda_lib, graph, k):
     import torch
     from gcge_old_gb300.solver import DeviceMatrix
     A = graph[0]
-    kw = (k + 1) // 2 * 2
+    kw = (k + 3) // 4 * 4
     rng = np.random.default_rng(k)
     Xc = rng.standard_normal((A.n, k)).astype(np.float32)
     Xr = np.zeros((A.n, kw), np.float32)
