@@ -595,12 +595,7 @@ __global__ void k_rows_step(const double* __restrict__ partial, int nblk, int le
   s.nu_host[slot] = m;
 }
 
-// y = A x on row-interleaved blocks (the operator of the mixed block CG).  A
-// block first copies the column indices and values of its 256 rows into
-// shared memory with coalesced loads (when they fit, kStage entries), so each
-// thread's gathers depend on one shared-memory read instead of a strided global
-// one; blocks whose rows hold more entries read them from global memory.
-constexpr int kStage = 2048;
+// y = A x on row-interleaved blocks (the operator of the mixed block CG)
 template <int KW>
 __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__ rp,
                                                   const int* __restrict__ ci,
@@ -609,56 +604,14 @@ __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__
                                                   const int* __restrict__ hidx,
                                                   const int* __restrict__ hch,
                                                   const float* __restrict__ hb) {
-  constexpr int G = KW <= 12 ? 4 : (KW <= 20 ? 2 : 1);
-  __shared__ int s_ci[kStage];
-  __shared__ float s_v[kStage];
-  const int r0 = blockIdx.x * kT;
-  const int r = r0 + threadIdx.x;
-  const int b0 = __ldg(rp + r0), b1 = __ldg(rp + min(r0 + kT, n));
-  const bool staged = b1 - b0 <= kStage;  // the same for the whole block
-  if (staged) {
-    for (int e = threadIdx.x; e < b1 - b0; e += kT) {
-      s_ci[e] = __ldg(ci + b0 + e);
-      s_v[e] = __ldg(val + b0 + e);
-    }
-    __syncthreads();
-  }
+  const int r = blockIdx.x * kT + threadIdx.x;
   if (r >= n) return;
   float acc[KW];
   const int h = hidx ? __ldg(hidx + r) : -1;
-  if (h >= 0) {
+  if (h >= 0)
     heavy_row_sum<KW>(hch, hb, h, acc);
-  } else if (staged) {
-#pragma unroll
-    for (int c = 0; c < KW; c++) acc[c] = 0.f;
-    const int e = __ldg(rp + r + 1) - b0;
-    int j = __ldg(rp + r) - b0;
-    for (; j + G <= e; j += G) {
-      int col[G];
-      float a[G];
-#pragma unroll
-      for (int u = 0; u < G; u++) {
-        col[u] = s_ci[j + u];
-        a[u] = s_v[j + u];
-      }
-      float xv[G][KW];
-#pragma unroll
-      for (int u = 0; u < G; u++) load_row<KW>(X, col[u], xv[u]);
-#pragma unroll
-      for (int u = 0; u < G; u++)
-#pragma unroll
-        for (int c = 0; c < KW; c++) acc[c] = fmaf(a[u], xv[u][c], acc[c]);
-    }
-    for (; j < e; j++) {
-      float xv[KW];
-      load_row<KW>(X, s_ci[j], xv);
-      const float a = s_v[j];
-#pragma unroll
-      for (int c = 0; c < KW; c++) acc[c] = fmaf(a, xv[c], acc[c]);
-    }
-  } else {
-    row_gather<KW, G>(rp, ci, val, X, r, acc);
-  }
+  else
+    row_gather<KW, (KW <= 12 ? 4 : (KW <= 20 ? 2 : 1))>(rp, ci, val, X, r, acc);
   store_row<KW>(Y, r, acc);
 }
 
