@@ -597,7 +597,8 @@ __global__ void k_rows_step(const double* __restrict__ partial, int nblk, int le
 
 // y = A x on row-interleaved blocks (the operator of the mixed block CG)
 template <int KW>
-__global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__ rp,
+__global__ void __launch_bounds__(kT, KW <= 12 ? 6 : (KW <= 16 ? 4 : 2))
+    k_rows_spmm(int n, const int* __restrict__ rp,
                                                   const int* __restrict__ ci,
                                                   const float* __restrict__ val,
                                                   const float* __restrict__ X, float* Y,
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(kT) k_rows_spmm(int n, const int* __restrict__
   if (h >= 0)
     heavy_row_sum<KW>(hch, hb, h, acc);
   else
-    row_gather<KW, (KW <= 12 ? 4 : (KW <= 20 ? 2 : 1))>(rp, ci, val, X, r, acc);
+    row_gather<KW, 1>(rp, ci, val, X, r, acc);
   store_row<KW>(Y, r, acc);
 }
 
