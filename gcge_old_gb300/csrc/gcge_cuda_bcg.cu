@@ -18,6 +18,8 @@ namespace gcge {
 namespace {
 
 constexpr int kT = 256;
+// 256-thread blocks of the fused A p kernel resident per SM at block widths <= 12
+constexpr int kApBlocks12 = 5;
 constexpr int kBatch = 4;  // steps launched per host synchronisation
 
 __device__ inline double block_sum(double v, double* sh) {
@@ -434,7 +436,7 @@ __global__ void __launch_bounds__(kT) k_rows_p(int n, const float* __restrict__ 
 
 // w = A p and partial p.w for the active columns
 template <int KW>
-__global__ void __launch_bounds__(kT) k_rows_ap(int n, const int* __restrict__ rp,
+__global__ void __launch_bounds__(kT, KW <= 12 ? kApBlocks12 : 1) k_rows_ap(int n, const int* __restrict__ rp,
                                                 const int* __restrict__ ci,
                                                 const float* __restrict__ val,
                                                 const float* __restrict__ P, float* W, int len,
@@ -644,8 +646,10 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
   const bool hv = M && M->nheavy > 0;
   const int* hidx = hv ? M->hidx : nullptr;
   // four CTAs of 8 warps per SM for the row-streaming kernels (two from 20
-  // columns up, where the update kernel holds over 100 registers a thread)
+  // columns up, where the update kernel holds over 100 registers a thread);
+  // the latency-bound A p kernel gets kApBlocks12 up to 12 columns
   const int nb = min((n + kT - 1) / kT, (KW <= 16 ? 4 : 2) * 152);
+  const int nba = KW <= 12 ? min((n + kT - 1) / kT, kApBlocks12 * 152) : nb;
   int nl = 0;
   if (hv) heavy_rows_f32(*M, val, X, KW, nullptr, st);
   k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial, hidx,
@@ -660,9 +664,9 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
     for (int j = 0; j < batch; j++) {
       k_rows_p<KW><<<nb, kT, 0, st>>>(n, R, P, s, niter + j == 1 ? 1 : 0);
       if (hv) heavy_rows_f32(*M, val, P, KW, s.nu, st);
-      k_rows_ap<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial, hidx,
-                                       hv ? M->hch : nullptr, hv ? M->cb32 : nullptr);
-      k_rows_alpha<<<1, 1024, 0, st>>>(partial, nb, len, s);
+      k_rows_ap<KW><<<nba, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial, hidx,
+                                        hv ? M->hch : nullptr, hv ? M->cb32 : nullptr);
+      k_rows_alpha<<<1, 1024, 0, st>>>(partial, nba, len, s);
       k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
       k_rows_step<<<1, 1024, 0, st>>>(partial, nb, len, s, rate, j);
       nl += 5;
