@@ -19,7 +19,8 @@ namespace {
 
 constexpr int kT = 256;
 // 256-thread blocks of the fused A p kernel resident per SM at block widths <= 12
-constexpr int kApBlocks12 = 5;
+// (five measured no faster: the kernel then spills)
+constexpr int kApBlocks12 = 4;
 constexpr int kBatch = 4;  // steps launched per host synchronisation
 
 __device__ inline double block_sum(double v, double* sh) {
