@@ -103,22 +103,15 @@ __device__ __forceinline__ uint32_t d8_pack(float lo, float hi) {
 // The 7 digits of x / 2^E (|x| < 2^E) as exact FP32 values, most significant
 // first.  Zero, subnormal and non-finite x give zero digits.
 __device__ __forceinline__ void d8_digits(double x, int E, float* f) {
-  const int ex = (__double2hiint(x) >> 20) & 0x7FF;
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
   long long m = 0;
   if (ex != 0 && ex != 0x7FF) {
-    if (E > -969) {
-      // trunc(x 2^(55-E)): the scaling by a power of two is exact and the
-      // conversion truncates toward zero, as the shift of the mantissa below
-      m = __double2ll_rz(x * __hiloint2double((1078 - E) << 20, 0));
-    } else {
-      const long long b = __double_as_longlong(x);
-      const unsigned long long mant =
-          ((unsigned long long)b & ((1ull << 52) - 1)) | (1ull << 52);
-      const int sh = ex - 1020 - E;  // <= 2 because |x| < 2^E
-      const unsigned long long mm =
-          sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
-      m = b < 0 ? -(long long)mm : (long long)mm;
-    }
+    const unsigned long long mant = ((unsigned long long)b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1020 - E;  // <= 2 because |x| < 2^E
+    const unsigned long long mm =
+        sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
+    m = b < 0 ? -(long long)mm : (long long)mm;
   }
   const long long u = m + 0x808080808080ll;  // bytes 0..5 of u are the low digits + 128
   const int hi = (int)(u >> 32);
