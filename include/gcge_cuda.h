@@ -64,7 +64,10 @@ const char* GCGE_CUDA_GetLastErrorMessage(void);
  * the reference's equivalents are CSR_ReadMatFile + the CSR_MAT struct). */
 int GCGE_CUDA_MatCreateFromCSR(GCGE_CUDA_MAT** mat, const GCGE_CUDA_CSR_HOST* csr);
 /* rowptr/col/val are host arrays when on_device == 0, device arrays otherwise
- * (then they are copied too, the caller keeps ownership). */
+ * (then they are copied too, the caller keeps ownership).  Rows of more than 64
+ * entries are cut into chunks here that products multiply warp by warp into
+ * scratch owned by the matrix: products with such a matrix must not run
+ * concurrently on different streams. */
 int GCGE_CUDA_MatCreate(GCGE_CUDA_MAT** mat, int n, const int* rowptr, const int* col,
                         const double* val, int on_device);
 int GCGE_CUDA_MatDestroy(GCGE_CUDA_MAT** mat);
