@@ -103,17 +103,16 @@ __device__ __forceinline__ uint32_t d8_pack(float lo, float hi) {
 // The 7 digits of x / 2^E (|x| < 2^E) as exact FP32 values, most significant
 // first.  Zero, subnormal and non-finite x give zero digits.
 __device__ __forceinline__ void d8_digits(double x, int E, float* f) {
-  // straight-line (no divergent branch within a warp): both shifts are formed
-  // and selected; a right shift by 63 already clears the 53-bit mantissa
   const long long b = __double_as_longlong(x);
   const int ex = (int)((b >> 52) & 0x7FF);
-  const unsigned long long mant = ((unsigned long long)b & ((1ull << 52) - 1)) | (1ull << 52);
-  const int sh = ex - 1020 - E;  // <= 2 because |x| < 2^E
-  const unsigned long long lft = mant << (sh > 0 ? sh : 0);
-  const unsigned long long rgt = mant >> (sh < 0 ? (sh > -63 ? -sh : 63) : 0);
-  const unsigned long long mm = sh >= 0 ? lft : rgt;
-  const long long sm = b < 0 ? -(long long)mm : (long long)mm;
-  const long long m = (ex != 0 && ex != 0x7FF) ? sm : 0ll;
+  long long m = 0;
+  if (ex != 0 && ex != 0x7FF) {
+    const unsigned long long mant = ((unsigned long long)b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1020 - E;  // <= 2 because |x| < 2^E
+    const unsigned long long mm =
+        sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
+    m = b < 0 ? -(long long)mm : (long long)mm;
+  }
   const long long u = m + 0x808080808080ll;  // bytes 0..5 of u are the low digits + 128
   const int hi = (int)(u >> 32);
   const unsigned lo = (unsigned)u;
