@@ -13,9 +13,9 @@ everything else) with the matrices and the initial block resident in HBM,
 timed with CUDA events on the solver's stream; fp64_s: the all-FP64 form
 (FP64 block CG; tall-skinny products FP64-accurate on the tensor cores in both
 forms); fp64_fma_products_s: one FP64 solve with those products on FP64 FMA
-units instead; tuned_inner_solve: one solve of each form with the block-CG step
-cap that suits it (mixed 40, FP64 30; the reference's default, used for
-value, is 20).
+units instead; tuned_inner_solve: one solve of each form with the block size
+and block-CG step cap that suit it (mixed 12 / 40, FP64 15 / 40; the
+reference's defaults 10 / 20 are what value uses).
 e2e: the same solve through the C ABI with HOST buffers: matrix upload,
 initial block upload and eigenvector download inside the timed region.
 roofline: the SpMM of the mixed solve's block CG: FP32 CSR SpMM on
@@ -651,13 +651,15 @@ def main():
     t_fma, st_fma, _, vec_fma = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64", 0, 1,
                                             gemm="fp64")
     del vec_fma
-    # each form with the inner block-CG step cap that suits it (the reference's
-    # default is 20): cheap FP32 steps buy fewer outer iterations
+    # each form with the block size and inner block-CG step cap that suit it
+    # (found by a sweep; the reference's defaults are 10 and 20): more inner
+    # steps buy fewer outer iterations, and the FP32 ones are cheap
     tuned = {}
-    for prec, cap in (("mixed", 40), ("fp64", 30)):
-        tt, stt, _, vt = time_solves(torch, S, L, dA, dB, nev, x0_dev, prec, 0, 1, cg_max_it=cap)
-        tuned[prec] = {"s": tt[0], "cg_max_it": cap, "gcg_iterations": stt[0]["num_iter"],
-                       "bcg_steps": stt[0]["bcg_steps"]}
+    for prec, bs, cap in (("mixed", 12, 40), ("fp64", 15, 40)):
+        tt, stt, _, vt = time_solves(torch, S, L, dA, dB, nev, x0_dev, prec, 0, 1, cg_max_it=cap,
+                                     block_size=bs)
+        tuned[prec] = {"s": tt[0], "block_size": bs, "cg_max_it": cap,
+                       "gcg_iterations": stt[0]["num_iter"], "bcg_steps": stt[0]["bcg_steps"]}
         del vt
     torch.cuda.synchronize()
     clocks = sampler.stop()
