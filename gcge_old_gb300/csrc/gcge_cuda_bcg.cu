@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kT) k_rows_p(int n, const float* __restrict__ 
 #pragma unroll
   for (int c = 0; c < KW; c++) {
     on[c] = s.mask[c] != 0;
-    beta[c] = (on[c] && !first) ? (float)(s.rho2[c] / s.rho1[c]) : 0.f;
+    beta[c] = (on[c] && !first) ? s.bcol[c] : 0.f;
   }
   for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
     float rv[KW], pv[KW];
@@ -594,6 +594,9 @@ __global__ void k_rows_step(const double* __restrict__ partial, int nblk, int le
       s.mask[idx] = 1;
     }
   }
+  // beta of the next p step, once here instead of in every thread of k_rows_p;
+  // indexed by column as the reference indexes it (rho arrays by active id)
+  for (int c = 0; c < 32; c++) s.bcol[c] = s.mask[c] ? (float)(s.rho2[c] / s.rho1[c]) : 0.f;
   *s.nu = m;
   s.nu_host[slot] = m;
 }

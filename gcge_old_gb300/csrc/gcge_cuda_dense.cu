@@ -738,8 +738,17 @@ void jacobi_eig(int nrows, const double* a, int lda, double* eval, double* evec,
   }
   dgemm_small(false, false, true, m, m, m, 1.0, a, lda, X, m, 0.0, AX, m, st);
   dgemm_small(true, false, false, m, m, m, 1.0, X, m, AX, m, 0.0, S, m, st);
-  k_cluster_jacobi<<<1, 1024, 0, st>>>(m, S, mask, normA_dev, eval, Z, m, il, iu, (double*)jw,
-                                       status, 1e-15, 60);
+  // the masked round-robin Jacobi while the matrix and the rotations fit in
+  // shared memory (large clusters parallelise over the whole CTA there); the
+  // cluster-wise kernel beyond, where round-robin sweeps would run from global
+  // memory
+  const int mp = (m % 2) ? m + 1 : m;
+  if (sizeof(double) * 2 * (size_t)mp * mp <= 220 * 1024)
+    launch_jacobi<double>(m, S, m, eval, Z, m, il, iu, (double*)jw, status, 0, 1e-15, 60, st,
+                          mask, normA_dev);
+  else
+    k_cluster_jacobi<<<1, 1024, 0, st>>>(m, S, mask, normA_dev, eval, Z, m, il, iu, (double*)jw,
+                                         status, 1e-15, 60);
   const int nout = iu - il + 1;
   dgemm_small(false, false, false, m, nout, m, 1.0, X, m, Z, m, 0.0, evec, lde, st);
 }

@@ -657,8 +657,8 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   if (s->partial_len < colpart) s->partial_len = colpart;
   CU(cudaMalloc(&s->partial, sizeof(double) * s->partial_len));
   // block-CG scalars
-  CU(cudaMalloc(&s->bcg_mem, sizeof(double) * 7 * GCGE_MAXCOLS));
-  CU(cudaMemsetAsync(s->bcg_mem, 0, sizeof(double) * 7 * GCGE_MAXCOLS, s->st));
+  CU(cudaMalloc(&s->bcg_mem, sizeof(double) * 8 * GCGE_MAXCOLS));
+  CU(cudaMemsetAsync(s->bcg_mem, 0, sizeof(double) * 8 * GCGE_MAXCOLS, s->st));
   CU(cudaMalloc(&s->bcg_int, sizeof(int) * (2 * GCGE_MAXCOLS + 1)));
   CU(cudaMemsetAsync(s->bcg_int, 0, sizeof(int) * (2 * GCGE_MAXCOLS + 1), s->st));
   CU(cudaHostAlloc(&s->h_pinned_int, sizeof(int) * 16, cudaHostAllocMapped));
@@ -676,6 +676,7 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   s->bcg.nu = s->bcg_int + GCGE_MAXCOLS;
   s->bcg.nu_host = s->h_pinned_int;
   s->bcg.acol = s->bcg_mem + 6 * GCGE_MAXCOLS;
+  s->bcg.bcol = reinterpret_cast<float*>(s->bcg_mem + 7 * GCGE_MAXCOLS);
   s->bcg.mask = s->bcg_int + GCGE_MAXCOLS + 1;
   CU(cudaStreamSynchronize(s->st));
   if (p.use_shift == 1 || p.if_shift == 1) CHK(build_shift_op(s));
