@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(kT) k_rows_update(int n, float* X, float* R,
 #pragma unroll
   for (int c = 0; c < KW; c++) {
     on[c] = s.mask[c] != 0;
-    alpha[c] = on[c] ? (float)s.acol[c] : 0.f;
+    alpha[c] = on[c] ? s.acolf[c] : 0.f;
   }
   float acc[KW];
 #pragma unroll
@@ -565,6 +565,7 @@ __global__ void k_rows_alpha(const double* __restrict__ partial, int nblk, int l
     const int c = s.unl[id];
     s.ptw[id] = pw[c];
     s.acol[c] = s.rho2[id] / s.ptw[id];
+    s.acolf[c] = (float)s.acol[c];  // once here instead of in every thread of k_rows_update
   }
 }
 

@@ -20,6 +20,7 @@ struct BcgScalars {
   double* acol;  // row-interleaved path: alpha of each column (32 doubles)
   int* mask;     // row-interleaved path: 1 for the active columns (32 ints)
   float* bcol;   // row-interleaved path: beta of each active column for the next p (32 floats)
+  float* acolf;  // row-interleaved path: acol rounded to float (32 floats)
 };
 
 // Solves A x_c = rhs_c for the len columns (rhs is overwritten by the

@@ -452,6 +452,7 @@ extern "C" int GCGE_CUDA_BlockCG(const GCGE_CUDA_MAT* A, double* const* rhs, dou
   s.acol = nullptr;  // column path only
   s.mask = nullptr;
   s.bcol = nullptr;
+  s.acolf = nullptr;
   double* partial = buf + 6 * GCGE_MAXCOLS;
   double* vecs = partial + (size_t)k * nb;
   int it = -1;

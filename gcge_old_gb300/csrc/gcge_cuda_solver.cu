@@ -677,6 +677,7 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   s->bcg.nu_host = s->h_pinned_int;
   s->bcg.acol = s->bcg_mem + 6 * GCGE_MAXCOLS;
   s->bcg.bcol = reinterpret_cast<float*>(s->bcg_mem + 7 * GCGE_MAXCOLS);
+  s->bcg.acolf = s->bcg.bcol + 64;  // 32 floats after the betas, still inside the slot
   s->bcg.mask = s->bcg_int + GCGE_MAXCOLS + 1;
   CU(cudaStreamSynchronize(s->st));
   if (p.use_shift == 1 || p.if_shift == 1) CHK(build_shift_op(s));
