@@ -374,7 +374,7 @@ template <int KW>
 __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__ rp,
                                                   const int* __restrict__ ci,
                                                   const float* __restrict__ val,
-                                                  const float* __restrict__ X, float* R, int len,
+                                                  const float* __restrict__ X, float* __restrict__ R, int len,
                                                   double* __restrict__ partial,
                                                   const int* __restrict__ hidx,
                                                   const int* __restrict__ hch,
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kT) k_rows_init(int n, const int* __restrict__
 
 // p = r (first step) or p = r + beta p, beta = rho2[c] / rho1[c], for the active columns
 template <int KW>
-__global__ void __launch_bounds__(kT) k_rows_p(int n, const float* __restrict__ R, float* P,
+__global__ void __launch_bounds__(kT) k_rows_p(int n, const float* __restrict__ R, float* __restrict__ P,
                                                BcgScalars s, int first) {
   if (*s.nu == 0) return;
   float beta[KW];
@@ -440,7 +440,7 @@ template <int KW>
 __global__ void __launch_bounds__(kT, KW <= 12 ? kApBlocks12 : 1) k_rows_ap(int n, const int* __restrict__ rp,
                                                 const int* __restrict__ ci,
                                                 const float* __restrict__ val,
-                                                const float* __restrict__ P, float* W, int len,
+                                                const float* __restrict__ P, float* __restrict__ W, int len,
                                                 BcgScalars s, double* __restrict__ partial,
                                                 const int* __restrict__ hidx,
                                                 const int* __restrict__ hch,
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(kT, KW <= 12 ? kApBlocks12 : 1) k_rows_ap(int 
 
 // x += alpha p, r -= alpha w and partial r.r for the active columns
 template <int KW>
-__global__ void __launch_bounds__(kT) k_rows_update(int n, float* X, float* R,
+__global__ void __launch_bounds__(kT) k_rows_update(int n, float* __restrict__ X, float* __restrict__ R,
                                                     const float* __restrict__ P,
                                                     const float* __restrict__ W, int len,
                                                     BcgScalars s, double* __restrict__ partial) {
