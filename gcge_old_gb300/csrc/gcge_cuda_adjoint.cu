@@ -164,8 +164,10 @@ __global__ void k_step(ColList<double> MU, ColList<double> R, ColList<double> P,
                        const int* __restrict__ active, int n) {
   const int c = blockIdx.y;
   if (!active[c]) return;
-  const double d = pu[c];
-  const double a = (d != 0.0) ? rz[c] / d : 0.0;
+  __shared__ double a_s;  // one division per block
+  if (threadIdx.x == 0) a_s = (pu[c] != 0.0) ? rz[c] / pu[c] : 0.0;
+  __syncthreads();
+  const double a = a_s;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     MU.p[c][r] = fma(a, P.p[c][r], MU.p[c][r]);
     R.p[c][r] = fma(-a, U.p[c][r], R.p[c][r]);
@@ -178,8 +180,10 @@ __global__ void k_direction(ColList<double> Z, ColList<double> P, const double* 
                             int n) {
   const int c = blockIdx.y;
   if (!active[c]) return;
-  const double d = rz_old[c];
-  const double b = (d != 0.0) ? rz_new[c] / d : 0.0;
+  __shared__ double b_s;  // one division per block
+  if (threadIdx.x == 0) b_s = (rz_old[c] != 0.0) ? rz_new[c] / rz_old[c] : 0.0;
+  __syncthreads();
+  const double b = b_s;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
     P.p[c][r] = fma(b, P.p[c][r], Z.p[c][r]);
 }

@@ -111,7 +111,11 @@ __global__ void k_bcg_p(int n, ColList<T> R, ColList<T> P, BcgScalars s, int fir
   if (first) {
     for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT) p[i] = r[i];
   } else {
-    const T beta = (T)(s.rho2[idx] / s.rho1[idx]);
+    // one division per block (not per thread: FP64 divisions are costly on GB300)
+    __shared__ T beta_s;
+    if (threadIdx.x == 0) beta_s = (T)(s.rho2[idx] / s.rho1[idx]);
+    __syncthreads();
+    const T beta = beta_s;
     for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT)
       p[i] = r[i] + beta * p[i];
   }
@@ -167,7 +171,10 @@ __global__ void k_bcg_update(int n, ColList<T> X, ColList<T> R, ColList<T> P, Co
   const int id = blockIdx.y;
   if (id >= *s.nu) return;
   const int idx = s.unl[id];
-  const T alpha = (T)(s.rho2[id] / s.ptw[id]);
+  __shared__ T alpha_s;  // one division per block
+  if (threadIdx.x == 0) alpha_s = (T)(s.rho2[id] / s.ptw[id]);
+  __syncthreads();
+  const T alpha = alpha_s;
   T* x = X.p[idx];
   T* r = R.p[idx];
   const T* p = P.p[idx];
