@@ -788,6 +788,19 @@ static __global__ void k_frob(const double* __restrict__ G, int m, int k, double
   if (threadIdx.x == 0) out[0] = sqrt(sh[0]);
 }
 
+// X_c[i] <- pseudo-random in [-1, 1): splitmix64 of (row, column, seed)
+static __global__ void k_fill_random(ColList<double> X, int n, unsigned seed) {
+  const int c = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned long long z = ((unsigned long long)c << 32 | (unsigned)i) +
+                           0x9E3779B97F4A7C15ull * (seed + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    X.p[c][i] = (double)(z >> 11) * 0x1.0p-52 - 1.0;
+  }
+}
+
 // V[start:*end] <- B-orthonormal, dropping dependent columns.  CholQR with
 // dropping, applied twice.  The scratch columns are T[0:k] (swapped with V).
 static int cholqr2(Solver* s, std::vector<double*>& V, int start, int* end,
@@ -1299,9 +1312,19 @@ extern "C" int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* s) {
     std::vector<double*> scratch(s->V.begin(), s->V.begin() + nev);
     int dx = nev;
     int rc = cholqr2(s, s->evec, 0, &dx, scratch);
+    // a block that loses columns (dependent or zero columns) is completed with
+    // pseudo-random columns and orthonormalised again, as the reference does
+    // for a short initial block (src/gcge_eigsol.c:134-217)
+    for (int attempt = 1; rc == GCGE_CUDA_OK && dx < nev && attempt <= 8; attempt++) {
+      dim3 g((n + 255) / 256, nev - dx);
+      KL((k_fill_random<<<g, 256, 0, s->st>>>(cols(s->evec, dx, nev), n, (unsigned)attempt)));
+      dx = nev;
+      rc = cholqr2(s, s->evec, 0, &dx, scratch);
+    }
     for (int j = 0; j < nev; j++) s->V[j] = scratch[j];
     tm.stop();
     if (rc) return rc;
+    if (dx < nev) return set_err(GCGE_CUDA_ERR_NUMERIC, "initial block: %d independent columns", dx);
     s->dim_x = dx;
   }
   for (int j = 0; j < nev; j++)

@@ -176,3 +176,21 @@ def test_solver_nev128_analytic(cuda_lib, precision):
     np.testing.assert_allclose(ev, exact, rtol=1e-9)
     crit = O.true_residuals(A, None, ev, vec) * np.abs(ev) / np.maximum(1.0, np.abs(ev))
     assert crit.max() < 2e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solver_rank_deficient_initial_block(cuda_lib, precision):
+    """Dependent and zero columns in the given block are dropped by the
+    orthonormalisation and replaced by pseudo-random ones (the reference's
+    completion of a short initial block); the solve then finds the same pairs."""
+    A, B = M.laplace3d_mass(12, seed=1)
+    nev = 8
+    x0 = M.initial_block(A.n, nev, seed=5)
+    x0[3] = x0[1]
+    x0[5] = 2.0 * x0[1] - x0[2]
+    x0[6] = 0.0
+    ev, vec, st = S.solve(A, B, nev, x0, ev_tol=1e-10, ev_max_it=300, precision=precision)
+    import scipy.linalg as sla
+    ref = sla.eigh(A.to_scipy().toarray(), B.to_scipy().toarray(), eigvals_only=True)[:nev]
+    np.testing.assert_allclose(ev, ref, rtol=1e-9)
+    assert O.true_residuals(A, B, ev, vec).max() < 1e-9
