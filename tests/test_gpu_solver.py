@@ -194,3 +194,18 @@ def test_solver_rank_deficient_initial_block(cuda_lib, precision):
     ref = sla.eigh(A.to_scipy().toarray(), B.to_scipy().toarray(), eigvals_only=True)[:nev]
     np.testing.assert_allclose(ev, ref, rtol=1e-9)
     assert O.true_residuals(A, B, ev, vec).max() < 1e-9
+
+
+def test_solver_indefinite_b_returns(cuda_lib):
+    """An indefinite B (negative diagonal entries) breaks the B-orthonormalisation:
+    the solve must end with a status or at ev_max_it, never hang."""
+    A = M.laplace2d(12)
+    d = np.ones(A.n)
+    d[::7] = -1.0
+    B = M.diag_matrix(d)
+    x0 = M.initial_block(A.n, 4, seed=3)
+    try:
+        ev, vec, st = S.solve(A, B, 4, x0, ev_tol=1e-10, ev_max_it=5)
+        assert st["num_iter"] <= 5
+    except Exception as e:  # an error status is an acceptable outcome
+        assert "Solve" in str(e)
