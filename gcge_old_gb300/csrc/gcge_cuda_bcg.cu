@@ -41,7 +41,9 @@ __global__ void __launch_bounds__(kT) k_bcg_init(int n, const int* __restrict__ 
                                                  const int* __restrict__ ci,
                                                  const T* __restrict__ val, ColList<T> X,
                                                  ColList<T> R, int len,
-                                                 double* __restrict__ partial) {
+                                                 double* __restrict__ partial,
+                                                 const int* __restrict__ hidx,
+                                                 const T* __restrict__ hb) {
   __shared__ double sh[32];
   const int c0 = blockIdx.y * KC;
   const int kc = min(KC, len - c0);
@@ -52,12 +54,19 @@ __global__ void __launch_bounds__(kT) k_bcg_init(int n, const int* __restrict__ 
     T ax[KC];
 #pragma unroll
     for (int c = 0; c < KC; c++) ax[c] = T(0);
-    for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
-      const int col = __ldg(ci + j);
-      const T a = __ldg(val + j);
+    const int h = hidx ? __ldg(hidx + r) : -1;
+    if (h >= 0) {  // a heavy row: its products were formed chunk by chunk
 #pragma unroll
       for (int c = 0; c < KC; c++)
-        if (c < kc) ax[c] = fma(a, X.p[c0 + c][col], ax[c]);
+        if (c < kc) ax[c] = hb[(size_t)h * len + c0 + c];
+    } else {
+      for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+        const int col = __ldg(ci + j);
+        const T a = __ldg(val + j);
+#pragma unroll
+        for (int c = 0; c < KC; c++)
+          if (c < kc) ax[c] = fma(a, X.p[c0 + c][col], ax[c]);
+      }
     }
 #pragma unroll
     for (int c = 0; c < KC; c++)
@@ -127,7 +136,9 @@ __global__ void __launch_bounds__(kT) k_bcg_ap(int n, const int* __restrict__ rp
                                                const int* __restrict__ ci,
                                                const T* __restrict__ val, ColList<T> P,
                                                ColList<T> W, BcgScalars s,
-                                               double* __restrict__ partial) {
+                                               double* __restrict__ partial,
+                                               const int* __restrict__ hidx,
+                                               const T* __restrict__ hb, int kmax) {
   __shared__ double sh[32];
   const int nu = *s.nu;
   const int c0 = blockIdx.y * KC;
@@ -143,12 +154,19 @@ __global__ void __launch_bounds__(kT) k_bcg_ap(int n, const int* __restrict__ rp
     T ap[KC];
 #pragma unroll
     for (int c = 0; c < KC; c++) ap[c] = T(0);
-    for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
-      const int col = __ldg(ci + j);
-      const T a = __ldg(val + j);
+    const int h = hidx ? __ldg(hidx + r) : -1;
+    if (h >= 0) {  // a heavy row: products of the active ids, formed chunk by chunk
 #pragma unroll
       for (int c = 0; c < KC; c++)
-        if (c < kc) ap[c] = fma(a, P.p[ix[c]][col], ap[c]);
+        if (c < kc) ap[c] = hb[(size_t)h * kmax + c0 + c];
+    } else {
+      for (int j = __ldg(rp + r); j < __ldg(rp + r + 1); j++) {
+        const int col = __ldg(ci + j);
+        const T a = __ldg(val + j);
+#pragma unroll
+        for (int c = 0; c < KC; c++)
+          if (c < kc) ap[c] = fma(a, P.p[ix[c]][col], ap[c]);
+      }
     }
 #pragma unroll
     for (int c = 0; c < KC; c++)
@@ -220,21 +238,27 @@ template <typename T>
 int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>& RHS,
             const ColList<T>& X, const ColList<T>& P, const ColList<T>& W, int len, int max_it,
             double rate, const BcgScalars& s, double* partial, cudaStream_t st,
-            int* launches) {
+            int* launches, const GcgeDevCsr* M) {
   if (len <= 0) return 0;
   const int nb = nblocks(n);
   int nl = 0;
+  // heavy rows (FP64 only): products of the long rows formed chunk-wise first
+  const bool hv = sizeof(T) == 8 && M && M->nheavy > 0;
+  const int* hidx = hv ? M->hidx : nullptr;
+  const T* hb = hv ? reinterpret_cast<const T*>(M->hb64) : nullptr;
+  const int hl = hv ? 2 * ((len + kHeavyGroup - 1) / kHeavyGroup) : 0;  // its launches
+  if (hv) heavy_cols_f64(*M, reinterpret_cast<const ColList<double>&>(X), len, st);
   // FP64: one pass over A for up to 16 columns; FP32: passes of 8 columns
   // (the 16-column FP32 pass, at 80 registers, left too few warps per SM)
   constexpr int KW = sizeof(T) == 8 ? 16 : 8;
   if (len <= 8)
-    k_bcg_init<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, X, RHS, len, partial);
+    k_bcg_init<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, X, RHS, len, partial, hidx, hb);
   else
     k_bcg_init<T, KW><<<dim3(nb, (len + KW - 1) / KW), kT, 0, st>>>(n, rp, ci, val, X, RHS,
-                                                                      len, partial);
+                                                                      len, partial, hidx, hb);
   k_reduce<<<len, 256, 0, st>>>(partial, nb, len, nullptr, s.rho2);
   k_ctrl_init<<<1, 1, 0, st>>>(s, len);
-  nl += 3;
+  nl += 3 + hl;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
   int niter = 1;
   int nu = s.nu_host[0];
@@ -247,16 +271,20 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
     const int batch = (max_it - niter) < kBatch ? (max_it - niter) : kBatch;
     for (int j = 0; j < batch; j++) {
       k_bcg_p<T><<<dim3(nb, len), kT, 0, st>>>(n, RHS, P, s, niter + j == 1 ? 1 : 0);
+      if (hv)
+        heavy_cols_active_f64(*M, reinterpret_cast<const ColList<double>&>(P), s.unl, s.nu, len,
+                              st);
       if (len <= 8)
-        k_bcg_ap<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, P, W, s, partial);
+        k_bcg_ap<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, P, W, s, partial, hidx, hb,
+                                                    len);
       else
         k_bcg_ap<T, KW><<<dim3(nb, (len + KW - 1) / KW), kT, 0, st>>>(n, rp, ci, val, P, W, s,
-                                                                       partial);
+                                                                       partial, hidx, hb, len);
       k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.ptw);
       k_bcg_update<T><<<dim3(nb, len), kT, 0, st>>>(n, X, RHS, P, W, s, partial);
       k_reduce<<<len, 256, 0, st>>>(partial, nb, len, s.nu, s.rnew);
       k_ctrl_step<<<1, 1, 0, st>>>(s, rate, j);
-      nl += 6;
+      nl += 6 + hl;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
     for (int j = 0; j < batch; j++) {
@@ -272,10 +300,11 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
 template int bcg_run<double>(const int*, const int*, const double*, int, const ColList<double>&,
                              const ColList<double>&, const ColList<double>&,
                              const ColList<double>&, int, int, double, const BcgScalars&, double*,
-                             cudaStream_t, int*);
+                             cudaStream_t, int*, const GcgeDevCsr*);
 template int bcg_run<float>(const int*, const int*, const float*, int, const ColList<float>&,
                             const ColList<float>&, const ColList<float>&, const ColList<float>&,
-                            int, int, double, const BcgScalars&, double*, cudaStream_t, int*);
+                            int, int, double, const BcgScalars&, double*, cudaStream_t, int*,
+                            const GcgeDevCsr*);
 
 }  // namespace gcge
 

@@ -26,10 +26,13 @@ struct BcgScalars {
 // Solves A x_c = rhs_c for the len columns (rhs is overwritten by the
 // residual).  The diagonal fast path is not used here: A is the stiffness.
 // Returns the reference's final niter, or -1 on a CUDA error.
+// M (optional, FP64 only): the matrix rp / ci / val describe, whose heavy rows
+// are then multiplied chunk-wise.
 template <typename T>
 int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>& RHS,
             const ColList<T>& X, const ColList<T>& P, const ColList<T>& W, int len, int max_it,
-            double rate, const BcgScalars& s, double* partial, cudaStream_t st, int* launches);
+            double rate, const BcgScalars& s, double* partial, cudaStream_t st, int* launches,
+            const GcgeDevCsr* M = nullptr);
 
 // The same FP32 block CG with the four vectors stored row-interleaved: R, X,
 // P, W are n x KW float arrays (element (r, c) at r*KW + c, KW = len rounded

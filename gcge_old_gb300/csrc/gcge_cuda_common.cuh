@@ -61,6 +61,10 @@ int heavy_setup(GcgeDevCsr& M, const int* h_rp);
 void heavy_free(GcgeDevCsr& M);
 // M.hb64[h * k + c] = (M X_c)[heavy row h] for c < k.
 void heavy_cols_f64(const GcgeDevCsr& M, const ColList<double>& X, int k, cudaStream_t st);
+// M.hb64[h * kmax + id] = (M P_{unl[id]})[heavy row h] for the active ids
+// id < *nu (a block CG's active list, read on the device), kmax >= *nu.
+void heavy_cols_active_f64(const GcgeDevCsr& M, const ColList<double>& P, const int* unl,
+                           const int* nu, int kmax, cudaStream_t st);
 // M.cb32[q * KW + c] = chunk q's share of (M X)[its row][c] for the row-interleaved
 // n x KW block X with M's FP32 values val (a heavy row's product is the sum of
 // its chunks hch[h] .. hch[h+1]-1, in that order); skipped on the device when

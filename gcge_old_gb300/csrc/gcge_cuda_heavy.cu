@@ -45,6 +45,51 @@ __global__ void k_heavy_cols(int nchunk, const int* __restrict__ chb, const int*
     for (int c = 0; c < kc; c++) cb[(size_t)warp * kHeavyGroup + g0 + c] = acc[c];
 }
 
+// the same over the active columns of a block CG: column g of this pass is
+// P.p[unl[cbase + g]] for cbase + g < *nu (the active count, on the device)
+__global__ void k_heavy_cols_active(int nchunk, const int* __restrict__ chb,
+                                    const int* __restrict__ che, const int* __restrict__ ci,
+                                    const double* __restrict__ v, ColList<double> P,
+                                    const int* __restrict__ unl, const int* __restrict__ nu,
+                                    int cbase, double* __restrict__ cb) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nchunk) return;
+  const int g0 = blockIdx.y * 8;
+  const int kc = min(8, *nu - cbase - g0);
+  if (kc <= 0) return;
+  const double* col[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) col[c] = P.p[unl[cbase + g0 + (c < kc ? c : 0)]];
+  double acc[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) acc[c] = 0.0;
+  const int e = __ldg(che + warp);
+  for (int j = __ldg(chb + warp) + lane; j < e; j += 32) {
+    const int cj = __ldg(ci + j);
+    const double a = __ldg(v + j);
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      if (c < kc) acc[c] = fma(a, col[c][cj], acc[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 8; c++)
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  if (lane == 0)
+    for (int c = 0; c < kc; c++) cb[(size_t)warp * kHeavyGroup + g0 + c] = acc[c];
+}
+
+__global__ void k_heavy_sum_active(int nheavy, const int* __restrict__ hch,
+                                   const double* __restrict__ cb, int ncols, int cbase,
+                                   const int* __restrict__ nu, int ldh, double* __restrict__ hb) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nheavy * ncols) return;
+  const int h = t / ncols, c = t % ncols;
+  if (cbase + c >= *nu) return;
+  double s = 0.0;
+  for (int q = __ldg(hch + h); q < __ldg(hch + h + 1); q++) s += cb[(size_t)q * kHeavyGroup + c];
+  hb[(size_t)h * ldh + cbase + c] = s;
+}
+
 __global__ void k_heavy_sum_cols(int nheavy, const int* __restrict__ hch,
                                  const double* __restrict__ cb, int ncols, int cbase, int ldh,
                                  double* __restrict__ hb) {
@@ -168,6 +213,20 @@ void heavy_cols_f64(const GcgeDevCsr& M, const ColList<double>& X, int k, cudaSt
                                                                  M.v, X, cbase, ncols, M.cb64);
     k_heavy_sum_cols<<<(M.nheavy * ncols + 255) / 256, 256, 0, st>>>(M.nheavy, M.hch, M.cb64,
                                                                      ncols, cbase, k, M.hb64);
+  }
+}
+
+void heavy_cols_active_f64(const GcgeDevCsr& M, const ColList<double>& P, const int* unl,
+                           const int* nu, int kmax, cudaStream_t st) {
+  if (M.nheavy == 0 || kmax <= 0) return;
+  const int threads = 32 * kWarpsPerBlock;
+  const int nbx = (M.nchunk + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  for (int cbase = 0; cbase < kmax; cbase += kHeavyGroup) {
+    const int ncols = kmax - cbase < kHeavyGroup ? kmax - cbase : kHeavyGroup;
+    k_heavy_cols_active<<<dim3(nbx, (ncols + 7) / 8), threads, 0, st>>>(
+        M.nchunk, M.chb, M.che, M.ci, M.v, P, unl, nu, cbase, M.cb64);
+    k_heavy_sum_active<<<(M.nheavy * ncols + 255) / 256, 256, 0, st>>>(
+        M.nheavy, M.hch, M.cb64, ncols, cbase, nu, kmax, M.hb64);
   }
 }
 

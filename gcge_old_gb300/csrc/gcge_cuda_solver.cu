@@ -1072,7 +1072,7 @@ static int compute_w(Solver* s) {
     steps = gcge::bcg_run<double>(Aop->rp, Aop->ci, Aop->v, s->n, R, Wc,
                                   cols(s->CG_p, 0, wl), cols(s->evec, 0, wl), wl,
                                   s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
-                                  &launches);
+                                  &launches, Aop);
   } else {
     // Iterative-refinement form: the FP32 block CG solves A e = rhs - A w0
     // from e0 = 0 and w = w0 + e.  These are the reference's CG iterates
