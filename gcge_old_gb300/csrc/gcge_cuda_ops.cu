@@ -464,7 +464,7 @@ extern "C" int GCGE_CUDA_BlockCG(const GCGE_CUDA_MAT* A, double* const* rhs, dou
       W.p[j] = vecs + (size_t)(k + j) * ld;
     }
     it = gcge::bcg_run<double>(M.rp, M.ci, M.v, n, R, X, P, W, k, max_it, rate, s, partial, 0,
-                               nullptr);
+                               nullptr, &M);
   } else {
     float* f = reinterpret_cast<float*>(vecs);
     float* v32 = nullptr;

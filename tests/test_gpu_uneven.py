@@ -61,6 +61,86 @@ def test_spmm_rows_f32_heavy_rows(cuda_lib, graph, k):
     dA.close()
 
 
+def _edge_rows_matrix():
+    """n = 3000 with empty rows (first and last among them), rows of exactly 64 and
+    65 entries (either side of the heavy-row threshold), 256 and 257 entries (either
+    side of a chunk boundary) and one row holding every column."""
+    from gcge_old_gb300.matrices import CSRMatrix
+    n = 3000
+    rng = np.random.default_rng(7)
+    lens = rng.integers(0, 9, n)
+    lens[[0, 17, 1500, n - 1]] = 0
+    lens[[5, 6]] = [64, 65]
+    lens[[100, 101, 102]] = [256, 257, 513]
+    lens[2000] = n
+    cols = [np.sort(rng.choice(n, L, replace=False)) for L in lens]
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum(lens)
+    ci = np.concatenate(cols).astype(np.int32)
+    val = rng.uniform(-1.0, 1.0, rp[-1])
+    return CSRMatrix(n, rp, ci, val)
+
+
+@pytest.mark.parametrize("k", [1, 8, 13])
+def test_spmm_edge_rows(cuda_lib, k):
+    import torch
+    from gcge_old_gb300.solver import DeviceMatrix
+    A = _edge_rows_matrix()
+    rng = np.random.default_rng(k)
+    dA = DeviceMatrix(A)
+    # FP64 columns
+    X = torch.from_numpy(rng.standard_normal((k, A.n))).cuda()
+    Y = torch.full_like(X, float("nan"))
+    xp = (C.c_void_p * k)(*[C.c_void_p(X[j].data_ptr()) for j in range(k)])
+    yp = (C.c_void_p * k)(*[C.c_void_p(Y[j].data_ptr()) for j in range(k)])
+    assert cuda_lib.GCGE_CUDA_MatDotMultiVec(dA.handle, xp, yp, k) == 0
+    ref = (A.to_scipy() @ X.cpu().numpy().T).T
+    scale = (abs(A.to_scipy()) @ np.abs(X.cpu().numpy().T)).T
+    got = Y.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert (np.abs(got - ref) <= 2e-14 * np.maximum(scale, 1e-300)).all()
+    assert (got[:, [0, 17, 1500, A.n - 1]] == 0).all()  # empty rows give exact zeros
+    # FP32 row-interleaved blocks
+    kw = (k + 3) // 4 * 4
+    Xr = np.zeros((A.n, kw), np.float32)
+    Xr[:, :k] = rng.standard_normal((A.n, k))
+    Xd = torch.from_numpy(Xr).cuda()
+    Yd = torch.full_like(Xd, float("nan"))
+    assert cuda_lib.GCGE_CUDA_MatDotRowsF32Async(dA.handle, C.c_void_p(Xd.data_ptr()),
+                                                 C.c_void_p(Yd.data_ptr()), k, None) == 0
+    torch.cuda.synchronize()
+    got = Yd.cpu().numpy()[:, :k]
+    ref = A.to_scipy() @ Xr[:, :k].astype(np.float64)
+    scale = abs(A.to_scipy()) @ np.abs(Xr[:, :k].astype(np.float64))
+    assert (np.abs(got - ref) <= 1e-5 * np.maximum(scale, 1e-30)).all()
+    assert (got[[0, 17, 1500, A.n - 1]] == 0).all()
+    dA.close()
+
+
+def test_block_cg_heavy_rows(cuda_lib, graph):
+    """The FP64 column block CG (GCGE_CUDA_BlockCG) on a power-law graph: the same
+    step count and iterate as the oracle's restatement of GCGE_BCG."""
+    from gcge_old_gb300.solver import DeviceMatrix
+    from gpu_util import dev_cols, host
+    from oracle import ops_ref as R
+    A = graph[0]
+    k = 13
+    rng = np.random.default_rng(8)
+    rhs = rng.standard_normal((k, A.n))
+    x0 = rng.standard_normal((k, A.n)) * 0.1
+    rs, rp = dev_cols(rhs)
+    xs, xp = dev_cols(x0)
+    dA = DeviceMatrix(A)
+    steps = C.c_int(0)
+    assert cuda_lib.GCGE_CUDA_BlockCG(dA.handle, rp, xp, k, A.n, 20, 1e-2, 0,
+                                      C.byref(steps)) == 0
+    X, _, niter = R.block_cg(A, rhs, x0, 20, 1e-2)
+    assert steps.value == niter
+    got = host(xs)
+    np.testing.assert_allclose(got, X, rtol=0, atol=1e-10 * np.abs(X).max())
+    dA.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_solve_power_law_graph(cuda_lib, precision):
     from gcge_old_gb300 import solver as S
