@@ -242,12 +242,13 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
   if (len <= 0) return 0;
   const int nb = nblocks(n);
   int nl = 0;
-  // heavy rows (FP64 only): products of the long rows formed chunk-wise first
-  const bool hv = sizeof(T) == 8 && M && M->nheavy > 0;
+  // heavy rows: products of the long rows formed chunk-wise first (with the
+  // values val, FP64 or the FP32 copy)
+  const bool hv = M && M->nheavy > 0;
   const int* hidx = hv ? M->hidx : nullptr;
   const T* hb = hv ? reinterpret_cast<const T*>(M->hb64) : nullptr;
   const int hl = hv ? 2 * ((len + kHeavyGroup - 1) / kHeavyGroup) : 0;  // its launches
-  if (hv) heavy_cols_f64(*M, reinterpret_cast<const ColList<double>&>(X), len, st);
+  if (hv) heavy_cols<T>(*M, val, X, len, st);
   // FP64: one pass over A for up to 16 columns; FP32: passes of 8 columns
   // (the 16-column FP32 pass, at 80 registers, left too few warps per SM)
   constexpr int KW = sizeof(T) == 8 ? 16 : 8;
@@ -271,9 +272,7 @@ int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>&
     const int batch = (max_it - niter) < kBatch ? (max_it - niter) : kBatch;
     for (int j = 0; j < batch; j++) {
       k_bcg_p<T><<<dim3(nb, len), kT, 0, st>>>(n, RHS, P, s, niter + j == 1 ? 1 : 0);
-      if (hv)
-        heavy_cols_active_f64(*M, reinterpret_cast<const ColList<double>&>(P), s.unl, s.nu, len,
-                              st);
+      if (hv) heavy_cols_active<T>(*M, val, P, s.unl, s.nu, len, st);
       if (len <= 8)
         k_bcg_ap<T, 8><<<dim3(nb, 1), kT, 0, st>>>(n, rp, ci, val, P, W, s, partial, hidx, hb,
                                                     len);

@@ -26,8 +26,8 @@ struct BcgScalars {
 // Solves A x_c = rhs_c for the len columns (rhs is overwritten by the
 // residual).  The diagonal fast path is not used here: A is the stiffness.
 // Returns the reference's final niter, or -1 on a CUDA error.
-// M (optional, FP64 only): the matrix rp / ci / val describe, whose heavy rows
-// are then multiplied chunk-wise.
+// M (optional): the matrix rp / ci describe (val: its values or their FP32
+// copy), whose heavy rows are then multiplied chunk-wise.
 template <typename T>
 int bcg_run(const int* rp, const int* ci, const T* val, int n, const ColList<T>& RHS,
             const ColList<T>& X, const ColList<T>& P, const ColList<T>& W, int len, int max_it,

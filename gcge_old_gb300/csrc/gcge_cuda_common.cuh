@@ -37,8 +37,9 @@ struct GcgeDevCsr {
   int* hch = nullptr;      // nheavy + 1: heavy row h owns chunks hch[h] .. hch[h+1]-1
   int* chb = nullptr;      // per chunk: first entry
   int* che = nullptr;      // per chunk: one past the last entry
-  double* hb64 = nullptr;  // nheavy x GCGE_MAXCOLS products (FP64 columns), [h * k + c]
-  double* cb64 = nullptr;  // nchunk x kHeavyGroup chunk partials
+  double* hb64 = nullptr;  // nheavy x GCGE_MAXCOLS products of columns, [h * k + c]
+                           // (FP64, or FP32 entries for the FP32 column block CG)
+  double* cb64 = nullptr;  // nchunk x kHeavyGroup chunk partials (likewise)
   float* cb32 = nullptr;   // nchunk x KW chunk partials (FP32 row-interleaved), [q * KW + c]
 };
 
@@ -59,12 +60,16 @@ constexpr int kHeavyRow = 64, kHeavyChunk = 256, kHeavyGroup = 64;
 // Builds the heavy-row chunks of M from its host row pointers; 0 or a cudaError_t.
 int heavy_setup(GcgeDevCsr& M, const int* h_rp);
 void heavy_free(GcgeDevCsr& M);
-// M.hb64[h * k + c] = (M X_c)[heavy row h] for c < k.
+// hb[h * k + c] = (M X_c)[heavy row h] for c < k, with M's values val (M.v, or
+// an FP32 copy for T = float); hb is M.hb64 viewed as T entries.
+template <typename T>
+void heavy_cols(const GcgeDevCsr& M, const T* val, const ColList<T>& X, int k, cudaStream_t st);
 void heavy_cols_f64(const GcgeDevCsr& M, const ColList<double>& X, int k, cudaStream_t st);
-// M.hb64[h * kmax + id] = (M P_{unl[id]})[heavy row h] for the active ids
-// id < *nu (a block CG's active list, read on the device), kmax >= *nu.
-void heavy_cols_active_f64(const GcgeDevCsr& M, const ColList<double>& P, const int* unl,
-                           const int* nu, int kmax, cudaStream_t st);
+// hb[h * kmax + id] = (M P_{unl[id]})[heavy row h] for the active ids id < *nu
+// (a block CG's active list, read on the device), kmax >= *nu.
+template <typename T>
+void heavy_cols_active(const GcgeDevCsr& M, const T* val, const ColList<T>& P, const int* unl,
+                       const int* nu, int kmax, cudaStream_t st);
 // M.cb32[q * KW + c] = chunk q's share of (M X)[its row][c] for the row-interleaved
 // n x KW block X with M's FP32 values val (a heavy row's product is the sum of
 // its chunks hch[h] .. hch[h+1]-1, in that order); skipped on the device when

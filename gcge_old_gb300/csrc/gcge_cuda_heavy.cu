@@ -19,21 +19,24 @@ namespace {
 
 constexpr int kWarpsPerBlock = 8;
 
+// Column form (T = double: FP64 columns and values; T = float: the FP32
+// columns of the mixed block CG with the FP32 copy of the values).
+template <typename T>
 __global__ void k_heavy_cols(int nchunk, const int* __restrict__ chb, const int* __restrict__ che,
-                             const int* __restrict__ ci, const double* __restrict__ v,
-                             ColList<double> X, int cbase, int ncols, double* __restrict__ cb) {
+                             const int* __restrict__ ci, const T* __restrict__ v,
+                             ColList<T> X, int cbase, int ncols, T* __restrict__ cb) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= nchunk) return;
   const int g0 = blockIdx.y * 8;
   const int kc = min(8, ncols - g0);
   if (kc <= 0) return;
-  double acc[8];
+  T acc[8];
 #pragma unroll
-  for (int c = 0; c < 8; c++) acc[c] = 0.0;
+  for (int c = 0; c < 8; c++) acc[c] = T(0);
   const int e = __ldg(che + warp);
   for (int j = __ldg(chb + warp) + lane; j < e; j += 32) {
     const int col = __ldg(ci + j);
-    const double a = __ldg(v + j);
+    const T a = __ldg(v + j);
 #pragma unroll
     for (int c = 0; c < 8; c++)
       if (c < kc) acc[c] = fma(a, __ldg(X.p[cbase + g0 + c] + col), acc[c]);
@@ -47,26 +50,27 @@ __global__ void k_heavy_cols(int nchunk, const int* __restrict__ chb, const int*
 
 // the same over the active columns of a block CG: column g of this pass is
 // P.p[unl[cbase + g]] for cbase + g < *nu (the active count, on the device)
+template <typename T>
 __global__ void k_heavy_cols_active(int nchunk, const int* __restrict__ chb,
                                     const int* __restrict__ che, const int* __restrict__ ci,
-                                    const double* __restrict__ v, ColList<double> P,
+                                    const T* __restrict__ v, ColList<T> P,
                                     const int* __restrict__ unl, const int* __restrict__ nu,
-                                    int cbase, double* __restrict__ cb) {
+                                    int cbase, T* __restrict__ cb) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= nchunk) return;
   const int g0 = blockIdx.y * 8;
   const int kc = min(8, *nu - cbase - g0);
   if (kc <= 0) return;
-  const double* col[8];
+  const T* col[8];
 #pragma unroll
   for (int c = 0; c < 8; c++) col[c] = P.p[unl[cbase + g0 + (c < kc ? c : 0)]];
-  double acc[8];
+  T acc[8];
 #pragma unroll
-  for (int c = 0; c < 8; c++) acc[c] = 0.0;
+  for (int c = 0; c < 8; c++) acc[c] = T(0);
   const int e = __ldg(che + warp);
   for (int j = __ldg(chb + warp) + lane; j < e; j += 32) {
     const int cj = __ldg(ci + j);
-    const double a = __ldg(v + j);
+    const T a = __ldg(v + j);
 #pragma unroll
     for (int c = 0; c < 8; c++)
       if (c < kc) acc[c] = fma(a, col[c][cj], acc[c]);
@@ -78,25 +82,27 @@ __global__ void k_heavy_cols_active(int nchunk, const int* __restrict__ chb,
     for (int c = 0; c < kc; c++) cb[(size_t)warp * kHeavyGroup + g0 + c] = acc[c];
 }
 
+template <typename T>
 __global__ void k_heavy_sum_active(int nheavy, const int* __restrict__ hch,
-                                   const double* __restrict__ cb, int ncols, int cbase,
-                                   const int* __restrict__ nu, int ldh, double* __restrict__ hb) {
+                                   const T* __restrict__ cb, int ncols, int cbase,
+                                   const int* __restrict__ nu, int ldh, T* __restrict__ hb) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nheavy * ncols) return;
   const int h = t / ncols, c = t % ncols;
   if (cbase + c >= *nu) return;
-  double s = 0.0;
+  T s = T(0);
   for (int q = __ldg(hch + h); q < __ldg(hch + h + 1); q++) s += cb[(size_t)q * kHeavyGroup + c];
   hb[(size_t)h * ldh + cbase + c] = s;
 }
 
+template <typename T>
 __global__ void k_heavy_sum_cols(int nheavy, const int* __restrict__ hch,
-                                 const double* __restrict__ cb, int ncols, int cbase, int ldh,
-                                 double* __restrict__ hb) {
+                                 const T* __restrict__ cb, int ncols, int cbase, int ldh,
+                                 T* __restrict__ hb) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nheavy * ncols) return;
   const int h = t / ncols, c = t % ncols;
-  double s = 0.0;
+  T s = T(0);
   for (int q = __ldg(hch + h); q < __ldg(hch + h + 1); q++) s += cb[(size_t)q * kHeavyGroup + c];
   hb[(size_t)h * ldh + cbase + c] = s;
 }
@@ -203,31 +209,51 @@ void heavy_free(GcgeDevCsr& M) {
   M.nheavy = M.nchunk = 0;
 }
 
-void heavy_cols_f64(const GcgeDevCsr& M, const ColList<double>& X, int k, cudaStream_t st) {
+template <typename T>
+void heavy_cols(const GcgeDevCsr& M, const T* val, const ColList<T>& X, int k, cudaStream_t st) {
   if (M.nheavy == 0 || k <= 0) return;
   const int threads = 32 * kWarpsPerBlock;
   const int nbx = (M.nchunk + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  T* cb = reinterpret_cast<T*>(M.cb64);  // T = float: the same buffers at float entries
+  T* hb = reinterpret_cast<T*>(M.hb64);
   for (int cbase = 0; cbase < k; cbase += kHeavyGroup) {
     const int ncols = k - cbase < kHeavyGroup ? k - cbase : kHeavyGroup;
-    k_heavy_cols<<<dim3(nbx, (ncols + 7) / 8), threads, 0, st>>>(M.nchunk, M.chb, M.che, M.ci,
-                                                                 M.v, X, cbase, ncols, M.cb64);
-    k_heavy_sum_cols<<<(M.nheavy * ncols + 255) / 256, 256, 0, st>>>(M.nheavy, M.hch, M.cb64,
-                                                                     ncols, cbase, k, M.hb64);
+    k_heavy_cols<T><<<dim3(nbx, (ncols + 7) / 8), threads, 0, st>>>(M.nchunk, M.chb, M.che,
+                                                                    M.ci, val, X, cbase, ncols,
+                                                                    cb);
+    k_heavy_sum_cols<T><<<(M.nheavy * ncols + 255) / 256, 256, 0, st>>>(M.nheavy, M.hch, cb,
+                                                                        ncols, cbase, k, hb);
   }
 }
 
-void heavy_cols_active_f64(const GcgeDevCsr& M, const ColList<double>& P, const int* unl,
-                           const int* nu, int kmax, cudaStream_t st) {
+template <typename T>
+void heavy_cols_active(const GcgeDevCsr& M, const T* val, const ColList<T>& P, const int* unl,
+                       const int* nu, int kmax, cudaStream_t st) {
   if (M.nheavy == 0 || kmax <= 0) return;
   const int threads = 32 * kWarpsPerBlock;
   const int nbx = (M.nchunk + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  T* cb = reinterpret_cast<T*>(M.cb64);
+  T* hb = reinterpret_cast<T*>(M.hb64);
   for (int cbase = 0; cbase < kmax; cbase += kHeavyGroup) {
     const int ncols = kmax - cbase < kHeavyGroup ? kmax - cbase : kHeavyGroup;
-    k_heavy_cols_active<<<dim3(nbx, (ncols + 7) / 8), threads, 0, st>>>(
-        M.nchunk, M.chb, M.che, M.ci, M.v, P, unl, nu, cbase, M.cb64);
-    k_heavy_sum_active<<<(M.nheavy * ncols + 255) / 256, 256, 0, st>>>(
-        M.nheavy, M.hch, M.cb64, ncols, cbase, nu, kmax, M.hb64);
+    k_heavy_cols_active<T><<<dim3(nbx, (ncols + 7) / 8), threads, 0, st>>>(
+        M.nchunk, M.chb, M.che, M.ci, val, P, unl, nu, cbase, cb);
+    k_heavy_sum_active<T><<<(M.nheavy * ncols + 255) / 256, 256, 0, st>>>(
+        M.nheavy, M.hch, cb, ncols, cbase, nu, kmax, hb);
   }
+}
+
+template void heavy_cols<double>(const GcgeDevCsr&, const double*, const ColList<double>&, int,
+                                 cudaStream_t);
+template void heavy_cols<float>(const GcgeDevCsr&, const float*, const ColList<float>&, int,
+                                cudaStream_t);
+template void heavy_cols_active<double>(const GcgeDevCsr&, const double*, const ColList<double>&,
+                                        const int*, const int*, int, cudaStream_t);
+template void heavy_cols_active<float>(const GcgeDevCsr&, const float*, const ColList<float>&,
+                                       const int*, const int*, int, cudaStream_t);
+
+void heavy_cols_f64(const GcgeDevCsr& M, const ColList<double>& X, int k, cudaStream_t st) {
+  heavy_cols<double>(M, M.v, X, k, st);
 }
 
 void heavy_rows_f32(const GcgeDevCsr& M, const float* val, const float* X, int KW, const int* nu,

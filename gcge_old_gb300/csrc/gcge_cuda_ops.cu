@@ -484,7 +484,7 @@ extern "C" int GCGE_CUDA_BlockCG(const GCGE_CUDA_MAT* A, double* const* rhs, dou
       k_cvt_d2f<<<(n + 255) / 256, 256>>>(x[j], X.p[j], n);
     }
     it = gcge::bcg_run<float>(M.rp, M.ci, v32, n, R, X, P, W, k, max_it, rate, s, partial, 0,
-                              nullptr);
+                              nullptr, &M);
     for (int j = 0; j < k; j++) {
       k_cvt_f2d<<<(n + 255) / 256, 256>>>(X.p[j], x[j], n);
       k_cvt_f2d<<<(n + 255) / 256, 256>>>(R.p[j], rhs[j], n);

@@ -1103,7 +1103,7 @@ static int compute_w(Solver* s) {
       steps = gcge::bcg_run<float>(Aop->rp, Aop->ci, Aop->v32, s->n, fr, fx,
                                    colsf(s->f_p, 0, wl), colsf(s->f_w, 0, wl), wl,
                                    s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
-                                   &launches);
+                                   &launches, Aop);
       KL(gcge::add_f32_to_f64(fx, Wc, wl, s->n, s->st));
     }
   }

@@ -117,13 +117,19 @@ def test_spmm_edge_rows(cuda_lib, k):
     dA.close()
 
 
-def test_block_cg_heavy_rows(cuda_lib, graph):
-    """The FP64 column block CG (GCGE_CUDA_BlockCG) on a power-law graph: the same
-    step count and iterate as the oracle's restatement of GCGE_BCG."""
+@pytest.mark.parametrize("fp32", [0, 1])
+def test_block_cg_heavy_rows(cuda_lib, fp32):
+    """The column block CG (GCGE_CUDA_BlockCG, FP64 and FP32) on a power-law graph:
+    the same step count and iterate as the oracle's restatement of GCGE_BCG.  The shift
+    (100) keeps the system well conditioned: with the 1e-3 shift of the solver
+    tests, 20 CG steps turn one-ulp differences in the products (the heavy rows
+    are summed chunk-wise, in another order than a row loop) into differences of
+    about 1e-2 in the iterate, in the oracle itself."""
     from gcge_old_gb300.solver import DeviceMatrix
     from gpu_util import dev_cols, host
     from oracle import ops_ref as R
-    A = graph[0]
+    A = M.chung_lu(50_000, seed=1, shift=100.0)[0]
+    assert (np.diff(A.rowptr) > 64).sum() > 100
     k = 13
     rng = np.random.default_rng(8)
     rhs = rng.standard_normal((k, A.n))
@@ -132,13 +138,40 @@ def test_block_cg_heavy_rows(cuda_lib, graph):
     xs, xp = dev_cols(x0)
     dA = DeviceMatrix(A)
     steps = C.c_int(0)
-    assert cuda_lib.GCGE_CUDA_BlockCG(dA.handle, rp, xp, k, A.n, 20, 1e-2, 0,
+    assert cuda_lib.GCGE_CUDA_BlockCG(dA.handle, rp, xp, k, A.n, 20, 1e-2, fp32,
                                       C.byref(steps)) == 0
     X, _, niter = R.block_cg(A, rhs, x0, 20, 1e-2)
-    assert steps.value == niter
     got = host(xs)
-    np.testing.assert_allclose(got, X, rtol=0, atol=1e-10 * np.abs(X).max())
+    if not fp32:
+        assert steps.value == niter
+        np.testing.assert_allclose(got, X, rtol=0, atol=1e-7 * np.abs(X).max())
+    else:  # FP32 columns and values: the same stopping rule, FP32 accuracy
+        assert abs(steps.value - niter) <= 2
+        np.testing.assert_allclose(got, X, rtol=0, atol=1e-4 * np.abs(X).max())
+    a = A.to_scipy()
+    for j in range(k):
+        r0 = np.linalg.norm(rhs[j] - a @ x0[j])
+        bound = 1e-2 * r0 * (1.05 if fp32 else 1.0001)
+        assert np.linalg.norm(rhs[j] - a @ got[j]) <= bound or steps.value == 20
     dA.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_wide_block_power_law_graph(cuda_lib, precision):
+    """Block size 36 (above the 32 columns of the row-interleaved FP32 blocks, so
+    the mixed solve runs the FP32 column block CG) on a shifted power-law graph
+    with 117 heavy rows, against the oracle port."""
+    from gcge_old_gb300 import solver as S
+    A, B, _ = M.chung_lu(5000, seed=2, shift=100.0)
+    assert (np.diff(A.rowptr) > 64).sum() > 100
+    nev = 40
+    x0 = M.initial_block(A.n, nev, seed=3)
+    kw = dict(ev_tol=1e-8, ev_max_it=150, block_size=36)
+    ev, vec, st = S.solve(A, B, nev, x0, precision=precision, **kw)
+    ref = O.port_solve(A, B, nev, x0, O.default_para(nev, **kw), threads=8)
+    assert np.max(np.abs(ev - ref["eval"]) / np.abs(ref["eval"])) < 1e-9
+    crit = O.true_residuals(A, B, ev, vec) * np.abs(ev) / np.maximum(1.0, np.abs(ev))
+    assert crit.max() < 1.5e-8, crit
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
