@@ -145,9 +145,12 @@ def test_block_cg_heavy_rows(cuda_lib, fp32):
     if not fp32:
         assert steps.value == niter
         np.testing.assert_allclose(got, X, rtol=0, atol=1e-7 * np.abs(X).max())
-    else:  # FP32 columns and values: the same stopping rule, FP32 accuracy
+    else:
+        # FP32 columns and values: the same stopping rule.  The iterates are not
+        # compared: one-ulp changes of the FP64 products already move the
+        # oracle's own iterate by 1e-8 here (an amplification of ~1e7), so FP32
+        # rounding moves it by O(1e-2); the residual bound below is the check.
         assert abs(steps.value - niter) <= 2
-        np.testing.assert_allclose(got, X, rtol=0, atol=1e-4 * np.abs(X).max())
     a = A.to_scipy()
     for j in range(k):
         r0 = np.linalg.norm(rhs[j] - a @ x0[j])
