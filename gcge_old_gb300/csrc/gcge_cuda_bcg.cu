@@ -669,14 +669,14 @@ __global__ void k_cols_to_rows(ColList<double> R, int len, float* __restrict__ R
 }
 
 template <int KW>
-__global__ void k_rows_add(const float* __restrict__ Xr, int len, ColList<double> Y, int n) {
+__global__ void k_rows_to_cols(const float* __restrict__ Xr, int len, ColList<double> Y, int n) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   float v[KW];
   load_row<KW>(Xr, r, v);
 #pragma unroll
   for (int c = 0; c < KW; c++)
-    if (c < len) Y.p[c][r] += (double)v[c];
+    if (c < len) Y.p[c][r] = (double)v[c];
 }
 
 template <int KW>
@@ -775,18 +775,18 @@ void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaS
   }
 }
 
-void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
-                          cudaStream_t st) {
+void rows_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
+                      cudaStream_t st) {
   const int g = (n + 255) / 256;
   switch (bcg_rows_width(len)) {
-    case 4: k_rows_add<4><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 8: k_rows_add<8><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 12: k_rows_add<12><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 16: k_rows_add<16><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 20: k_rows_add<20><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 24: k_rows_add<24><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 28: k_rows_add<28><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
-    case 32: k_rows_add<32><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 4: k_rows_to_cols<4><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 8: k_rows_to_cols<8><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 12: k_rows_to_cols<12><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 16: k_rows_to_cols<16><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 20: k_rows_to_cols<20><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 24: k_rows_to_cols<24><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 28: k_rows_to_cols<28><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
+    case 32: k_rows_to_cols<32><<<g, 256, 0, st>>>(Xr, len, Y, n); break;
   }
 }
 

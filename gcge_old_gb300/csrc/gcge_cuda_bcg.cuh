@@ -50,9 +50,9 @@ inline int bcg_rows_width(int len) { return (len + 3) / 4 * 4; }
 // Y = A X on row-interleaved n x bcg_rows_width(k) blocks (k <= 32).
 void spmm_rows_f32(const int* rp, const int* ci, const float* val, int n, const float* X,
                    float* Y, int k, cudaStream_t st, const GcgeDevCsr* M = nullptr);
-// Rr (n x KW rows) <- FP64 columns R[0:len] (zero-padded); Y[c] += Xr[:, c].
+// Rr (n x KW rows) <- FP64 columns R[0:len] (zero-padded); Y[c] = Xr[:, c].
 void cols_to_rows_f32(const ColList<double>& R, int len, float* Rr, int n, cudaStream_t st);
-void rows_add_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
-                          cudaStream_t st);
+void rows_to_cols_f64(const float* Xr, int len, const ColList<double>& Y, int n,
+                      cudaStream_t st);
 
 }  // namespace gcge

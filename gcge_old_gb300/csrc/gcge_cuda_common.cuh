@@ -132,8 +132,5 @@ void convert_f64_to_f32(const ColList<double>& X, const ColList<float>& Y, int k
                         cudaStream_t st);
 void convert_f32_to_f64(const ColList<float>& X, const ColList<double>& Y, int k, int n,
                         cudaStream_t st);
-// Y_j += (double)X_j
-void add_f32_to_f64(const ColList<float>& X, const ColList<double>& Y, int k, int n,
-                    cudaStream_t st);
 
 }  // namespace gcge

@@ -273,14 +273,6 @@ __global__ void k_convert(ColList<S> X, ColList<D> Y, int k, int n) {
   Y.p[c][row] = (D)X.p[c][row];
 }
 
-__global__ void k_add_f32(ColList<float> X, ColList<double> Y, int k, int n) {
-  const int row = blockIdx.x * kThreads + threadIdx.x;
-  if (row >= n) return;
-  const int c = blockIdx.y;
-  if (c >= k) return;
-  Y.p[c][row] += (double)X.p[c][row];
-}
-
 // Block-level sum of one value per thread into out (thread 0 returns it).
 __device__ inline double block_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -519,11 +511,5 @@ void convert_f32_to_f64(const ColList<float>& X, const ColList<double>& Y, int k
   k_convert<float, double><<<g, kThreads, 0, st>>>(X, Y, k, n);
 }
 
-void add_f32_to_f64(const ColList<float>& X, const ColList<double>& Y, int k, int n,
-                    cudaStream_t st) {
-  if (k <= 0) return;
-  dim3 g((n + kThreads - 1) / kThreads, k);
-  k_add_f32<<<g, kThreads, 0, st>>>(X, Y, k, n);
-}
 
 }  // namespace gcge

@@ -1075,10 +1075,15 @@ static int compute_w(Solver* s) {
                                   &launches, Aop);
   } else {
     // Iterative-refinement form: the FP32 block CG solves A e = rhs - A w0
-    // from e0 = 0 and w = w0 + e.  These are the reference's CG iterates
-    // shifted by w0 (same residuals, same stopping rule); keeping w0 in FP64
-    // matters near convergence, where w0 = x/lambda carries the eigenvector
-    // and the useful correction is as small as the eigen-residual.
+    // from e0 = 0 (the reference's CG iterates shifted by w0: same residuals,
+    // same stopping rule), and the W block is e itself.  w0 is x scaled, and
+    // x is a column of the basis W is orthogonalised against, so [X, P, e]
+    // spans the subspace of [X, P, w0 + e].  Near convergence e is as small as
+    // the eigen-residual: handing w0 + e to the orthogonalisation would
+    // leave it to cancel w0 (rounding ~1e-16 |w0|) under an absolute stopping
+    // test, and the renormalised remainder of a converged-looking column then
+    // kept a coupling of (|w0| / |e|) 1e-16 to X (1e-5 on hub-localised
+    // eigenvectors of a power-law graph, where the solve broke down).
     ColList<double> AW = cols(s->evec, 0, wl);
     KL(gcge::spmm_f64(*Aop, Wc, AW, wl, s->st));
     KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
@@ -1094,7 +1099,7 @@ static int compute_w(Solver* s) {
       steps = gcge::bcg_run_rows_f32(Aop->rp, Aop->ci, Aop->v32, s->n, Rr, Xr, Pr, Wr,
                                      wl, s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial,
                                      s->st, &launches, Aop);
-      KL(gcge::rows_add_to_cols_f64(Xr, wl, Wc, s->n, s->st));
+      KL(gcge::rows_to_cols_f64(Xr, wl, Wc, s->n, s->st));
     } else {
       ColList<float> fr = colsf(s->f_rhs, 0, wl), fx = colsf(s->f_x, 0, wl);
       KL(gcge::convert_f64_to_f32(R, fr, wl, s->n, s->st));
@@ -1104,7 +1109,7 @@ static int compute_w(Solver* s) {
                                    colsf(s->f_p, 0, wl), colsf(s->f_w, 0, wl), wl,
                                    s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
                                    &launches, Aop);
-      KL(gcge::add_f32_to_f64(fx, Wc, wl, s->n, s->st));
+      KL(gcge::convert_f32_to_f64(fx, Wc, wl, s->n, s->st));
     }
   }
   s->launches += launches;

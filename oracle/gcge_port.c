@@ -38,6 +38,11 @@ typedef struct {
    * eval_sm: eval_type "sm" (smallest magnitude) instead of "sa". */
   int use_shift, if_shift, eval_sm;
   double shift;
+  /* mixed: the W step of the CUDA solver's mixed precision (not part of the
+   * reference): the FP64 residual r = rhs - A w0 of the scaled start w0, the
+   * block CG on A e = r in FP32 from e = 0, and W = e (w0 is a scaled column
+   * of X, so [X, P, e] spans the subspace of [X, P, w0 + e]) */
+  int mixed;
 } port_para;
 
 typedef struct {
@@ -49,6 +54,7 @@ typedef struct {
   int *unlock, *itmp;
   int num_iter, num_unlock, num_conv_continuous;
   double* Bx; /* B x of the shifted block-CG operator */
+  float *a32, *b32, *f_r, *f_x, *f_p, *f_w; /* mixed: FP32 values and block-CG columns */
   port_para p;
   const port_csr *A, *B;
   long long spmv_count;
@@ -554,6 +560,101 @@ static void bcg(port_ws* w, double** RHS, double** X, int s0, int s1, int len, d
   }
 }
 
+/* FP32 operator of the mixed W step: y = (A + shift B) x in FP32 sums. */
+static void spmv32(port_ws* w, const float* x, float* y) {
+  const int n = w->n;
+  const port_csr* A = w->A;
+  const port_csr* B = w->B;
+  const int sh = w->p.if_shift == 1;
+  const float sigma = (float)w->p.shift;
+  w->spmv_count++;
+#pragma omp parallel for schedule(static) if (n > 32768)
+  for (int i = 0; i < n; i++) {
+    float s = 0.f;
+    for (int k = A->rp[i]; k < A->rp[i + 1]; k++) s += w->a32[k] * x[A->ci[k]];
+    if (sh) {
+      float t = 0.f;
+      if (B)
+        for (int k = B->rp[i]; k < B->rp[i + 1]; k++) t += w->b32[k] * x[B->ci[k]];
+      else
+        t = x[i];
+      s += sigma * t;
+    }
+    y[i] = s;
+  }
+}
+
+static double dot32(int n, const float* x, const float* y) {
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static) if (n > 32768)
+  for (int i = 0; i < n; i++) s += (double)(x[i] * y[i]);
+  return s;
+}
+
+/* The block CG above on FP32 columns (R: right-hand sides, overwritten by the
+ * residuals; X: start and result), the same bookkeeping. */
+static void bcg32(port_ws* w, int len) {
+  const int n = w->n;
+  double* rho1 = w->sub_dtmp;
+  double* rho2 = rho1 + len;
+  double* err = rho2 + len;
+  double* lerr = err + len;
+  double* ptw = lerr + len;
+  int* unl = w->itmp;
+  int nu = 0;
+  for (int idx = 0; idx < len; idx++) {
+    float* r = w->f_r + (size_t)idx * n;
+    float* ax = w->f_w + (size_t)idx * n;
+    spmv32(w, w->f_x + (size_t)idx * n, ax);
+    for (int i = 0; i < n; i++) r[i] -= ax[i];
+    rho2[idx] = dot32(n, r, r);
+  }
+  for (int idx = 0; idx < len; idx++) {
+    err[idx] = sqrt(rho2[idx]);
+    lerr[idx] = err[idx];
+    if (err[idx] >= 1e-15) unl[nu++] = idx;
+  }
+  int niter = 1;
+  while (nu > 0 && niter < w->p.cg_max_it) {
+    for (int id = 0; id < nu; id++) {
+      const int idx = unl[id];
+      float* p = w->f_p + (size_t)idx * n;
+      const float* r = w->f_r + (size_t)idx * n;
+      float* wv = w->f_w + (size_t)idx * n;
+      if (niter == 1) {
+        for (int i = 0; i < n; i++) p[i] = r[i];
+      } else {
+        const float beta = (float)(rho2[idx] / rho1[idx]);
+        for (int i = 0; i < n; i++) p[i] = r[i] + beta * p[i];
+      }
+      spmv32(w, p, wv);
+      ptw[id] = dot32(n, p, wv);
+    }
+    for (int id = 0; id < nu; id++) {
+      const int idx = unl[id];
+      const float alpha = (float)(rho2[id] / ptw[id]);
+      float* x = w->f_x + (size_t)idx * n;
+      float* r = w->f_r + (size_t)idx * n;
+      const float* p = w->f_p + (size_t)idx * n;
+      const float* wv = w->f_w + (size_t)idx * n;
+      for (int i = 0; i < n; i++) {
+        x[i] += alpha * p[i];
+        r[i] -= alpha * wv[i];
+      }
+      rho1[id] = rho2[id];
+      rho2[id] = dot32(n, r, r);
+    }
+    for (int id = 0; id < nu; id++) lerr[unl[id]] = sqrt(fabs(rho2[id]));
+    int old = nu;
+    nu = 0;
+    for (int id = 0; id < old; id++) {
+      int idx = unl[id];
+      if (lerr[idx] >= w->p.cg_rate * err[idx] && lerr[idx] >= 1e-15) unl[nu++] = idx;
+    }
+    niter++;
+  }
+}
+
 static void compute_w(port_ws* w) { /* :118-260 */
   const int n = w->n;
   int ws = w->dim_xp, wl = w->unconv_bs;
@@ -572,7 +673,30 @@ static void compute_w(port_ws* w) { /* :118-260 */
       axpby(n, 1.0 / (lam + w->p.shift), x, 0.0, wc);
     }
   }
-  bcg(w, w->V_tmp, w->V, 0, ws, wl, w->CG_p, w->evec);
+  if (!w->p.mixed) {
+    bcg(w, w->V_tmp, w->V, 0, ws, wl, w->CG_p, w->evec);
+    return;
+  }
+  /* mixed: r = rhs - A w0 in FP64, A e = r in FP32 from e = 0, W = e */
+  for (int idx = 0; idx < wl; idx++) {
+    double* r = w->V_tmp[idx];
+    double* wc = w->V[ws + idx];
+    spmv(w->A, wc, w->evec[0], w);
+    shift_term(w, wc, w->evec[0]);
+    axpby(n, -1.0, w->evec[0], 1.0, r);
+    float* fr = w->f_r + (size_t)idx * n;
+    float* fx = w->f_x + (size_t)idx * n;
+    for (int i = 0; i < n; i++) {
+      fr[i] = (float)r[i];
+      fx[i] = 0.f;
+    }
+  }
+  bcg32(w, wl);
+  for (int idx = 0; idx < wl; idx++) {
+    double* wc = w->V[ws + idx];
+    const float* fx = w->f_x + (size_t)idx * n;
+    for (int i = 0; i < n; i++) wc[i] = (double)fx[i];
+  }
 }
 
 static void compute_p(port_ws* w) { /* :329-478 */
@@ -754,6 +878,18 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
   w->unlock = (int*)calloc(w->max_dim_x, sizeof(int));
   w->res = (double*)calloc(nev, sizeof(double));
   w->Bx = (double*)calloc(n, sizeof(double));
+  if (w->p.mixed) {
+    const int annz = a_rp[n], bnnz = b_rp ? b_rp[n] : 0;
+    w->a32 = (float*)malloc(sizeof(float) * (annz > 0 ? annz : 1));
+    w->b32 = (float*)malloc(sizeof(float) * (bnnz > 0 ? bnnz : 1));
+    for (int k = 0; k < annz; k++) w->a32[k] = (float)a_v[k];
+    for (int k = 0; k < bnnz; k++) w->b32[k] = (float)b_v[k];
+    const size_t fn = (size_t)n * w->bs;
+    w->f_r = (float*)calloc(fn, sizeof(float));
+    w->f_x = (float*)calloc(fn, sizeof(float));
+    w->f_p = (float*)calloc(fn, sizeof(float));
+    w->f_w = (float*)calloc(fn, sizeof(float));
+  }
   for (int i = 0; i < nev; i++) w->res[i] = 1.0;
   for (int i = 0; i < w->max_dim_x; i++) w->unlock[i] = i;
   w->dim_x = nev;
@@ -837,6 +973,12 @@ int gcge_port_solve(int n, const int* a_rp, const int* a_ci, const double* a_v, 
   free(w->unlock);
   free(w->res);
   free(w->Bx);
+  free(w->a32);
+  free(w->b32);
+  free(w->f_r);
+  free(w->f_x);
+  free(w->f_p);
+  free(w->f_w);
   return 0;
 }
 

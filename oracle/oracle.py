@@ -33,7 +33,7 @@ class PortPara(C.Structure):
                 ("orth_zero_tol", C.c_double), ("reorth_tol", C.c_double),
                 ("scbgs_reorth_tol", C.c_double), ("multi_tol_for_lock", C.c_double),
                 ("use_shift", C.c_int), ("if_shift", C.c_int), ("eval_sm", C.c_int),
-                ("shift", C.c_double)]
+                ("shift", C.c_double), ("mixed", C.c_int)]
 
 
 def build_port(force: bool = False) -> str:

@@ -160,16 +160,19 @@ def test_block_cg_heavy_rows(cuda_lib, fp32):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_solve_wide_block_power_law_graph(cuda_lib, precision):
-    """Block size 36 (above the 32 columns of the row-interleaved FP32 blocks, so
-    the mixed solve runs the FP32 column block CG) on a shifted power-law graph
-    with 117 heavy rows, against the oracle port."""
+@pytest.mark.parametrize("nev,bs", [(16, 10), (40, 36)])
+def test_solve_hub_localised_power_law_graph(cuda_lib, precision, nev, bs):
+    """A shifted power-law graph (shift 100, 117 heavy rows) whose lowest
+    eigenvectors sit on hub nodes, against the oracle port: block size 10 (the
+    mixed solve on row-interleaved FP32 blocks) and 36 (above their 32 columns:
+    the FP32 column block CG).  The mixed W step hands the FP32 correction
+    alone to the orthogonalisation; with w0 + e the mixed solve broke down on
+    this problem (spurious eigenvalues near 1e-6)."""
     from gcge_old_gb300 import solver as S
     A, B, _ = M.chung_lu(5000, seed=2, shift=100.0)
     assert (np.diff(A.rowptr) > 64).sum() > 100
-    nev = 40
     x0 = M.initial_block(A.n, nev, seed=3)
-    kw = dict(ev_tol=1e-8, ev_max_it=150, block_size=36)
+    kw = dict(ev_tol=1e-8, ev_max_it=150, block_size=bs)
     ev, vec, st = S.solve(A, B, nev, x0, precision=precision, **kw)
     ref = O.port_solve(A, B, nev, x0, O.default_para(nev, **kw), threads=8)
     assert np.max(np.abs(ev - ref["eval"]) / np.abs(ref["eval"])) < 1e-9

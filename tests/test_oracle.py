@@ -69,6 +69,24 @@ def test_reference_vs_port_fresh_seed():
     assert ref["iters"] == port["iters"]
 
 
+def test_port_mixed_w_step_hub_localised_spectrum():
+    """The port's emulation of the CUDA solver's mixed W step (FP32 block CG on
+    the FP64 residual, W = the FP32 correction) converges like the FP64 solve
+    on a shifted power-law graph whose lowest eigenvectors sit on hub nodes
+    (handing w0 + e instead of e to the orthogonalisation lost the basis's
+    B-orthonormality there and gave spurious eigenvalues near 1e-6)."""
+    A, B, _ = M.chung_lu(5000, seed=2, shift=100.0)
+    nev = 16
+    x0 = M.initial_block(A.n, nev, seed=3)
+    para = dict(ev_tol=1e-8, ev_max_it=150, block_size=10)
+    f64 = O.port_solve(A, B, nev, x0, O.default_para(nev, **para), threads=4)
+    mix = O.port_solve(A, B, nev, x0, O.default_para(nev, mixed=1, **para), threads=4)
+    assert f64["iters"] < 60 and abs(mix["iters"] - f64["iters"]) <= 5
+    np.testing.assert_allclose(mix["eval"], f64["eval"], rtol=1e-10)
+    crit = O.true_residuals(A, B, mix["eval"], mix["evec"]) * mix["eval"] / np.maximum(1, mix["eval"])
+    assert crit.max() < 1.5e-8
+
+
 def test_port_bounded_sample():
     """max_outer bounds the outer loop (used for the timed CPU sample)."""
     A = M.laplace2d(40)
