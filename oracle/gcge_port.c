@@ -832,6 +832,7 @@ void gcge_port_default_para(port_para* p, int nev) {
   p->if_shift = 0;
   p->eval_sm = 0;
   p->shift = 0.0;
+  p->mixed = 0;
 }
 
 /* Solve A x = lambda B x for the nev smallest pairs from the initial block x0
