@@ -296,10 +296,6 @@ static ColList<double> cols(const std::vector<double*>& v, int s, int e) {
   for (int i = 0; i < e - s; i++) c.p[i] = v[s + i];
   return c;
 }
-// offset (floats, 8 KB + 256 B) between the row-interleaved FP32 blocks of the
-// mixed block CG
-constexpr size_t kRowsPad = 2112;
-
 static ColList<float> colsf(const std::vector<float*>& v, int s, int e) {
   ColList<float> c;
   for (int i = 0; i < e - s; i++) c.p[i] = v[s + i];
@@ -627,7 +623,7 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
     CHK(mat_ensure_f32(s->A->m, s->st));
     // four column blocks of the block CG, wide enough for the row-interleaved
     // layout (block size rounded up to 4)
-    const size_t f32n = (size_t)s->ldn * 4 * gcge::bcg_rows_width(s->bs) + 4 * kRowsPad;
+    const size_t f32n = (size_t)s->ldn * 4 * gcge::bcg_rows_width(s->bs);
     CU(cudaMalloc(&s->pool32, sizeof(float) * f32n));
     CU(cudaMemsetAsync(s->pool32, 0, sizeof(float) * f32n, s->st));
     float* f = s->pool32;
@@ -1093,10 +1089,7 @@ static int compute_w(Solver* s) {
     KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
     if (wl <= 32) {
       // row-interleaved FP32 vectors: one contiguous row per SpMM gather
-      // the four blocks start kRowsPad floats apart beyond their size, so that
-      // the streams a row kernel reads together do not start on the same
-      // DRAM channel
-      const size_t blk = (size_t)s->ldn * gcge::bcg_rows_width(wl) + kRowsPad;
+      const size_t blk = (size_t)s->ldn * gcge::bcg_rows_width(wl);
       float* Rr = s->pool32;
       float* Xr = Rr + blk;
       float* Pr = Xr + blk;
