@@ -515,41 +515,62 @@ __global__ void __launch_bounds__(kT, KW <= 12 ? kApBlocks12 : 1) k_rows_ap(int 
   block_sum_cols<KW>(dot, len, sh, partial);
 }
 
-// x += alpha p, r -= alpha w and partial r.r for the active columns
+// x += alpha p, r -= alpha w and partial r.r for the active columns.  The
+// blocks are walked as flat float4 arrays (n * KW/4 of them): consecutive
+// threads take consecutive float4s, so every load instruction of a warp reads
+// 512 contiguous bytes (a thread per 48-byte row touched twice the sectors it
+// used and its 4 streams thrashed L1).  The thread count of the grid is a
+// multiple of G = KW/4, so a thread keeps one group of 4 columns (4q..4q+3)
+// for all its float4s.  Block partials per column: the threads of a group in
+// thread order, a warp per column, fixed shuffle tree.
 template <int KW>
-__global__ void __launch_bounds__(kT) k_rows_update(int n, float* __restrict__ X, float* __restrict__ R,
-                                                    const float* __restrict__ P,
-                                                    const float* __restrict__ W, int len,
-                                                    BcgScalars s, double* __restrict__ partial) {
-  __shared__ double sh[(kT / 32) * 32];
+__global__ void __launch_bounds__(kT, 4) k_rows_update(int n, float* __restrict__ X,
+                                                       float* __restrict__ R,
+                                                       const float* __restrict__ P,
+                                                       const float* __restrict__ W, int len,
+                                                       BcgScalars s, double* __restrict__ partial) {
+  constexpr int G = KW / 4;
+  __shared__ double sacc[4][kT];
   if (*s.nu == 0) return;
-  bool on[KW];
-  float alpha[KW];
+  const int f0 = blockIdx.x * kT + threadIdx.x;  // < gridDim.x * kT, which fits an int
+  const int q = f0 % G;
+  bool on[4];
+  float alpha[4];
 #pragma unroll
-  for (int c = 0; c < KW; c++) {
-    on[c] = s.mask[c] != 0;
-    alpha[c] = on[c] ? s.acolf[c] : 0.f;
+  for (int j = 0; j < 4; j++) {
+    on[j] = s.mask[4 * q + j] != 0;
+    alpha[j] = on[j] ? s.acolf[4 * q + j] : 0.f;
   }
-  float acc[KW];
-#pragma unroll
-  for (int c = 0; c < KW; c++) acc[c] = 0.f;
-  for (int r = blockIdx.x * kT + threadIdx.x; r < n; r += gridDim.x * kT) {
-    float xv[KW], rv[KW], pv[KW], wv[KW];
-    load_row<KW>(X, r, xv);
-    load_row<KW>(R, r, rv);
-    load_row<KW>(P, r, pv);
-    load_row<KW>(W, r, wv);
-#pragma unroll
-    for (int c = 0; c < KW; c++)
-      if (on[c]) {
-        xv[c] = fmaf(alpha[c], pv[c], xv[c]);
-        rv[c] = fmaf(-alpha[c], wv[c], rv[c]);
-        acc[c] = fmaf(rv[c], rv[c], acc[c]);
-      }
-    store_row<KW>(X, r, xv);
-    store_row<KW>(R, r, rv);
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const long long n4 = (long long)n * G, stride = (long long)gridDim.x * kT;
+  float4* X4 = reinterpret_cast<float4*>(X);
+  float4* R4 = reinterpret_cast<float4*>(R);
+  const float4* P4 = reinterpret_cast<const float4*>(P);
+  const float4* W4 = reinterpret_cast<const float4*>(W);
+  for (long long f = f0; f < n4; f += stride) {  // f % G == q: stride is a multiple of G
+    float4 x = X4[f], r = R4[f];
+    const float4 p = __ldg(P4 + f), w = __ldg(W4 + f);
+    if (on[0]) { x.x = fmaf(alpha[0], p.x, x.x); r.x = fmaf(-alpha[0], w.x, r.x); acc[0] = fmaf(r.x, r.x, acc[0]); }
+    if (on[1]) { x.y = fmaf(alpha[1], p.y, x.y); r.y = fmaf(-alpha[1], w.y, r.y); acc[1] = fmaf(r.y, r.y, acc[1]); }
+    if (on[2]) { x.z = fmaf(alpha[2], p.z, x.z); r.z = fmaf(-alpha[2], w.z, r.z); acc[2] = fmaf(r.z, r.z, acc[2]); }
+    if (on[3]) { x.w = fmaf(alpha[3], p.w, x.w); r.w = fmaf(-alpha[3], w.w, r.w); acc[3] = fmaf(r.w, r.w, acc[3]); }
+    X4[f] = x;
+    R4[f] = r;
   }
-  block_sum_cols<KW>(acc, len, sh, partial);
+#pragma unroll
+  for (int j = 0; j < 4; j++) sacc[j][threadIdx.x] = (double)acc[j];
+  __syncthreads();
+  // thread t of this block has group (blockIdx.x * kT + t) % G
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int b0 = (blockIdx.x * kT) % G;
+  for (int c = wid; c < len; c += kT / 32) {
+    const int g = c >> 2, j = c & 3;
+    const int t0 = (g - b0 + G) % G;  // first thread of group g
+    double v = 0.0;
+    for (int t = t0 + G * lane; t < kT; t += 32 * G) v += sacc[j][t];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) partial[(size_t)c * gridDim.x + blockIdx.x] = v;
+  }
 }
 
 // column sums of the per-block partials: warp w adds column w (lanes take
@@ -690,6 +711,13 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
   // the latency-bound A p kernel gets kApBlocks12 up to 12 columns
   const int nb = min((n + kT - 1) / kT, (KW <= 16 ? 4 : 2) * 152);
   const int nba = KW <= 12 ? min((n + kT - 1) / kT, kApBlocks12 * 152) : nb;
+  // the update kernel: flat float4s, four CTAs per SM (its loop is unrolled
+  // into 56-64 registers; at six CTAs it spilled), a multiple of KW/4 CTAs
+  const long long n4 = (long long)n * (KW / 4);
+  int nbu = (int)((n4 + kT - 1) / kT);
+  if (nbu > 4 * 152) nbu = 4 * 152;
+  nbu = nbu / (KW / 4) * (KW / 4);
+  if (nbu < KW / 4) nbu = KW / 4;
   int nl = 0;
   if (hv) heavy_rows_f32(*M, val, X, KW, nullptr, st);
   k_rows_init<KW><<<nb, kT, 0, st>>>(n, rp, ci, val, X, R, len, partial, hidx,
@@ -707,8 +735,8 @@ int rows_run(const int* rp, const int* ci, const float* val, int n, float* R, fl
       k_rows_ap<KW><<<nba, kT, 0, st>>>(n, rp, ci, val, P, W, len, s, partial, hidx,
                                         hv ? M->hch : nullptr, hv ? M->cb32 : nullptr);
       k_rows_alpha<<<1, 1024, 0, st>>>(partial, nba, len, s);
-      k_rows_update<KW><<<nb, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
-      k_rows_step<<<1, 1024, 0, st>>>(partial, nb, len, s, rate, j);
+      k_rows_update<KW><<<nbu, kT, 0, st>>>(n, X, R, P, W, len, s, partial);
+      k_rows_step<<<1, 1024, 0, st>>>(partial, nbu, len, s, rate, j);
       nl += 5;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
