@@ -37,6 +37,23 @@ def test_port_matches_reference_golden(name):
     assert tr.max() < 10 * max(tr_ref.max(), 1e-14)
 
 
+@pytest.mark.parametrize("name", [n for n in GOLDEN_NAMES if "m128" not in n and "3x3" not in n])
+def test_port_mixed_w_step_matches_reference_golden(name):
+    """The port's mixed W step (FP32 block CG, W = the FP32 correction) reaches the
+    reference's eigenvalues and residual bound on the golden fixtures."""
+    A, B, nev, x0, d = load_golden(name)
+    para = para_for(nev, d["flags_dict"])
+    para.mixed = 1
+    para.ev_max_it = max(para.ev_max_it, 2 * int(d["iters"]) + 10)
+    r = O.port_solve(A, B, nev, x0, para, threads=2)
+    rel = np.max(np.abs(r["eval"] - d["eval"]) / np.abs(d["eval"]))
+    assert rel < 1e-9, rel
+    assert r["iters"] <= int(d["iters"]) + 5
+    tr = O.true_residuals(A, B, r["eval"], r["evec"])
+    tr_ref = O.true_residuals(A, B, d["eval"], d["evec"])
+    assert tr.max() < 10 * max(tr_ref.max(), 1e-14)
+
+
 def test_port_matches_reference_golden_headline_cpu_case():
     """128 x 128 Laplacian, nev 20, block 20, tol 1e-13 (the CPU-runnable case)."""
     A, B, nev, x0, d = load_golden("ref_lap2d_m128_nev20")
