@@ -315,15 +315,17 @@ def reference_iters():
     return None, None
 
 
-def cpu_sample(A, B, nev, x0, threads, fallback_iters):
+def cpu_sample(A, B, nev, x0, threads, fallback_iters, full_size=True,
+               fallback_src="GPU FP64 iteration count"):
     """Oracle port on the host: start phase + one GCG iteration, extrapolated
-    to the full iteration count."""
+    to the full iteration count (the reference's own count on the full-size
+    workload, else fallback_iters)."""
     from oracle import oracle as O
     p = O.default_para(nev, ev_tol=1e-10, ev_max_it=1000)
     r = O.port_solve(A, B, nev, x0, p, max_outer=1, threads=threads)
-    iters, src = reference_iters()
+    iters, src = reference_iters() if full_size else (None, None)
     if iters is None:
-        iters, src = fallback_iters, "GPU FP64 iteration count"
+        iters, src = fallback_iters, fallback_src
     t_iter = r["t_loop"] / max(1, r["loop_iters"])
     est = r["t_init"] + max(0, iters - 2) * t_iter
     sample = ("oracle port, %d threads: start phase (X orth, RR, [X,W] step) %.2f s + 1 GCG iteration "
@@ -341,7 +343,8 @@ def run_reference_arm(args):
     wall = []
     sample = ""
     for it in range(args.warmup + args.steps):
-        est, w, sample = cpu_sample(A, B, nev, x0, threads, 60)
+        est, w, sample = cpu_sample(A, B, nev, x0, threads, 60, full_size=not args.small,
+                                    fallback_src="an assumed 60 iterations")
         if it >= args.warmup:
             vals.append(est)
             wall.append(w)
@@ -697,7 +700,8 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        est, wall, sample = cpu_sample(A, B, nev, x0, threads, st_fp64[-1]["num_iter"])
+        est, wall, sample = cpu_sample(A, B, nev, x0, threads, st_fp64[-1]["num_iter"],
+                                       full_size=not args.small)
         cpu = {"value": est, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
 
     traffic = None
