@@ -104,7 +104,7 @@ int GCGE_CUDA_EigGradCSR2(const GCGE_CUDA_MAT* M, double* const* X, double* cons
  * nrow, ncol, nnz, rowptr[nrow+1], col[nnz], val[nnz], whitespace separated,
  * 0-based; written with 17 significant digits, so it reads back bit-exact.
  * Binary: PETSc's Mat binary format (what the reference's PETSc app loads,
- * test/data/*.petsc.bin): big-endian int32 classid 1211216, rows, cols, nnz,
+ * the test/data files ending in .petsc.bin): big-endian int32 classid 1211216, rows, cols, nnz,
  * row lengths, col, then big-endian float64 val; 32-bit indices.
  * CSR_ReadFile picks the format from the first four bytes, checks the
  * structure (row pointers 0..nnz without decrease, columns in range) and
