@@ -12,7 +12,9 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address once with cudaGetSymbolAddress and caches it per
-// device.  That first call should come before any stream capture starts.
+// device.  That first call should come before any stream capture starts.  A
+// cudaDeviceReset unloads the module, so the cached address is stale after
+// one: the entry point is not for use on a device after a reset.
 //
 // Sharing: every call, from every thread, uses the same array, and the array
 // keeps whatever the last call left in it.  Each call overwrites all the
@@ -73,13 +75,20 @@ extern "C" int GCGE_CUDA_MultiVecInnerProdNoAlloc(double* const* V, int k1, doub
   double* partials = nullptr;
   const int rc = partials_for_current_device(&partials);
   if (rc != GCGE_CUDA_OK) return rc;
+  // an error pending from earlier, unrelated work is reported as such and
+  // left pending for the caller (peek, not get)
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess)
+    return gcge_record_error(GCGE_CUDA_ERR_CUDA,
+                             "MultiVecInnerProdNoAlloc: a CUDA error is pending from earlier work; "
+                             "nothing launched");
   ColList<double> Vc, Wc;
   for (int i = 0; i < k1; i++) Vc.p[i] = V[i];
   for (int j = 0; j < k2; j++) Wc.p[j] = W[j];
   // k1 * k2 <= 4096 selects the narrow Gram kernel, whose partials take at
   // most kRowBlocks * k1 * k2 doubles.
   gcge::gram_f64(Vc, k1, Wc, k2, n, a, lda, sym != 0, partials, (cudaStream_t)stream);
-  if (cudaGetLastError() != cudaSuccess)
+  if (cudaPeekAtLastError() != cudaSuccess)
     return gcge_record_error(GCGE_CUDA_ERR_CUDA, "MultiVecInnerProdNoAlloc: launch failed");
   return GCGE_CUDA_OK;
 }

@@ -238,6 +238,18 @@ struct Para {
   int if_shift = 0;
   double shift = 0.0;
   int eval_type = 0;  // 0 "sa" (smallest algebraic), 1 "sm" (smallest magnitude)
+  // convergence criterion (GCGE_PARA conv_type, src/gcge_eigsol.c:713-721):
+  // 0 "R" divides the residual by max(1, |lambda|), 1 "O" by
+  // (conv_omega_norm + |lambda|), 2 "A" leaves it absolute
+  int conv_type = 0;
+  double conv_omega_norm = 0.0;
+  // W block of the FP64 block CG: 0 the reference's in-place iterate w0 + e,
+  // 1 the correction e alone (what the mixed form always hands over)
+  int w_form = 0;
+  // reports on stdout in the reference's format (GCGE_PrintFinalInfo,
+  // src/gcge_para.c:577-699); off unless asked for
+  int print_result = 0, print_conv = 0, print_final_part_time = 0, print_eval = 0,
+      print_para = 0;
 };
 
 // ------------------------------------------------------------------ solver
@@ -384,6 +396,21 @@ static int set_param(Para& p, const char* name, double v) {
   else if (k == "use_shift") p.use_shift = (int)v;
   else if (k == "if_shift") p.if_shift = (int)v;
   else if (k == "shift") p.shift = v;
+  else if (k == "conv_type") {
+    if (v != 0.0 && v != 1.0 && v != 2.0)
+      return set_err(GCGE_CUDA_ERR_ARG, "conv_type: 0 (R), 1 (O) or 2 (A)");
+    p.conv_type = (int)v;
+  }
+  else if (k == "conv_omega_norm") p.conv_omega_norm = v;
+  else if (k == "w_form") {
+    if (v != 0.0 && v != 1.0) return set_err(GCGE_CUDA_ERR_ARG, "w_form: 0 (reference) or 1 (correction)");
+    p.w_form = (int)v;
+  }
+  else if (k == "print_result") p.print_result = (int)v;
+  else if (k == "print_conv") p.print_conv = (int)v;
+  else if (k == "print_final_part_time") p.print_final_part_time = (int)v;
+  else if (k == "print_eval") p.print_eval = (int)v;
+  else if (k == "print_para") p.print_para = (int)v;
   else if (k == "eval_type") {
     if (v != 0.0 && v != 1.0) return set_err(GCGE_CUDA_ERR_ARG, "eval_type: 0 (sa) or 1 (sm)");
     p.eval_type = (int)v;
@@ -403,56 +430,127 @@ extern "C" int GCGE_CUDA_SOLVER_SetParamDouble(GCGE_CUDA_SOLVER* s, const char* 
   return set_param(s->para, name, v);
 }
 
-// Same flag names as GCGE_PARA_SetFromCommandLine (src/gcge_para.c:128-407),
-// unknown flags skipped as there.  -gcge_cg_rate is read as a real number
-// (the reference reads it with atoi, :287, which turns 1e-2 into 0).
+// The flags of GCGE_PARA_SetFromCommandLine (src/gcge_para.c:128-407).  A
+// -gcge_* flag is either honoured, accepted because it has no effect on one
+// GPU (MPI layout options) or none in the reference either (opt_rr_eig_partly
+// is overwritten with 1 by GCGE_ComputeSubspaceMatrix, src/gcge_rayleighritz.c:175;
+// multi_tol feeds only the unused GCGE_CheckEvalMultiplicity), accepted only
+// with the value whose behaviour this solver implements, or rejected with
+// GCGE_CUDA_ERR_ARG: no flag is dropped silently.  -gcge_cg_rate is read as a
+// real number (the reference reads it with atoi, :287, which turns 1e-2 into 0).
+// Arguments that do not start with -gcge_ are skipped, as there.
+static void print_usage() {
+  printf("GCGE CUDA solver flags (values in brackets: the only value accepted):\n"
+         "  -gcge_nev <i> -gcge_ev_max_it <i> -gcge_block_size <i> -gcge_num_init_evec <i>\n"
+         "  -gcge_ev_tol <d> -gcge_conv_type R|O|A -gcge_conv_omega_norm <d> -gcge_eval_type sa|sm\n"
+         "  -gcge_cg_max_it <i> -gcge_cg_rate <d> -gcge_max_reorth_time <i> -gcge_orth_zero_tol <d>\n"
+         "  -gcge_reorth_tol <d> -gcge_scbgs_reorth_tol <d> -gcge_multi_tol_for_lock <d>\n"
+         "  -gcge_use_shift <i> -gcge_print_result|print_conv|print_final_part_time|print_eval|"
+         "print_para <i>\n"
+         "  -gcge_orth_type [B] -gcge_w_orth_type [multi] -gcge_p_orth_type [multi] "
+         "-gcge_x_orth_type [bgs]\n"
+         "  -gcge_if_use_bcg [1] -gcge_if_use_cg [1] -gcge_use_bcg_continuous [0] -gcge_if_lobgcg [0]\n"
+         "  -gcge_x_orth_block_size [0] -gcge_w_orth_block_size [0] -gcge_max_direct_orth_length [1]\n"
+         "  -gcge_scbgs_wself_max_reorth_time [1]\n"
+         "  no effect here: -gcge_opt_bcast -gcge_opt_allgatherv -gcge_min_nev_each_proc "
+         "-gcge_partition_type -gcge_opt_rr_eig_partly -gcge_multi_tol -gcge_print_cg_error "
+         "-gcge_print_part_time -gcge_print_orth_zero -gcge_print_split\n"
+         "  this solver: -gcge_precision fp64|mixed -gcge_gemm ozaki|fp64 -gcge_w_form "
+         "reference|correction -gcge_print_level <i>\n");
+}
+
 extern "C" int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* s, int argc, char** argv) {
   if (!s) return set_err(GCGE_CUDA_ERR_ARG, "SetFromCommandLine: null solver");
+  if (s->setup_done)
+    return set_err(GCGE_CUDA_ERR_STATE, "SetFromCommandLine: parameters are fixed after Setup");
+  if (argc > 0 && !argv) return set_err(GCGE_CUDA_ERR_ARG, "SetFromCommandLine: null argv");
   static const char* ints[] = {"-gcge_nev", "-gcge_ev_max_it", "-gcge_block_size",
                                "-gcge_num_init_evec", "-gcge_cg_max_it", "-gcge_max_reorth_time",
-                               "-gcge_print_level", "-gcge_use_shift"};
+                               "-gcge_print_level", "-gcge_use_shift", "-gcge_print_result",
+                               "-gcge_print_conv", "-gcge_print_final_part_time",
+                               "-gcge_print_eval", "-gcge_print_para"};
   static const char* dbls[] = {"-gcge_ev_tol", "-gcge_cg_rate", "-gcge_orth_zero_tol",
                                "-gcge_reorth_tol", "-gcge_scbgs_reorth_tol",
-                               "-gcge_multi_tol_for_lock"};
-  int i = 0;
-  while (i < argc) {
+                               "-gcge_multi_tol_for_lock", "-gcge_conv_omega_norm"};
+  static const char* no_effect[] = {"-gcge_opt_bcast", "-gcge_opt_allgatherv",
+                                    "-gcge_min_nev_each_proc", "-gcge_partition_type",
+                                    "-gcge_opt_rr_eig_partly", "-gcge_multi_tol",
+                                    "-gcge_print_cg_error", "-gcge_print_part_time",
+                                    "-gcge_print_orth_zero", "-gcge_print_split"};
+  static const struct { const char* flag; const char* value; bool num; } fixed[] = {
+      {"-gcge_orth_type", "B", false},        {"-gcge_w_orth_type", "multi", false},
+      {"-gcge_p_orth_type", "multi", false},  {"-gcge_x_orth_type", "bgs", false},
+      {"-gcge_if_use_bcg", "1", true},        {"-gcge_if_use_cg", "1", true},
+      {"-gcge_use_bcg_continuous", "0", true}, {"-gcge_if_lobgcg", "0", true},
+      {"-gcge_x_orth_block_size", "0", true}, {"-gcge_w_orth_block_size", "0", true},
+      {"-gcge_max_direct_orth_length", "1", true},
+      {"-gcge_scbgs_wself_max_reorth_time", "1", true}};
+  Para p = s->para;  // committed only when every flag is valid
+  for (int i = 0; i < argc; i++) {
     const char* a = argv[i];
-    bool hit = false;
-    if (a && i + 1 < argc) {
-      for (const char* f : ints)
-        if (!strcmp(a, f)) {
-          CHK(set_param(s->para, f, (double)atoi(argv[i + 1])));
-          hit = true;
-        }
-      for (const char* f : dbls)
-        if (!strcmp(a, f)) {
-          CHK(set_param(s->para, f, atof(argv[i + 1])));
-          hit = true;
-        }
-      if (!strcmp(a, "-gcge_gemm")) {
-        const char* v = argv[i + 1];
-        if (!strcmp(v, "ozaki") || !strcmp(v, "1")) s->para.gemm = 1;
-        else if (!strcmp(v, "fp64") || !strcmp(v, "0")) s->para.gemm = 0;
-        else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_gemm: fp64 or ozaki");
-        hit = true;
-      }
-      if (!strcmp(a, "-gcge_eval_type")) {  // src/gcge_para.c:184-187
-        const char* v = argv[i + 1];
-        if (!strcmp(v, "sa")) s->para.eval_type = 0;
-        else if (!strcmp(v, "sm")) s->para.eval_type = 1;
-        else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_eval_type: sa or sm");
-        hit = true;
-      }
-      if (!strcmp(a, "-gcge_precision")) {
-        const char* v = argv[i + 1];
-        if (!strcmp(v, "mixed") || !strcmp(v, "1")) s->para.precision = 1;
-        else if (!strcmp(v, "fp64") || !strcmp(v, "0")) s->para.precision = 0;
-        else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_precision: fp64 or mixed");
-        hit = true;
-      }
+    if (!a || strncmp(a, "-gcge_", 6) != 0) continue;
+    if (!strcmp(a, "-gcge_help")) {
+      print_usage();
+      break;
     }
-    i += hit ? 2 : 1;
+    if (i + 1 >= argc || !argv[i + 1])
+      return set_err(GCGE_CUDA_ERR_ARG, "%s: missing value", a);
+    const char* v = argv[++i];
+    bool hit = false;
+    for (const char* f : ints)
+      if (!strcmp(a, f)) {
+        CHK(set_param(p, f, (double)atoi(v)));
+        hit = true;
+      }
+    for (const char* f : dbls)
+      if (!strcmp(a, f)) {
+        CHK(set_param(p, f, atof(v)));
+        hit = true;
+      }
+    for (const char* f : no_effect)
+      if (!strcmp(a, f)) hit = true;
+    for (const auto& f : fixed)
+      if (!strcmp(a, f.flag)) {
+        const bool ok = f.num ? atoi(v) == atoi(f.value) : !strcmp(v, f.value);
+        if (!ok)
+          return set_err(GCGE_CUDA_ERR_ARG, "%s %s is not supported by the CUDA solver (only %s)",
+                         a, v, f.value);
+        hit = true;
+      }
+    if (!strcmp(a, "-gcge_gemm")) {
+      if (!strcmp(v, "ozaki") || !strcmp(v, "1")) p.gemm = 1;
+      else if (!strcmp(v, "fp64") || !strcmp(v, "0")) p.gemm = 0;
+      else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_gemm: fp64 or ozaki");
+      hit = true;
+    }
+    if (!strcmp(a, "-gcge_eval_type")) {  // src/gcge_para.c:184-187
+      if (!strcmp(v, "sa")) p.eval_type = 0;
+      else if (!strcmp(v, "sm")) p.eval_type = 1;
+      else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_eval_type: sa or sm");
+      hit = true;
+    }
+    if (!strcmp(a, "-gcge_conv_type")) {  // src/gcge_para.c:179-182, used at src/gcge_eigsol.c:713-721
+      if (!strcmp(v, "R")) p.conv_type = 0;
+      else if (!strcmp(v, "O")) p.conv_type = 1;
+      else if (!strcmp(v, "A")) p.conv_type = 2;
+      else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_conv_type: R, O or A");
+      hit = true;
+    }
+    if (!strcmp(a, "-gcge_precision")) {
+      if (!strcmp(v, "mixed") || !strcmp(v, "1")) p.precision = 1;
+      else if (!strcmp(v, "fp64") || !strcmp(v, "0")) p.precision = 0;
+      else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_precision: fp64 or mixed");
+      hit = true;
+    }
+    if (!strcmp(a, "-gcge_w_form")) {
+      if (!strcmp(v, "reference") || !strcmp(v, "0")) p.w_form = 0;
+      else if (!strcmp(v, "correction") || !strcmp(v, "1")) p.w_form = 1;
+      else return set_err(GCGE_CUDA_ERR_ARG, "-gcge_w_form: reference or correction");
+      hit = true;
+    }
+    if (!hit) return set_err(GCGE_CUDA_ERR_ARG, "unknown flag %s", a);
   }
+  s->para = p;
   return GCGE_CUDA_OK;
 }
 
@@ -1069,6 +1167,13 @@ static int compute_w(Solver* s) {
     return GCGE_CUDA_OK;
   }
   if (s->para.precision == 0) {
+    if (s->para.w_form == 1) {
+      // the correction form (see the mixed branch below) in FP64
+      ColList<double> AW = cols(s->evec, 0, wl);
+      KL(gcge::spmm_f64(*Aop, Wc, AW, wl, s->st));
+      KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
+      for (int i = 0; i < wl; i++) CU(cudaMemsetAsync(Wc.p[i], 0, sizeof(double) * s->n, s->st));
+    }
     steps = gcge::bcg_run<double>(Aop->rp, Aop->ci, Aop->v, s->n, R, Wc,
                                   cols(s->CG_p, 0, wl), cols(s->evec, 0, wl), wl,
                                   s->para.cg_max_it, s->para.cg_rate, s->bcg, s->partial, s->st,
@@ -1163,8 +1268,9 @@ static int compute_p(Solver* s) {
   return GCGE_CUDA_OK;
 }
 
-// GCGE_CheckConvergence (src/gcge_eigsol.c:663-887), "R" criterion.  The
-// residuals are computed on the device in chunks; the lock logic runs here.
+// GCGE_CheckConvergence (src/gcge_eigsol.c:663-887) with the "R", "O" and
+// absolute criteria (:704-721).  The residuals are computed on the device in
+// chunks; the lock logic runs here.
 static int check_convergence(Solver* s) {
   const int nev = s->nev;
   std::vector<int>& unlock = s->unlock;
@@ -1178,6 +1284,8 @@ static int check_convergence(Solver* s) {
   const int chunk = 16;
   std::vector<double> r2(chunk), x2(chunk);
   bool stop = false;
+  double max_res = 0.0, min_res = 0.0;
+  int max_ind = 0, min_ind = 0;
   for (int c0 = start; c0 < nev && !stop; c0 += chunk) {
     const int k = (nev - c0 < chunk) ? nev - c0 : chunk;
     KL(gcge::residual_f64(s->A->m, Bptr(s), cols(s->evec, c0, c0 + k), s->d_eval + c0, k,
@@ -1190,7 +1298,8 @@ static int check_convergence(Solver* s) {
       const double rn = sqrt(r2[idx - c0]), en = sqrt(x2[idx - c0]);
       double r = rn / en;
       const double ab = r;
-      r /= (1.0 > fabs(eval[idx]) ? 1.0 : fabs(eval[idx]));
+      if (p.conv_type == 0) r /= (1.0 > fabs(eval[idx]) ? 1.0 : fabs(eval[idx]));
+      else if (p.conv_type == 1) r /= (p.conv_omega_norm + fabs(eval[idx]));
       res[idx] = r;
       if (r < ev_tol && ab < 1e-2) {
         if (idx > 0) {
@@ -1220,6 +1329,12 @@ static int check_convergence(Solver* s) {
           unlock[nu++] = idx;
         }
       }
+      if (idx == start) {
+        max_res = min_res = r;
+      } else {
+        if (r > max_res) { max_res = r; max_ind = idx; }
+        if (r < min_res) { min_res = r; min_ind = idx; }
+      }
       if (idx - max_conv_idx > 9) {
         stop = true;
         break;
@@ -1248,6 +1363,103 @@ static int check_convergence(Solver* s) {
   if (p.print_level > 0)
     fprintf(stderr, "[gcge-cuda] iter %d conv %d unconv_bs %d res[0]=%.3e\n", s->num_iter, ncc, nu,
             res[0]);
+  // per-iteration report in the layout of GCGE_PrintIterationInfo
+  // (src/gcge_para.c:461-514), whose iteration label is the count before this check
+  const int it = s->num_iter - 1;
+  if (p.print_conv == 1)
+    printf("num_conv_continuous(%3d) = %3d; max_res(%3d) = %e; min_res(%3d) = %e;\n", it, ncc, it,
+           max_res, it, min_res);
+  if (p.print_eval == 1) {
+    const char* ct = p.conv_type == 0 ? "relative_res" : p.conv_type == 1 ? "omega_res" : "abosolute_res";
+    for (int i = 0; i < nev; i++) {
+      printf("eval(%d,%3d) = %20.15e ; %s(%d,%3d) =  %20.15e ;", it, i + 1, eval[i], ct, it, i + 1,
+             res[i]);
+      if (res[i] < ev_tol) printf(" (converged)\n");
+      else if (i == max_ind) printf(" (max)\n");
+      else if (i == min_ind) printf(" (min)\n");
+      else printf("\n");
+    }
+  }
+  if (p.print_conv == 1 || p.print_eval == 1) fflush(stdout);
+  return GCGE_CUDA_OK;
+}
+
+// Final report in the layout of GCGE_PrintFinalInfo (src/gcge_para.c:577-699):
+// the eigenvalue / residual table, the iteration summary and the phase times
+// (seconds of wall time here; the reference's are CPU user time).  The P step
+// is timed as one phase (its orthonormalisation runs inside it): p_orth
+// reads 0 and p_axpy holds the whole P step.
+static void print_final_info(const Solver* s) {
+  const Para& p = s->para;
+  const GCGE_CUDA_STATS& t = s->stats;
+  const double total = t.t_x_orth + t.t_x_axpy + t.t_p + t.t_w_line + t.t_w_orth + t.t_rr_mat +
+                       t.t_rr_eig + t.t_conv;
+  if (p.print_result) {
+    printf("\nFinal eigenvalues and residual information:\n");
+    printf("\n            eigenvalue           ");
+    if (p.conv_type == 0) printf("relative residual\n\n");
+    else if (p.conv_type == 1) printf("omega residual\n\n");
+    else printf("abosolute residual\n\n");
+    for (int i = 0; i < s->nev; i++) {
+      printf("%5d  %20.15e  %20.15e ", i + 1, s->eval[i], s->res[i]);
+      printf(s->res[i] < p.ev_tol ? " (converged)\n" : "\n");
+    }
+  }
+  if (p.print_conv == 1) {
+    printf("\nTotal gcg iteration: %d, total time: %.2lf. ", s->num_iter, total);
+    if (s->num_conv_continuous == s->nev) printf("All %d eigenpairs converged! ", s->nev);
+    else printf("%d converged, %d unconverged. ", s->num_conv_continuous, s->nev - s->num_conv_continuous);
+  }
+  if (p.print_final_part_time == 1) {
+    printf("Use 1 process. block_size: %d", s->bs);
+    printf("\nDetail time in total gcg iteration:\n"
+           "Section Name        x_orth       x_axpy       p_orth       p_axpy   check_conv\n"
+           "Section Time  %12.2lf %12.2lf %12.2lf %12.2lf %12.2lf\n",
+           t.t_x_orth, t.t_x_axpy, 0.0, t.t_p, t.t_conv);
+    if (total >= 1e-10)
+      printf("Section Ratio %11.2lf%% %11.2lf%% %11.2lf%% %11.2lf%% %11.2lf%%\n", 100 * t.t_x_orth / total,
+             100 * t.t_x_axpy / total, 0.0, 100 * t.t_p / total, 100 * t.t_conv / total);
+    printf("Section Name        w_lsol       w_orth       rr_eig       rr_mat\n"
+           "Section Time  %12.2lf %12.2lf %12.2lf %12.2lf\n",
+           t.t_w_line, t.t_w_orth, t.t_rr_eig, t.t_rr_mat);
+    if (total < 1e-10) printf("Total time is less than 1e-10, the percentege is not presented.\n");
+    else
+      printf("Section Ratio %11.2lf%% %11.2lf%% %11.2lf%% %11.2lf%%\n\n", 100 * t.t_w_line / total,
+             100 * t.t_w_orth / total, 100 * t.t_rr_eig / total, 100 * t.t_rr_mat / total);
+  }
+  fflush(stdout);
+}
+
+static void print_para_info(const Solver* s) {
+  const Para& p = s->para;
+  static const char* ct[] = {"R", "O", "A"};
+  printf("GCGE CUDA parameters: nev %d, block_size %d, ev_max_it %d, ev_tol %g, conv_type %s "
+         "(omega norm %g), eval_type %s, cg_max_it %d, cg_rate %g, max_reorth_time %d, "
+         "orth_zero_tol %g, scbgs_reorth_tol %g, multi_tol_for_lock %g, use_shift %d, "
+         "precision %s, w_form %s, products %s\n",
+         s->nev, s->bs, p.ev_max_it, p.ev_tol, ct[p.conv_type], p.conv_omega_norm,
+         p.eval_type ? "sm" : "sa", p.cg_max_it, p.cg_rate, p.max_reorth_time, p.orth_zero_tol,
+         p.scbgs_reorth_tol, p.multi_tol_for_lock, p.use_shift, p.precision ? "mixed" : "fp64",
+         p.w_form ? "correction" : "reference", p.gemm ? "ozaki" : "fp64");
+  fflush(stdout);
+}
+
+static int omega_norm(Solver* s) {
+  const int nev = s->nev;
+  double acc = 0.0;
+  std::vector<double> r2(16), x2(16);
+  for (int c0 = 0; c0 < nev; c0 += 16) {
+    const int k = nev - c0 < 16 ? nev - c0 : 16;
+    // d_eval is zero here: the residual kernel returns ||A x||^2 and ||x||^2
+    KL(gcge::residual_f64(s->A->m, Bptr(s), cols(s->evec, c0, c0 + k), s->d_eval, k, s->d_small,
+                          s->d_small + GCGE_MAXCOLS, s->partial, s->st));
+    CU(cudaMemcpyAsync(r2.data(), s->d_small, sizeof(double) * k, cudaMemcpyDeviceToHost, s->st));
+    CU(cudaMemcpyAsync(x2.data(), s->d_small + GCGE_MAXCOLS, sizeof(double) * k,
+                       cudaMemcpyDeviceToHost, s->st));
+    CHK(sync(s));
+    for (int i = 0; i < k; i++) acc += r2[i] / x2[i];
+  }
+  s->para.conv_omega_norm = sqrt(acc / nev);
   return GCGE_CUDA_OK;
 }
 
@@ -1277,10 +1489,12 @@ extern "C" int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* s) {
     return set_err(GCGE_CUDA_ERR_STATE, "Solve: eigenvalue/eigenvector arrays not set");
   Para& p = s->para;
   const int nev = s->nev, n = s->n;
-  if (p.num_init_evec < nev)
-    return set_err(GCGE_CUDA_ERR_ARG,
-                   "Solve: give the initial block in evec and set num_init_evec = nev");
+  if (p.num_init_evec < 0) return set_err(GCGE_CUDA_ERR_ARG, "Solve: num_init_evec < 0");
+  // the first num_init_evec columns of evec are the given start; the rest are
+  // pseudo-random, as the reference fills them (src/gcge_eigsol.c:134-140)
+  const int n_given = p.num_init_evec < nev ? p.num_init_evec : nev;
   const double t_start = now_s();
+  if (p.print_para) print_para_info(s);
   memset(&s->stats, 0, sizeof(s->stats));
   s->launches = 0;
   s->eval.assign(s->mx, 0.0);
@@ -1301,7 +1515,7 @@ extern "C" int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* s) {
   CU(cudaMemsetAsync(s->d_eval, 0, sizeof(double) * s->mx, s->st));
   CU(cudaMemsetAsync(s->sub_mat, 0, sizeof(double) * (size_t)s->mx * s->mx, s->st));
   CU(cudaMemsetAsync(s->sub_evec, 0, sizeof(double) * (size_t)s->mx * s->mx, s->st));
-  for (int j = 0; j < nev; j++) {
+  for (int j = 0; j < n_given; j++) {
     if (s->evec_dev)
       CU(cudaMemcpyAsync(s->evec[j], s->evec_dev + (size_t)j * n, sizeof(double) * n,
                          cudaMemcpyDeviceToDevice, s->st));
@@ -1309,6 +1523,14 @@ extern "C" int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* s) {
       CU(cudaMemcpyAsync(s->evec[j], s->evec_user + (size_t)j * n, sizeof(double) * n,
                          cudaMemcpyHostToDevice, s->st));
   }
+  if (n_given < nev) {
+    dim3 g((n + 255) / 256, nev - n_given);
+    KL((k_fill_random<<<g, 256, 0, s->st>>>(cols(s->evec, n_given, nev), n, 0u)));
+  }
+  // "O" criterion from a random start: ||A||_Omega = ||A Omega||_F / ||Omega||_F
+  // over the normalised random block (src/gcge_eigsol.c:141-177); with a given
+  // start the caller's conv_omega_norm stays
+  if (p.conv_type == 1 && n_given == 0) CHK(omega_norm(s));
   // initial B-orthonormalisation of the given block (:219-242)
   {
     Timer tm(s, &s->stats.t_x_orth);
@@ -1392,6 +1614,7 @@ extern "C" int GCGE_CUDA_SOLVER_Solve(GCGE_CUDA_SOLVER* s) {
   s->stats.num_conv_continuous = s->num_conv_continuous;
   s->stats.kernel_launches = s->launches;
   s->stats.seconds = now_s() - t_start;
+  if (p.print_result || p.print_conv || p.print_final_part_time) print_final_info(s);
   return GCGE_CUDA_OK;
 }
 

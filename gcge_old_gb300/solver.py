@@ -73,7 +73,11 @@ class GCGESolver:
 
     INT_PARAMS = {"nev", "ev_max_it", "block_size", "num_init_evec", "cg_max_it",
                   "max_reorth_time", "print_level", "gemm", "use_shift", "if_shift",
-                  "eval_type"}
+                  "eval_type", "conv_type", "w_form", "print_result", "print_conv",
+                  "print_final_part_time", "print_eval", "print_para"}
+    NAMED = {"precision": {"fp64": 0, "mixed": 1}, "eval_type": {"sa": 0, "sm": 1},
+             "gemm": {"fp64": 0, "ozaki": 1}, "conv_type": {"R": 0, "O": 1, "A": 2},
+             "w_form": {"reference": 0, "correction": 1}}
 
     def __init__(self, A, B=None, nev: int = 1, **params):
         self._lib = L.load()
@@ -89,15 +93,9 @@ class GCGESolver:
         L.check(self._lib.GCGE_CUDA_SOLVER_SetNumEigen(h, nev), "SetNumEigen")
         params.setdefault("num_init_evec", nev)
         for k, v in params.items():
-            if k == "precision":
-                v = {"fp64": 0, "mixed": 1}.get(v, v)
-                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"precision", int(v)), k)
-            elif k == "eval_type":
-                v = {"sa": 0, "sm": 1}.get(v, v)
-                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"eval_type", int(v)), k)
-            elif k == "gemm":
-                v = {"fp64": 0, "ozaki": 1}.get(v, v)
-                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, b"gemm", int(v)), k)
+            if k in self.NAMED:
+                v = self.NAMED[k].get(v, v)
+                L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, k.encode(), int(v)), k)
             elif k in self.INT_PARAMS:
                 L.check(self._lib.GCGE_CUDA_SOLVER_SetParamInt(h, k.encode(), int(v)), k)
             else:
@@ -125,9 +123,12 @@ class GCGESolver:
         self._pcg = L.PCGParam(max_it, rate)
         self.set_linear_solver(self._lib.GCGE_CUDA_JacobiPCG, self._pcg)
 
-    def solve(self, x0: np.ndarray):
-        """x0: initial block, shape (nev, n) (= column-major n x nev)."""
-        self.evec[...] = np.asarray(x0, dtype=np.float64).reshape(self.nev, self.n)
+    def solve(self, x0: np.ndarray | None = None):
+        """x0: initial block, shape (nev, n) (= column-major n x nev); its first
+        num_init_evec columns are used and the rest start pseudo-random (x0 =
+        None with num_init_evec = 0: a random start)."""
+        if x0 is not None:
+            self.evec[...] = np.asarray(x0, dtype=np.float64).reshape(self.nev, self.n)
         L.check(self._lib.GCGE_CUDA_SOLVER_Solve(self.handle), "Solve")
         return self.eval.copy(), self.evec.copy()
 

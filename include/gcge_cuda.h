@@ -229,8 +229,12 @@ int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W,
  * GCGE_CUDA_ERR_ARG.  `a` is a DEVICE array; the call is asynchronous on the
  * given cudaStream_t (NULL = legacy default stream).  The first call on each
  * device looks up the scratch array's address; make that first call before
- * any stream capture begins.  All calls share the one scratch array (each
- * overwrites what it reads), so calls that overlap on the GPU race. */
+ * any stream capture begins.  The address is kept per device for the life of
+ * the process: after cudaDeviceReset on a device, this entry point must not
+ * be called on that device again.  All calls share the one scratch array
+ * (each overwrites what it reads), so calls that overlap on the GPU race.  A
+ * CUDA error left pending by earlier work is reported (and left pending for
+ * the caller's own check) instead of launching. */
 #define GCGE_CUDA_NOALLOC_MAX_OUTPUTS 4096
 int GCGE_CUDA_MultiVecInnerProdNoAlloc(double* const* V, int k1, double* const* W, int k2, int n,
                                        double* a, int lda, int sym, void* stream);

@@ -10,10 +10,14 @@
 # command line with MPI off (what the reference Makefile does with sed,
 # Makefile:34-38).  LAPACK/BLAS come from scipy's bundled OpenBLAS.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_DIR   (or GCGE_REFERENCE_DIR set)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-${GCGE_REFERENCE_DIR:-/root/reference}}"
+REF="${1:-${GCGE_REFERENCE_DIR:-}}"
+if [ -z "$REF" ]; then
+  echo "usage: $0 REFERENCE_DIR (or set GCGE_REFERENCE_DIR)" >&2
+  exit 2
+fi
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/gcge_eigsol.c" ]; then
   echo "reference sources not found under $REF; oracle/_ref not built" >&2

@@ -43,6 +43,10 @@ typedef struct {
    * block CG on A e = r in FP32 from e = 0, and W = e (w0 is a scaled column
    * of X, so [X, P, e] spans the subspace of [X, P, w0 + e]) */
   int mixed;
+  /* convergence criterion (src/gcge_eigsol.c:713-721): 0 "R", 1 "O" (divide
+   * by conv_omega_norm + |lambda|), 2 absolute */
+  int conv_type;
+  double conv_omega_norm;
 } port_para;
 
 typedef struct {
@@ -743,7 +747,8 @@ static void check_convergence(port_ws* w) {
     }
     double rn = sqrt(dot(n, t1, t1)), en = sqrt(dot(n, ev, ev));
     double r = rn / en, ab = r;
-    r /= (1.0 > fabs(eval[idx]) ? 1.0 : fabs(eval[idx]));
+    if (w->p.conv_type == 0) r /= (1.0 > fabs(eval[idx]) ? 1.0 : fabs(eval[idx]));
+    else if (w->p.conv_type == 1) r /= (w->p.conv_omega_norm + fabs(eval[idx]));
     res[idx] = r;
     if (r < w->p.ev_tol && ab < 1e-2) {
       if (idx > 0) {
@@ -833,6 +838,8 @@ void gcge_port_default_para(port_para* p, int nev) {
   p->eval_sm = 0;
   p->shift = 0.0;
   p->mixed = 0;
+  p->conv_type = 0;
+  p->conv_omega_norm = 0.0;
 }
 
 /* Solve A x = lambda B x for the nev smallest pairs from the initial block x0

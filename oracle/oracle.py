@@ -21,6 +21,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SRC = os.path.join(HERE, "gcge_port.c")
+# where the reference checkout is read from when the checker is built (the
+# reference is never needed at run time): $GCGE_REFERENCE_DIR, else the
+# checkout location of the build container
+REFERENCE_DIR = os.environ.get("GCGE_REFERENCE_DIR", "/root/reference")
 PORT_SO = os.path.join(HERE, "_build", "libgcge_port.so")
 REF_SO = os.path.join(HERE, "_ref", "libgcge_ref.so")
 
@@ -33,7 +37,8 @@ class PortPara(C.Structure):
                 ("orth_zero_tol", C.c_double), ("reorth_tol", C.c_double),
                 ("scbgs_reorth_tol", C.c_double), ("multi_tol_for_lock", C.c_double),
                 ("use_shift", C.c_int), ("if_shift", C.c_int), ("eval_sm", C.c_int),
-                ("shift", C.c_double), ("mixed", C.c_int)]
+                ("shift", C.c_double), ("mixed", C.c_int), ("conv_type", C.c_int),
+                ("conv_omega_norm", C.c_double)]
 
 
 def build_port(force: bool = False) -> str:
@@ -47,10 +52,14 @@ def build_port(force: bool = False) -> str:
     return PORT_SO
 
 
+def reference_present() -> bool:
+    return os.path.isfile(os.path.join(REFERENCE_DIR, "src", "gcge_eigsol.c"))
+
+
 def build_ref() -> str | None:
     """Compile the reference into oracle/_ref/ when its checkout is present."""
     script = os.path.join(HERE, "build_ref.sh")
-    r = subprocess.run(["bash", script], capture_output=True, text=True)
+    r = subprocess.run(["bash", script, REFERENCE_DIR], capture_output=True, text=True)
     return REF_SO if r.returncode == 0 and os.path.exists(REF_SO) else None
 
 

@@ -3,7 +3,7 @@ tests/golden/csr_files/ as fixtures for the CSR file readers: the same 1089 x 10
 FE stiffness matrix as CSR text (A_5.txt) and as PETSc binary (A_5.petsc.bin),
 and the 81 x 81 text matrix A_3.txt.  Run once where the reference is present:
 
-    python tests/golden/copy_csr_files.py /root/reference
+    python tests/golden/copy_csr_files.py REFERENCE_DIR
 """
 import os
 import shutil
@@ -22,4 +22,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: copy_csr_files.py REFERENCE_DIR")
+    main(sys.argv[1])

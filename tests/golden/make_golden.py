@@ -20,7 +20,9 @@ from gcge_old_gb300 import matrices as M  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF_DATA = os.environ.get("GCGE_REFERENCE_DIR", "/root/reference") + "/test/data"
+# the reference checkout (oracle.REFERENCE_DIR: $GCGE_REFERENCE_DIR or the
+# build container's checkout); the recipe runs only where it exists
+REF_DATA = os.path.join(O.REFERENCE_DIR, "test", "data")
 
 
 def save(name, A, B, nev, x0, flags, keep_vecs=True):
@@ -69,6 +71,7 @@ def main():
 
     shifted()
     more_structures()
+    criteria()
 
 
 def shifted():
@@ -107,13 +110,17 @@ def more_structures():
          {"-gcge_ev_tol": 1e-10, "-gcge_ev_max_it": 300})
 
 
-if __name__ == "__main__":
-    if sys.argv[1:] == ["shifted"]:
-        shifted()
-    elif sys.argv[1:] == ["structures"]:
-        more_structures()
-    else:
-        main()
+def criteria():
+    """The "O" (omega-norm) and absolute convergence criteria
+    (src/gcge_eigsol.c:713-721) with a given start, where the omega norm is the
+    -gcge_conv_omega_norm value."""
+    A, B = M.diffusion27(10, seed=2)
+    save("ref_diff27_m10_nev10_convO", A, B, 10, M.initial_block(A.n, 10, seed=4),
+         {"-gcge_ev_tol": 1e-12, "-gcge_ev_max_it": 150, "-gcge_conv_type": "O",
+          "-gcge_conv_omega_norm": 0.5})
+    A = M.laplace2d(32)
+    save("ref_lap2d_m32_nev10_convA", A, None, 10, M.initial_block(A.n, 10, seed=3),
+         {"-gcge_ev_tol": 1e-12, "-gcge_ev_max_it": 150, "-gcge_conv_type": "A"})
 
 
 def make_cfg2_summary(out_path=os.path.join(OUT, "cfg2_reference_summary.json")):
@@ -132,3 +139,53 @@ def make_cfg2_summary(out_path=os.path.join(OUT, "cfg2_reference_summary.json"))
                "seconds": r["seconds"], "host": "1 core, %s" % platform.machine(),
                "max_true_residual": float(tr.max()), "eval": [float(x) for x in r["eval"]],
                "res": [float(x) for x in r["res"]]}, open(out_path, "w"), indent=1)
+
+
+def make_cfg3_summary(ev_tol=1e-11, out_path=os.path.join(OUT, "cfg3_port_summary.json")):
+    """The 27-point mixed-precision workload at full size (160^3, n = 4,096,000,
+    nev 100, block 20) solved by the oracle port on all host threads (the
+    reference itself would take days on one core): writes its eigenvalues,
+    criterion values, true residuals, iteration count and time.  ev_tol is
+    tighter than the residual target 1e-10 because with a mass matrix of size
+    h^3 that residual bound leaves the eigenvalues free by up to ~1e-9
+    relative; the eigenvalue error falls with the square of the residual."""
+    import json
+    import platform
+    import time
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    A, B = M.diffusion27(160, seed=0)
+    x0 = M.initial_block(A.n, 100, seed=0)
+    gen = time.time() - t0
+    p = O.default_para(100, ev_tol=ev_tol, ev_max_it=1000)
+    r = O.port_solve(A, B, 100, x0, p, threads=threads)
+    tr = O.true_residuals(A, B, r["eval"], r["evec"])
+    json.dump({"workload": "diffusion27_q1_lognormal_160^3_consistent_mass_nev100 (seed 0 matrix, "
+                           "seed 0 initial block)",
+               "generator": "gcge_old_gb300.matrices.diffusion27(160, seed=0), initial_block(n, 100, seed=0)",
+               "solver": "oracle port (oracle/gcge_port.c), reference default parameters, block size 20",
+               "ev_tol": ev_tol, "iters": r["iters"], "seconds": r["seconds"],
+               "generator_seconds": gen,
+               "host": "%d threads, %s" % (threads, platform.machine()),
+               "max_true_residual": float(tr.max()), "eval": [float(x) for x in r["eval"]],
+               "res": [float(x) for x in r["res"]], "true_res": [float(x) for x in tr]},
+              open(out_path, "w"), indent=1)
+    print("cfg3: iters %d, %.0f s, max true residual %.2e" % (r["iters"], r["seconds"], tr.max()))
+
+
+if __name__ == "__main__":
+    # python tests/golden/make_golden.py [shifted|structures|criteria|cfg2|cfg3]
+    what = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if what == "shifted":
+        shifted()
+    elif what == "structures":
+        more_structures()
+    elif what == "criteria":
+        criteria()
+    elif what == "cfg2":
+        make_cfg2_summary()
+    elif what == "cfg3":
+        make_cfg3_summary(*[float(a) for a in sys.argv[2:3]])
+    else:
+        main()
+

@@ -102,3 +102,42 @@ def test_new_entry_points_check_arguments_without_gpu():
                                      None) == 1
     assert lib.GCGE_CUDA_MatGetSize(None, None, None) == 1
     assert lib.GCGE_CUDA_MatCreateFromFile(None, b"x") == 1
+
+
+def _argv(*args):
+    return len(args), (C.c_char_p * len(args))(*[a.encode() for a in args])
+
+
+def test_command_line_rejects_what_it_does_not_honour():
+    """Reference flags (src/gcge_para.c:128-407) are honoured, accepted where
+    they have no effect on one GPU, accepted only at the value this solver
+    implements, or rejected: none is dropped silently."""
+    from gcge_old_gb300 import lib as L
+    lib = L.load(build_if_missing=True)
+    s = C.c_void_p()
+    assert lib.GCGE_CUDA_SOLVER_Create(C.byref(s)) == 0
+    ok = [("-gcge_conv_type", "O"), ("-gcge_conv_type", "A"), ("-gcge_conv_type", "R"),
+          ("-gcge_conv_omega_norm", "3.5"), ("-gcge_orth_type", "B"),
+          ("-gcge_w_orth_type", "multi"), ("-gcge_p_orth_type", "multi"),
+          ("-gcge_x_orth_type", "bgs"), ("-gcge_if_use_bcg", "1"), ("-gcge_if_use_cg", "1"),
+          ("-gcge_use_bcg_continuous", "0"), ("-gcge_if_lobgcg", "0"),
+          ("-gcge_opt_rr_eig_partly", "0"), ("-gcge_opt_bcast", "1"), ("-gcge_multi_tol", "0.3"),
+          ("-gcge_print_result", "0"), ("-gcge_print_final_part_time", "0"),
+          ("-gcge_w_form", "correction"), ("-gcge_w_form", "reference")]
+    for f, v in ok:
+        assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, *_argv(f, v)) == 0, (f, v)
+    bad = [("-gcge_w_orth_type", "scbgs"), ("-gcge_x_orth_type", "scbgs"), ("-gcge_orth_type", "A"),
+           ("-gcge_if_use_bcg", "0"), ("-gcge_use_bcg_continuous", "1"), ("-gcge_if_lobgcg", "1"),
+           ("-gcge_w_orth_block_size", "5"), ("-gcge_conv_type", "X"), ("-gcge_no_such_flag", "1"),
+           ("-gcge_w_form", "other")]
+    for f, v in bad:
+        assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, *_argv(f, v)) == 1, (f, v)
+        assert f.encode() in lib.GCGE_CUDA_GetLastErrorMessage(), f
+    # a flag without its value
+    assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, *_argv("prog", "-gcge_nev")) == 1
+    # arguments that are not -gcge_* flags are skipped, as the reference skips them
+    assert lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s, *_argv("prog", "-other", "x")) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"conv_type", 1) == 0
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"conv_type", 3) == 1
+    assert lib.GCGE_CUDA_SOLVER_SetParamInt(s, b"w_form", 1) == 0
+    assert lib.GCGE_CUDA_SOLVER_Free(C.byref(s)) == 0

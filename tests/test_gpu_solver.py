@@ -21,7 +21,7 @@ def gpu_params(flags, precision):
     for k, v in flags.items():
         if k == "fixed_shift":
             p["if_shift"], p["shift"] = 1, float(v)
-        elif k == "eval_type":
+        elif k in ("eval_type", "conv_type"):
             p[k] = v
         else:
             p[k] = int(v) if k in ("block_size", "ev_max_it", "cg_max_it", "use_shift") else float(v)
@@ -209,3 +209,80 @@ def test_solver_indefinite_b_returns(cuda_lib):
         assert st["num_iter"] <= 5
     except Exception as e:  # an error status is an acceptable outcome
         assert "Solve" in str(e)
+
+
+def test_random_start_with_omega_criterion(cuda_lib):
+    """num_init_evec = 0: the start block is pseudo-random (src/gcge_eigsol.c:134-140),
+    and the "O" criterion takes its omega norm from that block (:141-177).  The
+    pairs found are the reference's (golden fixture from another start)."""
+    A, B, nev, x0, d = load_golden("ref_diff27_m10_nev10")
+    s = S.GCGESolver(A, B, nev, num_init_evec=0, conv_type="O", ev_tol=1e-12, ev_max_it=300)
+    try:
+        ev, vec = s.solve()
+        res = s.residuals()
+    finally:
+        s.close()
+    rel = np.abs(ev - d["eval"]) / np.abs(d["eval"])
+    assert rel.max() < EV_RTOL, rel.max()
+    assert res.max() < 1e-12
+    assert O.true_residuals(A, B, ev, vec).max() < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_partial_start_block(cuda_lib, precision):
+    """num_init_evec < nev: the given columns first, pseudo-random ones after."""
+    A, B = M.laplace3d_mass(12, seed=1)
+    nev = 10
+    x0 = M.initial_block(A.n, nev, seed=5)
+    ev, vec, st = S.solve(A, B, nev, x0, num_init_evec=4, ev_tol=1e-11, ev_max_it=300,
+                          precision=precision)
+    import scipy.linalg as sla
+    ref = sla.eigh(A.to_scipy().toarray(), B.to_scipy().toarray(), eigvals_only=True)[:nev]
+    np.testing.assert_allclose(ev, ref, rtol=1e-10)
+
+
+def test_fp64_correction_w_form(cuda_lib):
+    """-gcge_w_form correction: the FP64 block CG hands the correction e to the
+    W orthogonalisation instead of w0 + e (the mixed form's W step in FP64);
+    same pairs as the reference."""
+    A, B, nev, x0, d = load_golden("ref_lap3d_m12_nev12")
+    ev, vec, st = S.solve(A, B, nev, x0, w_form="correction",
+                          **gpu_params(d["flags_dict"], "fp64"))
+    rel = np.abs(ev - d["eval"]) / np.abs(d["eval"])
+    assert rel.max() < EV_RTOL, rel.max()
+    assert O.true_residuals(A, B, ev, vec).max() < 1e-9
+    assert st["num_iter"] <= int(d["iters"]) + 3
+
+
+def test_final_report_in_reference_layout(cuda_lib, capfd):
+    """print_result / print_conv / print_final_part_time write the report of
+    GCGE_PrintFinalInfo (src/gcge_para.c:577-699) to stdout."""
+    A, B, nev, x0, d = load_golden("ref_lap2d_m32_nev10")
+    capfd.readouterr()
+    ev, vec, st = S.solve(A, B, nev, x0, print_result=1, print_conv=1, print_final_part_time=1,
+                          **gpu_params(d["flags_dict"], "fp64"))
+    out = capfd.readouterr().out
+    assert "Final eigenvalues and residual information:" in out
+    assert "relative residual" in out
+    rows = [l for l in out.splitlines() if l.strip().endswith("(converged)")]
+    assert len(rows) == nev
+    first = rows[0].split()
+    assert first[0] == "1" and abs(float(first[1]) - ev[0]) <= 1e-14 * abs(ev[0])
+    assert "Total gcg iteration: %d" % st["num_iter"] in out
+    assert "All %d eigenpairs converged!" % nev in out
+    assert "Section Name        w_lsol       w_orth       rr_eig       rr_mat" in out
+
+
+def test_command_line_after_setup_is_a_state_error(cuda_lib):
+    import ctypes as C
+    A = M.laplace2d(16)
+    s = S.GCGESolver(A, None, 4)
+    try:
+        args = [b"-gcge_precision", b"mixed"]
+        argv = (C.c_char_p * 2)(*args)
+        assert cuda_lib.GCGE_CUDA_SOLVER_SetFromCommandLine(s.handle, 2, argv) == 4
+        assert cuda_lib.GCGE_CUDA_SOLVER_SetParamInt(s.handle, b"nev", 5) == 4
+        ev, vec = s.solve(M.initial_block(A.n, 4, seed=1))
+        assert np.all(np.isfinite(ev))
+    finally:
+        s.close()

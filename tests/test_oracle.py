@@ -21,6 +21,10 @@ def para_for(nev, flags):
             kw["eval_sm"] = int(v == "sm")
         elif k == "fixed_shift":
             kw["if_shift"], kw["shift"] = 1, float(v)
+        elif k == "conv_type":
+            kw["conv_type"] = {"R": 0, "O": 1, "A": 2}[v]
+        elif k == "conv_omega_norm":
+            kw["conv_omega_norm"] = float(v)
     return O.default_para(nev, **kw)
 
 

@@ -1,5 +1,6 @@
 """The allocation-free inner product (GCGE_CUDA_MultiVecInnerProdNoAlloc)
-against the allocating one (GCGE_CUDA_MultiVecInnerProd), through the C ABI.
+against the allocating one (GCGE_CUDA_MultiVecInnerProd), through the C ABI,
+and both against V W^T computed by numpy on the host.
 
 Kept in its own file, collected last, so that it runs both alone in a fresh
 process and after every other test has used the library's other scratch.
@@ -51,6 +52,10 @@ def test_no_alloc_inner_prod_matches_two_calls_in_a_row(cuda_lib):
         ref = _reference(cuda_lib, vp, k1, wp, k2, n, sym)
         got = _no_alloc(cuda_lib, vp, k1, wp, k2, n, sym, lda)
         np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.sqrt(n))
+        # independent check: the same products from numpy (FP64 on the host)
+        host = V @ W.T
+        np.testing.assert_allclose(got, host, rtol=1e-12, atol=1e-12 * np.sqrt(n))
+        np.testing.assert_allclose(ref, host, rtol=1e-12, atol=1e-12 * np.sqrt(n))
         if sym:
             assert np.array_equal(got, got.T)
 
