@@ -112,6 +112,17 @@ size_t gram_oz_partial_doubles(int k1, int k2);
 // the B-Gram of a diagonal B).
 void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2, int n, double* G,
              int ldg, bool sym, double* partial, cudaStream_t st, const double* wdiag = nullptr);
+// Digit planes (gcge_cuda_ozaki.cu): the FP64-accurate digits of a block of
+// columns cut once, for Gram products that multiply the same columns again.
+// Column c of a plane set starts at planes + c * planes_stride(n) (16-byte
+// aligned).
+size_t planes_stride(int n);
+void cut_planes(const ColList<double>& X, int k, int n, uint8_t* planes, size_t pstride,
+                cudaStream_t st);
+// gram_oz with V = plane columns voff .. voff + k1 - 1 (not symmetric).
+void gram_oz_planes(const uint8_t* planes, size_t pstride, int voff, int k1,
+                    const ColList<double>& W, int k2, int n, double* G, int ldg, double* partial,
+                    cudaStream_t st, const double* wdiag = nullptr);
 // G[i + j*ldg] = sum_b partial[b*k1*k2 + i + j*k1] (fixed order); sym mirrors
 // the upper triangle.
 void gram_reduce_partials(int k1, int k2, int nblk, bool sym, const double* partial, double* G,

@@ -328,6 +328,32 @@ extern "C" int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double
   return finish();
 }
 
+extern "C" int GCGE_CUDA_MultiVecInnerProdPlanes(double* const* V, int k1, double* const* W,
+                                                 int k2, int n, const double* wdiag, double* a,
+                                                 int lda) {
+  if (!V || !W || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||
+      lda < k1)
+    return GCGE_CUDA_ERR_ARG;
+  if (k1 == 0 || k2 == 0) return GCGE_CUDA_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const size_t part = gcge::gram_oz_partial_doubles(k1, k2);
+  const size_t ps = gcge::planes_stride(n);
+  const size_t pl_doubles = (ps * k1 + 7) / 8 + 2;
+  double* buf;
+  if (scratch(part + (size_t)k1 * k2 + pl_doubles, &buf)) return GCGE_CUDA_ERR_ALLOC;
+  double* G = buf + part;
+  uint8_t* planes = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(G + (size_t)k1 * k2) + 15) & ~(uintptr_t)15);
+  gcge::cut_planes(mk(V, k1), k1, n, planes, ps, 0);
+  gcge::gram_oz_planes(planes, ps, 0, k1, mk(W, k2), k2, n, G, k1, buf, 0, wdiag);
+  std::vector<double> h((size_t)k1 * k2);
+  if (cudaMemcpy(h.data(), G, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GCGE_CUDA_ERR_CUDA;
+  for (int j = 0; j < k2; j++)
+    for (int i = 0; i < k1; i++) a[i + (size_t)j * lda] = h[i + (size_t)j * k1];
+  return finish();
+}
+
 extern "C" int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int k2,
                                             int n, const double* a, int lda, double beta) {
   if (!x || !y || !a || k1 < 0 || k2 < 0 || k1 > GCGE_MAXCOLS || k2 > GCGE_MAXCOLS || n <= 0 ||

@@ -11,6 +11,7 @@
 // traffic, bound the GCG iteration.
 //
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 #include "gcge_cuda_common.cuh"
@@ -246,6 +247,7 @@ __device__ __forceinline__ void d8_fill_nan(ColList<double> Y, int j0, int N, in
 // level 9 by (a, b) = (2, 7), issued on its own then).  A digit a is the
 // 128 x 16 tile at abase + (a-1)*astride (core matrices 2048 bytes apart
 // along K); the B image is the 7Nw x 16 matrix described at k_d8_split_c.
+template <bool F16 = false>
 __device__ __forceinline__ void d8_issue(uint32_t tacc, uint32_t abase, uint32_t astride,
                                          uint32_t bbase, int Nw, bool first) {
   const int maxd = 256 / Nw;
@@ -260,7 +262,9 @@ __device__ __forceinline__ void d8_issue(uint32_t tacc, uint32_t abase, uint32_t
       const uint32_t accum = (first && (a == 1 || (a == 2 && b0 == D8_S))) ? 0u : 1u;
       const uint64_t bd = gcge::tc::smem_desc(bbase + (b0 - 1) * Nw * 16, D8_S * Nw * 16, 128);
       gcge::tc::mma_bf16(tacc + (uint32_t)((a + b0 - 2) * Nw), ad, bd,
-                         gcge::tc::idesc_bf16(TC_M, cnt * Nw), accum);
+                         F16 ? gcge::tc::idesc_f16(TC_M, cnt * Nw)
+                             : gcge::tc::idesc_bf16(TC_M, cnt * Nw),
+                         accum);
       b0 += cnt;
     }
   }
@@ -781,6 +785,417 @@ int gram_tc_all(const ColList<double>& V, int k1, const ColList<double>& W, int 
   return nblk;
 }
 
+// ---------------------------------------------------------------- digit planes
+// The Gram blocks of one GCG iteration (the block Gram-Schmidt passes of the W
+// orthogonalisation and the Rayleigh-Ritz projection) all multiply the same
+// basis columns [X, P] (and W once it is orthonormal).  Cutting those columns
+// into digits in every product is what bounds k_gram_tc (integer work on its
+// slicer warps), so they are cut once into "digit planes": per column and
+// 64-row chunk a record of PL_REC bytes,
+//   bytes 0..3    the chunk exponent E (|x| < 2^E over the chunk; -2000 for
+//                 an all-zero chunk, 4096 when the chunk holds a NaN or Inf),
+//   bytes 16..    4 stages of 16 rows, each stage 7 digit rows of 16 bytes:
+//                 digit a (0 = most significant) of row r is byte a of
+//                 u = m + 0x0080808080808080, m = trunc(x 2^{55-E}),
+//                 i.e. the balanced base-256 digit plus 128.
+// Seven digit bytes hold m only while m <= 0x007F7F7F7F7F7F7F (the top digit
+// then stays in [-128, 127]); a chunk whose largest value is within 0.4 % of
+// 2^E is cut with E + 1 instead (54 bits of it kept).  Rows past n are zero.
+// The Gram kernel turns a byte b into the f16 value (1024 + b) - 1152 = b - 128
+// with one byte permute and one half2 subtraction per two digits.
+constexpr int PL_K = 64;              // rows per record (the Gram's chunk)
+constexpr int PL_HDR = 16;            // header bytes
+constexpr int PL_STB = D8_S * TC_KS;  // bytes per 16-row stage (112)
+constexpr int PL_REC = PL_HDR + (PL_K / TC_KS) * PL_STB;  // 464
+constexpr long long PL_MAXM = 0x007F7F7F7F7F7F7Fll;
+constexpr int PL_WARPS = 8;
+
+// m = trunc(x 2^{55-E}) for |x| < 2^{E+1} (zero, subnormal and non-finite: 0)
+__device__ __forceinline__ long long d8_mant(double x, int E) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0 || ex == 0x7FF) return 0;
+  const unsigned long long mant = ((unsigned long long)b & ((1ull << 52) - 1)) | (1ull << 52);
+  const int sh = ex - 1020 - E;
+  const unsigned long long mm = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
+  return b < 0 ? -(long long)mm : (long long)mm;
+}
+
+// One warp per (column, chunk): lane l holds rows 2l, 2l+1 of the chunk.  The
+// record is assembled in shared memory and written as 29 16-byte stores.
+// Grid: (chunk groups, columns), PL_WARPS warps per block.
+__global__ void __launch_bounds__(PL_WARPS * 32)
+    k_cut_planes(ColList<double> X, int n, int nchunks, uint8_t* __restrict__ planes,
+                 size_t pstride) {
+  __shared__ __align__(16) uint8_t rec[PL_WARPS][PL_REC];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double* x = X.p[blockIdx.y];
+  uint8_t* out = planes + (size_t)blockIdx.y * pstride;
+  uint8_t* sb = rec[warp];
+  const bool vec = ((uintptr_t)x & 15) == 0;
+  for (int q = blockIdx.x * PL_WARPS + warp; q < nchunks; q += gridDim.x * PL_WARPS) {
+    const int r = q * PL_K + 2 * lane;
+    double v0 = 0.0, v1 = 0.0;
+    if (vec && r + 1 < n) {
+      const double2 t = __ldg(reinterpret_cast<const double2*>(x + r));
+      v0 = t.x;
+      v1 = t.y;
+    } else {
+      if (r < n) v0 = __ldg(x + r);
+      if (r + 1 < n) v1 = __ldg(x + r + 1);
+    }
+    const int f0 = (__double2hiint(v0) >> 20) & 0x7FF, f1 = (__double2hiint(v1) >> 20) & 0x7FF;
+    const int fmax = __reduce_max_sync(0xffffffffu, max(f0 == 0x7FF ? 0 : f0, f1 == 0x7FF ? 0 : f1));
+    const int bad = __reduce_or_sync(0xffffffffu, (f0 == 0x7FF) | (f1 == 0x7FF));
+    int E = bad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
+    long long m0 = 0, m1 = 0;
+    if (E > -2000 && E < 4096) {
+      m0 = d8_mant(v0, E);
+      m1 = d8_mant(v1, E);
+      if (__any_sync(0xffffffffu, m0 > PL_MAXM || m1 > PL_MAXM)) {
+        E += 1;
+        m0 = d8_mant(v0, E);
+        m1 = d8_mant(v1, E);
+      }
+    }
+    const unsigned long long u0 = (unsigned long long)(m0 + 0x0080808080808080ll);
+    const unsigned long long u1 = (unsigned long long)(m1 + 0x0080808080808080ll);
+    // rows 2l, 2l+1: stage l / 8, rows 2 (l % 8), 2 (l % 8) + 1 of it
+    uint8_t* dst = sb + PL_HDR + (lane >> 3) * PL_STB + 2 * (lane & 7);
+#pragma unroll
+    for (int a = 0; a < D8_S; a++) {
+      const int sh = 8 * (D8_S - 1 - a);
+      const unsigned short w = (unsigned short)(((u0 >> sh) & 0xFF) | (((u1 >> sh) & 0xFF) << 8));
+      *reinterpret_cast<unsigned short*>(dst + a * TC_KS) = w;
+    }
+    if (lane < 4) reinterpret_cast<int*>(sb)[lane] = lane == 0 ? E : 0;
+    __syncwarp();
+    if (lane < PL_REC / 16)
+      reinterpret_cast<uint4*>(out + (size_t)q * PL_REC)[lane] = reinterpret_cast<const uint4*>(sb)[lane];
+    __syncwarp();
+  }
+}
+
+// Two biased digit bytes (the low half first) -> two f16 digits in one word.
+__device__ __forceinline__ uint32_t pl_f16x2(uint32_t word, uint32_t sel) {
+  const uint32_t h = __byte_perm(word, 0x64u, sel);
+  const __half2 v = __hsub2(*reinterpret_cast<const __half2*>(&h), __float2half2_rn(1152.0f));
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// d8_slice4 with f16 digits (the operand type of the plane-fed Gram)
+__device__ __forceinline__ void d8h_slice4(const double* v, const int* E, uint8_t* dst,
+                                           int dstride) {
+  float f[4][D8_S];
+#pragma unroll
+  for (int q = 0; q < 4; q++) d8_digits(v[q], E[q], f[q]);
+#pragma unroll
+  for (int a = 0; a < D8_S; a++) {
+    const __half2 lo = __floats2half2_rn(f[0][a], f[1][a]);
+    const __half2 hi = __floats2half2_rn(f[2][a], f[3][a]);
+    uint2 w;
+    w.x = *reinterpret_cast<const uint32_t*>(&lo);
+    w.y = *reinterpret_cast<const uint32_t*>(&hi);
+    *reinterpret_cast<uint2*>(dst + a * dstride) = w;
+  }
+}
+
+// G = V^T diag(wd) W with V given as digit planes (column i of V: the records
+// at vpl + (voff + i) * pstride) and W as FP64 columns.  The roles and the
+// fold are k_gram_tc's; the slicer warps only turn V's digit bytes into f16
+// digits (V quads) and cut W (W quads), and the MMAs run on f16 operands.
+// The raw ring holds, per chunk, V's records (PL_REC bytes each, header
+// included) then W's raw columns and the diagonal (GC_RAWLD bytes each).
+__host__ __device__ __forceinline__ int gp_nraw(int mi, int wcols) {
+  const int room = GC_SMEM_CAP - 2 * GC_SB - GC_FOLDB - GC_FIXED;
+  const int k = room / (mi * PL_REC + wcols * GC_RAWLD);
+  return k < GC_MAXRAW ? k : GC_MAXRAW;
+}
+size_t gp_smem(int mi, int wcols) {
+  return (size_t)2 * GC_SB + GC_FOLDB + GC_FIXED +
+         (size_t)gp_nraw(mi, wcols) * (mi * PL_REC + wcols * GC_RAWLD);
+}
+
+template <bool BULK>
+__global__ void __launch_bounds__(GC_THREADS, 1)
+    k_gram_pl(const uint8_t* __restrict__ vpl, size_t pstride, int voff, int k1, ColList<double> W,
+              int k2, int n, int ntn, const double* __restrict__ wd, double* __restrict__ partial,
+              int nchunks, int nraw) {
+  extern __shared__ __align__(1024) uint8_t smgc[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.y / ntn, nt = blockIdx.y % ntn;
+  const int i0 = mt * GC_MI, j0 = nt * GC_N;
+  const int mi = min(GC_MI, k1 - i0), nj = min(GC_N, k2 - j0);
+  const int wcols = nj + (wd ? 1 : 0);     // raw FP64 columns: W, then the diagonal
+  const int VB = mi * PL_REC;               // V record bytes per chunk
+  const int RC = VB + wcols * GC_RAWLD;
+  constexpr uint32_t ncols = 2 * D8_NL * GC_N;
+  uint8_t* base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smgc) + 1023) & ~(uintptr_t)1023);
+  double* gS = reinterpret_cast<double*>(base + 2 * GC_SB);
+  long long* gT = reinterpret_cast<long long*>(gS + TC_M * GC_N);
+  int* gE = reinterpret_cast<int*>(gT + TC_M * GC_N);
+  uint8_t* rawbase = reinterpret_cast<uint8_t*>(gE + TC_M * GC_N);
+  int* cex = reinterpret_cast<int*>(rawbase + nraw * RC);
+  uint64_t* mfull = reinterpret_cast<uint64_t*>(cex + 3 * GC_CE);
+  uint64_t* mempty = mfull + 2;
+  uint64_t* maccf = mfull + 4;
+  uint64_t* macce = mfull + 6;
+  uint64_t* mraw = mfull + 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mraw + GC_MAXRAW);
+  const int cbase = nchunks / (int)gridDim.x, crem = nchunks % (int)gridDim.x;
+  const int nch = cbase + ((int)blockIdx.x < crem ? 1 : 0);
+  const int cfirst = (int)blockIdx.x * cbase + min((int)blockIdx.x, crem);
+  auto wptr = [&](int c) -> const double* { return c < nj ? W.p[j0 + c] : wd; };
+  auto vrec = [&](int i, int chunk) -> const uint8_t* {
+    return vpl + (size_t)(voff + i0 + i) * pstride + (size_t)chunk * PL_REC;
+  };
+
+  if (warp == 0) gcge::tc::tmem_alloc(tslot, ncols);
+  if (tid == 0) {
+    for (int b = 0; b < 2; b++) {
+      gcge::tc::mbar_init(&mfull[b], GC_SW);
+      gcge::tc::mbar_init(&mempty[b], 1);
+      gcge::tc::mbar_init(&maccf[b], 1);
+      gcge::tc::mbar_init(&macce[b], GC_FW);
+    }
+    for (int b = 0; b < nraw; b++) gcge::tc::mbar_init(&mraw[b], 1);
+  }
+  for (int e = tid; e < TC_M * GC_N; e += GC_THREADS) {
+    gS[e] = 0.0;
+    gT[e] = 0;
+    gE[e] = -1000000;
+  }
+  gcge::tc::fence_before();
+  __syncthreads();
+  gcge::tc::fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+
+  if (warp == GC_PW) {
+    // ------------------------------------------------ producer / MMA warp
+    auto issue_raw = [&](int cc) {
+      const int chunk = cfirst + cc;
+      const int row0 = chunk * GC_K;
+      const int valid = min(GC_K, n - row0);
+      const int rows = BULK ? (valid & ~1) : 0;
+      uint64_t* mb = &mraw[cc % nraw];
+      if (lane == 0) gcge::tc::mbar_arrive_expect_tx(mb, (uint32_t)(VB + wcols * rows * 8));
+      __syncwarp();
+      uint8_t* dst = rawbase + (cc % nraw) * RC;
+      for (int i = lane; i < mi; i += 32)
+        gcge::tc::bulk_g2s(dst + i * PL_REC, vrec(i, chunk), (uint32_t)PL_REC, mb);
+      if (rows > 0)
+        for (int c = lane; c < wcols; c += 32)
+          gcge::tc::bulk_g2s(dst + VB + c * GC_RAWLD, wptr(c) + row0, (uint32_t)(rows * 8), mb);
+    };
+    for (int cc = 0; cc < nraw && cc < nch; cc++) issue_raw(cc);
+    for (int c = 0; c < nch; c++) {
+      const int tb = c & 1;
+      if (c >= 2 && !gcge::tc::mbar_wait_warp(&macce[tb], ((c >> 1) - 1) & 1, TC_WAIT)) ok = false;
+      for (int st = 0; st < GC_ST; st++) {
+        const int g = c * GC_ST + st, buf = g & 1;
+        if (!gcge::tc::mbar_wait_warp(&mfull[buf], (g >> 1) & 1, TC_WAIT)) ok = false;
+        if (lane == 0) {
+          gcge::tc::fence_after();
+          uint8_t* As = base + buf * GC_SB;
+          d8_issue<true>(tmem + (uint32_t)(tb * D8_NL * GC_N), gcge::tc::smem_u32(As),
+                         TC_M * TC_KS * 2, gcge::tc::smem_u32(As + TC_ABYTES), GC_N, st == 0);
+          gcge::tc::commit(&mempty[buf]);
+          if (st == GC_ST - 1) gcge::tc::commit(&maccf[tb]);
+        }
+        __syncwarp();
+      }
+      if (c + nraw < nch) issue_raw(c + nraw);
+    }
+  } else if (warp >= GC_SW) {
+    // ------------------------------------------------ fold warps (as k_gram_tc)
+    const int q4 = warp - GC_SW;
+    const int i = 32 * q4 + lane;
+    for (int c = 0; c < nch; c++) {
+      const int tb = c & 1;
+      if (!gcge::tc::mbar_wait_warp(&maccf[tb], (c >> 1) & 1, TC_WAIT)) ok = false;
+      gcge::tc::fence_after();
+      if (32 * q4 < mi) {
+        const int* ce = cex + (c % 3) * GC_CE;
+        const int ea = ce[i];
+        const uint32_t tacc = tmem + (uint32_t)(tb * D8_NL * GC_N) + ((uint32_t)(32 * q4) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < GC_N; c0 += 4) {
+          uint32_t acc[D8_NL][4];
+#pragma unroll
+          for (int l = 0; l < D8_NL; l++)
+            gcge::tc::tmem_ld4(tacc + (uint32_t)(l * GC_N + c0), acc[l]);
+          gcge::tc::tmem_wait_ld();
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) {
+            const int j = c0 + jj;
+            if (i >= mi || j >= nj) continue;
+            const int eb = ce[TC_M + j];
+            const int o = j * TC_M + i;
+            if (ea >= 4096 || eb >= 4096) {
+              gS[o] = __longlong_as_double(0x7ff8000000000000ll);
+            } else if (ea > -2000 && eb > -2000) {
+              int lv[D8_NL];
+#pragma unroll
+              for (int l = 0; l < D8_NL; l++) lv[l] = __float2int_rn(__uint_as_float(acc[l][jj]));
+              const int p0 = lv[0] * 256 + lv[1], p1 = lv[2] * 256 + lv[3];
+              const int p2 = lv[4] * 256 + lv[5], p3 = lv[6] * 256 + lv[7];
+              const long long T = ((long long)p0 << 26) + ((long long)p1 << 10) +
+                                  (long long)((p2 + 32) >> 6) +
+                                  (long long)((p3 + (1 << 21)) >> 22);
+              const int E = ea + eb;
+              const long long t = gT[o], r = t + T;
+              if (gE[o] != E || ((t ^ r) & (T ^ r)) < 0) {
+                gc_flush(gT + o, gE + o, gS + o);
+                gT[o] = T;
+                gE[o] = E;
+              } else {
+                gT[o] = r;
+              }
+            }
+          }
+        }
+      }
+      gcge::tc::fence_before();
+      __syncwarp();
+      if (lane == 0) gcge::tc::mbar_arrive(&macce[tb]);
+    }
+  } else {
+    // ------------------------------------------------ slicer warps
+    // per stage: W quads first (the costly cuts, on threads 0 ..), then V
+    // quads (byte -> f16), lane = (column c, quad q = rows 4q .. 4q+3)
+    const int nwq = 4 * nj, nvq = 4 * mi;
+    const int st0 = warp * 32 + lane;
+    for (int c = 0; c < nch; c++) {
+      const int cb = cfirst + c;
+      const int row0 = cb * GC_K;
+      const int valid = min(GC_K, n - row0);
+      const int rb = c % nraw;
+      uint8_t* rbuf = rawbase + rb * RC;
+      double* raw = reinterpret_cast<double*>(rbuf + VB);
+      if (!gcge::tc::mbar_wait_warp(&mraw[rb], (c / nraw) & 1, TC_WAIT)) ok = false;
+      const int rfill = BULK ? (valid & ~1) : 0;
+      if (rfill < GC_K) {  // W rows the bulk copy did not bring: tail row, zero padding
+        const int nr = GC_K - rfill;
+        for (int e = st0; e < wcols * nr; e += GC_SW * 32) {
+          const int col = e / nr, rr = rfill + e % nr;
+          raw[col * (GC_RAWLD / 8) + rr] = rr < valid ? __ldg(wptr(col) + row0 + rr) : 0.0;
+        }
+        gcge::tc::named_sync(1, GC_SW * 32);
+      }
+      int* ce = cex + (c % 3) * GC_CE;
+      // V exponents from the record headers; W exponents as in k_gram_tc
+      for (int i = st0; i < mi; i += GC_SW * 32) ce[i] = *reinterpret_cast<const int*>(rbuf + i * PL_REC);
+      for (int col = warp; col < nj; col += GC_SW) {
+        const double2 v2 = *reinterpret_cast<const double2*>(raw + col * (GC_RAWLD / 8) + 2 * lane);
+        int f0 = (__double2hiint(v2.x) >> 20) & 0x7FF, f1 = (__double2hiint(v2.y) >> 20) & 0x7FF;
+        int bad = (f0 == 0x7FF) | (f1 == 0x7FF);
+        if (wd) {
+          const double2 w2 = *reinterpret_cast<const double2*>(raw + nj * (GC_RAWLD / 8) + 2 * lane);
+          const int g0 = (__double2hiint(w2.x) >> 20) & 0x7FF,
+                    g1 = (__double2hiint(w2.y) >> 20) & 0x7FF;
+          bad |= (g0 == 0x7FF) | (g1 == 0x7FF);
+          f0 = (f0 == 0 || g0 == 0) ? 0 : max(f0 + g0 - 1022, 1);
+          f1 = (f1 == 0 || g1 == 0) ? 0 : max(f1 + g1 - 1022, 1);
+        }
+        const int fmax = __reduce_max_sync(0xffffffffu, max(f0, f1));
+        const int anybad = __reduce_or_sync(0xffffffffu, bad);
+        if (lane == 0) ce[TC_M + col] = anybad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
+      }
+      gcge::tc::named_sync(1, GC_SW * 32);
+      for (int st = 0; st < GC_ST; st++) {
+        const int g = c * GC_ST + st, buf = g & 1;
+        if (g >= 2 && !gcge::tc::mbar_wait_warp(&mempty[buf], ((g >> 1) - 1) & 1, TC_WAIT))
+          ok = false;
+        uint8_t* As = base + buf * GC_SB;
+        uint8_t* Bs = As + TC_ABYTES;
+        for (int u = st0; u < nwq + nvq; u += GC_SW * 32) {
+          if (u < nwq) {
+            const GcQuad q = gc_quad(u, nj);
+            const double* src = raw + q.col * (GC_RAWLD / 8) + st * TC_KS + q.roff;
+            const double2 a01 = *reinterpret_cast<const double2*>(src);
+            const double2 a23 = *reinterpret_cast<const double2*>(src + 2);
+            double v[4] = {a01.x, a01.y, a23.x, a23.y};
+            if (wd) {
+              const double* ws = raw + nj * (GC_RAWLD / 8) + st * TC_KS + q.roff;
+              const double2 w01 = *reinterpret_cast<const double2*>(ws);
+              const double2 w23 = *reinterpret_cast<const double2*>(ws + 2);
+              v[0] *= w01.x;
+              v[1] *= w01.y;
+              v[2] *= w23.x;
+              v[3] *= w23.y;
+            }
+            const int E0 = ce[TC_M + q.col];
+            int E[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+              E[t] = E0;
+              if (E0 >= 4096) v[t] = 0.0;
+            }
+            uint8_t* dst = Bs + q.g * (D8_S * GC_N * 16) + (q.col >> 3) * 128 + (q.col & 7) * 16 +
+                           q.h * 8;
+            d8h_slice4(v, E, dst, GC_N * 16);
+          } else {
+            const int vq = u - nwq;
+            const int col = vq >> 2, qq = vq & 3;
+            const uint8_t* src = rbuf + col * PL_REC + PL_HDR + st * PL_STB + qq * 4;
+            uint8_t* dst = As + (qq >> 1) * (TC_M / 8 * 128) + (col >> 3) * 128 + (col & 7) * 16 +
+                           (qq & 1) * 8;
+#pragma unroll
+            for (int a = 0; a < D8_S; a++) {
+              const uint32_t w = *reinterpret_cast<const uint32_t*>(src + a * TC_KS);
+              uint2 o;
+              o.x = pl_f16x2(w, 0x4140);
+              o.y = pl_f16x2(w, 0x4342);
+              *reinterpret_cast<uint2*>(dst + a * (TC_M * TC_KS * 2)) = o;
+            }
+          }
+        }
+        gcge::tc::fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) gcge::tc::mbar_arrive(&mfull[buf]);
+      }
+    }
+  }
+  const int anybad = __syncthreads_or(ok ? 0 : 1);
+  if (anybad && tid == 0) atomicExch(&g_oz_tc_status, 1);
+  double* out = partial + (size_t)blockIdx.x * k1 * k2;
+  for (int e = tid; e < mi * nj; e += GC_THREADS) {
+    const int ii = e % mi, jj = e / mi;
+    const int o = jj * TC_M + ii;
+    gc_flush(gT + o, gE + o, gS + o);
+    out[(i0 + ii) + (size_t)(j0 + jj) * k1] =
+        anybad ? __longlong_as_double(0x7ff8000000000000ll) : gS[o];
+  }
+  gcge::tc::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    gcge::tc::fence_after();
+    gcge::tc::tmem_dealloc(tmem, ncols);
+  }
+}
+
+template <bool BULK>
+int gram_pl_all(const uint8_t* vpl, size_t pstride, int voff, int k1, const ColList<double>& W,
+                int k2, int n, const double* wd, double* partial, cudaStream_t st) {
+  const int ntm = (k1 + GC_MI - 1) / GC_MI, ntn = (k2 + GC_N - 1) / GC_N;
+  const int nchunks = (n + GC_K - 1) / GC_K;
+  const int mi = k1 < GC_MI ? k1 : GC_MI;
+  const int wcols = (k2 < GC_N ? k2 : GC_N) + (wd ? 1 : 0);
+  const int nraw = gp_nraw(mi, wcols);
+  const int nblk = nchunks < 152 ? nchunks : 152;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gram_pl<BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         GC_SMEM_CAP);
+    attr = true;
+  }
+  k_gram_pl<BULK><<<dim3(nblk, ntm * ntn), GC_THREADS, gp_smem(mi, wcols), st>>>(
+      vpl, pstride, voff, k1, W, k2, n, ntn, wd, partial, nchunks, nraw);
+  return nblk;
+}
+
 }  // namespace
 
 size_t lincomb_oz_scratch_bytes(int k1, int k2) {
@@ -862,6 +1277,29 @@ void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2,
   const int nblk = vec ? gram_tc_all<true>(V, k1, W, k2, n, wdiag, partial, st)
                        : gram_tc_all<false>(V, k1, W, k2, n, wdiag, partial, st);
   gram_reduce_partials(k1, k2, nblk, sym, partial, G, ldg, st);
+}
+
+size_t planes_stride(int n) { return (size_t)((n + PL_K - 1) / PL_K) * PL_REC; }
+
+// Digit planes of the k columns of X into planes (column c at c * pstride).
+void cut_planes(const ColList<double>& X, int k, int n, uint8_t* planes, size_t pstride,
+                cudaStream_t st) {
+  if (k <= 0 || n <= 0) return;
+  const int nchunks = (n + PL_K - 1) / PL_K;
+  const int gx = (nchunks + 4 * PL_WARPS - 1) / (4 * PL_WARPS);
+  k_cut_planes<<<dim3(gx, k), PL_WARPS * 32, 0, st>>>(X, n, nchunks, planes, pstride);
+}
+
+// G = V^T diag(wdiag) W with V = the plane columns voff .. voff + k1 - 1.
+void gram_oz_planes(const uint8_t* planes, size_t pstride, int voff, int k1,
+                    const ColList<double>& W, int k2, int n, double* G, int ldg, double* partial,
+                    cudaStream_t st, const double* wdiag) {
+  if (k1 <= 0 || k2 <= 0 || n <= 0) return;
+  bool vec = ((uintptr_t)wdiag & 15) == 0;
+  for (int j = 0; j < k2; j++) vec = vec && ((uintptr_t)W.p[j] & 15) == 0;
+  const int nblk = vec ? gram_pl_all<true>(planes, pstride, voff, k1, W, k2, n, wdiag, partial, st)
+                       : gram_pl_all<false>(planes, pstride, voff, k1, W, k2, n, wdiag, partial, st);
+  gram_reduce_partials(k1, k2, nblk, false, partial, G, ldg, st);
 }
 
 }  // namespace gcge

@@ -276,6 +276,13 @@ struct GCGE_CUDA_SOLVER_ {
   double *sub_mat = nullptr, *sub_evec = nullptr, *sub_tmp = nullptr, *sub_tmp2 = nullptr;
   double *d_eval = nullptr, *d_small = nullptr, *partial = nullptr, *jac_work = nullptr;
   void* oz_scratch = nullptr;
+  // digit planes of V[0:plane_n] (gcge::cut_planes), cut in w_orth and used
+  // by its Gram passes and the Rayleigh-Ritz Gram of the same iteration;
+  // plane_n = 0 outside that window
+  uint8_t* planes = nullptr;
+  size_t pstride = 0;
+  int plane_n = 0;
+  std::vector<double*> plane_src;
   size_t partial_len = 0;
   int* d_int = nullptr;
   gcge::BcgScalars bcg{};
@@ -567,6 +574,9 @@ static void free_ws(Solver* s) {
   cudaFree(s->jac_work);
   cudaFree(s->oz_scratch);
   s->oz_scratch = nullptr;
+  cudaFree(s->planes);
+  s->planes = nullptr;
+  s->plane_n = 0;
   cudaFree(s->d_int);
   cudaFree(s->bcg_mem);
   cudaFree(s->bcg_int);
@@ -747,6 +757,12 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   CU(cudaMalloc(&s->d_int, sizeof(int) * 4 * GCGE_MAXCOLS));
   CU(cudaMalloc(&s->jac_work, sizeof(double) * gcge::jacobi_work_doubles(s->mx)));
   CU(cudaMalloc(&s->oz_scratch, gcge::lincomb_oz_scratch_bytes(s->mx, s->mx)));
+  if (s->para.gemm == 1 || s->para.gemm == 3) {
+    s->pstride = gcge::planes_stride(s->n);
+    CU(cudaMalloc(&s->planes, s->pstride * (size_t)s->mx));
+    s->plane_src.assign(s->mx, nullptr);
+  }
+  s->plane_n = 0;
   // partial sums: Gram tiles (<= 4 x 4 tiles of 64 x 64 per row block) or
   // per-column partials of the row-split reductions
   const int tiles = ((s->mx + 63) / 64) * ((s->mx + 63) / 64);
@@ -857,6 +873,29 @@ static void gram(Solver* s, const ColList<double>& V, int k1, const ColList<doub
     gcge::gram_f64(V, k1, W, k2, s->n, G, ldg, sym, s->partial, s->st);
 }
 
+// Digit planes of V[0:k] (the columns from plane_n on are cut; those before
+// were cut in this window from the same buffers).  Returns false when the
+// configuration has no planes.
+static bool planes_cover(Solver* s, int k) {
+  if (!s->planes || k <= 0) return false;
+  if (k > s->plane_n) {
+    gcge::cut_planes(cols(s->V, s->plane_n, k), k - s->plane_n, s->n,
+                     s->planes + (size_t)s->plane_n * s->pstride, s->pstride, s->st);
+    s->launches++;
+    for (int i = s->plane_n; i < k; i++) s->plane_src[i] = s->V[i];
+    s->plane_n = k;
+  }
+  return true;
+}
+
+// true when the planes hold V[start:end] as it is now
+static bool planes_valid(const Solver* s, int start, int end) {
+  if (!s->planes || end > s->plane_n) return false;
+  for (int i = start; i < end; i++)
+    if (s->plane_src[i] != s->V[i]) return false;
+  return true;
+}
+
 // Y_j = s_j X_j (host scalars), used for the W initial guess / rhs scaling.
 static __global__ void k_scale_copy(ColList<double> X, ColList<double> Y, DblList sc, int k,
                                     int n) {
@@ -952,6 +991,10 @@ static int w_orth(Solver* s, int start, int* end) {
   const bool oz = (p.gemm == 1 || p.gemm == 3);
   const bool ozl = (p.gemm == 1 || p.gemm == 2);
   const double* bdiag = s->B ? s->B->m.diag : nullptr;
+  // [X, P] is fixed during the orthogonalisation and the Rayleigh-Ritz step
+  // that follows: its digit planes are cut once here
+  s->plane_n = 0;
+  const bool pl = oz && start > 0 && planes_cover(s, start);
   if (start > 0) {
     double vi = 1.0;
     int it = 0;
@@ -962,7 +1005,14 @@ static int w_orth(Solver* s, int start, int* end) {
       ColList<double> W = cols(s->V, start, *end);
       ColList<double> T = cols(s->V_tmp, 0, l2);
       ColList<double> V1 = cols(s->V, 0, start);
-      if (oz && (bdiag || !s->B)) {
+      if (pl && (bdiag || !s->B)) {
+        KL(gcge::gram_oz_planes(s->planes, s->pstride, 0, start, W, l2, s->n, s->sub_tmp2, start,
+                                s->partial, s->st, bdiag));
+      } else if (pl) {
+        KL(gcge::apply_b_f64(Bptr(s), W, T, l2, s->n, s->st));
+        KL(gcge::gram_oz_planes(s->planes, s->pstride, 0, start, T, l2, s->n, s->sub_tmp2, start,
+                                s->partial, s->st));
+      } else if (oz && (bdiag || !s->B)) {
         KL(gcge::gram_oz(V1, start, W, l2, s->n, s->sub_tmp2, start, false, s->partial, s->st,
                          bdiag));
       } else {
@@ -988,7 +1038,10 @@ static int w_orth(Solver* s, int start, int* end) {
       if (it >= p.max_reorth_time) break;
     }
   }
-  return cholqr2(s, s->V, start, end, s->V_tmp);
+  CHK(cholqr2(s, s->V, start, end, s->V_tmp));
+  // the orthonormal W joins the planes for the Rayleigh-Ritz Gram
+  if (pl) planes_cover(s, *end);
+  return GCGE_CUDA_OK;
 }
 
 // GCGE_ComputeSubspaceMatrixVTAW (src/gcge_rayleighritz.c:40-90); A W goes
@@ -1009,7 +1062,11 @@ static int vtaw(Solver* s, int start_W, int start_V, int end_V, double* smat) {
   // one Gram [V[start_V:xpl], W]^T (A W), then the W^T A W block is made
   // symmetric from its upper triangle (the "sym" product of the reference)
   ColList<double> VV = cols(s->V, start_V, end_V);
-  KL(gram(s, VV, end_V - start_V, AW, wl, smat + start_V, end_V, false));
+  if (planes_valid(s, start_V, end_V))
+    KL(gcge::gram_oz_planes(s->planes, s->pstride, start_V, end_V - start_V, AW, wl, s->n,
+                            smat + start_V, end_V, s->partial, s->st));
+  else
+    KL(gram(s, VV, end_V - start_V, AW, wl, smat + start_V, end_V, false));
   KL((k_mirror_upper<<<(wl * wl + 127) / 128, 128, 0, s->st>>>(smat + xpl, end_V, wl)));
   return GCGE_CUDA_OK;
 }
@@ -1030,6 +1087,7 @@ static int compute_subspace_matrix(Solver* s) {
     KL(gcge::set_diag(s->sub_mat, ldm, s->d_eval, dim_x, s->st));
   }
   CHK(vtaw(s, dim_xp, s->num_soft_locked, ldm, s->sub_mat + (size_t)dim_xp * ldm));
+  s->plane_n = 0;  // the X and P updates change the basis next
   if (s->if_shift_run == 1) KL(gcge::add_diag(s->sub_mat, ldm, s->shift_run, ldm, s->st));  // :181-189
   return GCGE_CUDA_OK;
 }

@@ -100,6 +100,16 @@ SIGNATURES = {
                                               C.c_int, C.c_int]),
     "GCGE_CUDA_MultiVecInnerProdOzaki": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,
                                                    C.c_void_p, C.c_int, C.c_int]),
+    "GCGE_CUDA_SetOps": (C.c_int, [C.c_void_p]),
+    "GCGE_CUDA_MultiVecCreate": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "GCGE_CUDA_MultiVecDestroy": (C.c_int, [C.c_void_p]),
+    "GCGE_CUDA_MultiVecSetFromHost": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                C.c_int]),
+    "GCGE_CUDA_MultiVecGetToHost": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]),
+    "GCGE_CUDA_OpsGetError": (C.c_int, []),
+    "GCGE_CUDA_OpsClearError": (None, []),
+    "GCGE_CUDA_MultiVecInnerProdPlanes": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,
+                                                    C.c_void_p, C.c_void_p, C.c_int]),
     "GCGE_CUDA_MultiVecInnerProdNoAlloc": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,
                                                      C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "GCGE_CUDA_MultiVecLinearComb": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int, C.c_void_p,

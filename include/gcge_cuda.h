@@ -219,6 +219,15 @@ int GCGE_CUDA_MultiVecInnerProd(double* const* V, int k1, double* const* W, int 
  * exact FP32 level sums in tensor memory, 64-bit fixed-point combination. */
 int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W, int k2, int n,
                                      double* a, int lda, int sym);
+/* a[i + j*lda] = sum_r V[i][r] d[r] W[j][r] (d = wdiag, a DEVICE array of n
+ * entries, or NULL for the identity) into a HOST array, with the columns of V
+ * first cut into digit planes (7 digit bytes per value and one exponent per
+ * 64-row chunk), the form in which the solver multiplies the same basis
+ * columns by several blocks in one GCG iteration; same accuracy as
+ * GCGE_CUDA_MultiVecInnerProdOzaki (MultiVecInnerProd, src/gcge_ops.h:113-114,
+ * with the B-inner product of a diagonal B folded in). */
+int GCGE_CUDA_MultiVecInnerProdPlanes(double* const* V, int k1, double* const* W, int k2, int n,
+                                      const double* wdiag, double* a, int lda);
 /* Allocation-free FP64 inner products (no counterpart in the reference):
  * the same a[i + j*lda] = V[i] . W[j] as GCGE_CUDA_MultiVecInnerProd, for
  * callers that must not allocate device memory (a fixed memory budget owned

@@ -2,13 +2,13 @@
 mass (the benchmark's generator) on an m^3 grid for a fixed number of GCG
 iterations, so a profiler sees a bounded, repeatable launch sequence.
 
-    python -m gcge_old_gb300.profile_solve --grid 96 --iters 6 --precision mixed
+    python profile_solve.py --grid 96 --iters 6 --precision mixed
 
 With --spmm K it only runs K-column CSR SpMMs of the same matrix (five FP64
 launches, five FP32 column launches, five FP32 row-interleaved launches), for
 traffic counters of those kernels:
 
-    python -m gcge_old_gb300.profile_solve --grid 96 --spmm 10
+    python profile_solve.py --grid 96 --spmm 10
 
 --graph N solves the shifted Laplacian of an N-node Chung-Lu graph with B = D
 instead (uneven rows); --aniso M --adjoint K solves the 2D anisotropic problem
@@ -16,13 +16,13 @@ on an M x M grid and then runs K steps of the eigenvector adjoint's projected
 CG for the first eigenvector (a bounded launch sequence: the adjoint stops
 there whether or not it converged):
 
-    python -m gcge_old_gb300.profile_solve --graph 1000000 --nev 128 --iters 3
-    python -m gcge_old_gb300.profile_solve --aniso 512 --nev 32 --adjoint 200
+    python profile_solve.py --graph 1000000 --nev 128 --iters 3
+    python profile_solve.py --aniso 512 --nev 32 --adjoint 200
 """
 import argparse
 
-from . import matrices as M
-from . import solver as S
+from gcge_old_gb300 import matrices as M
+from gcge_old_gb300 import solver as S
 
 
 def spmm_only(A, k):
@@ -30,7 +30,7 @@ def spmm_only(A, k):
 
     import torch
 
-    from . import lib as L
+    from gcge_old_gb300 import lib as L
     lib = L.load()
     dA = S.DeviceMatrix(A)
     X = [torch.randn(A.n, dtype=torch.float64, device="cuda") for _ in range(k)]
@@ -60,7 +60,7 @@ def adjoint_steps(A, B, nev, steps):
     import numpy as np
     import torch
 
-    from . import lib as L
+    from gcge_old_gb300 import lib as L
     lib = L.load()
     x0 = M.initial_block(A.n, nev, seed=0)
     ev, vec, _ = S.solve(A, B, nev, x0, ev_tol=1e-12, ev_max_it=2000, precision="fp64")

@@ -11,9 +11,16 @@ from conftest import ROOT
 
 
 def header_functions():
-    txt = open(os.path.join(ROOT, "include", "gcge_cuda.h")).read()
-    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(GCGE_CUDA_\w+)\s*\(", txt)))
+    """Every GCGE_CUDA_* function declared in include/*.h (the table's
+    struct fields are members, not exports: only names followed by "(" at the
+    start of a declaration count)."""
+    import glob
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names |= set(re.findall(r"^[A-Za-z_][\w\s\*]*?\b(GCGE_CUDA_\w+)\s*\(", txt, flags=re.M))
+    return sorted(names)
 
 
 def test_library_builds_and_exports_header(tmp_path):

@@ -110,3 +110,77 @@ def test_kept_levels_give_fp64_accurate_dot_products(K, spread, seed):
         dropped = sum(abs(S[L]) * Fraction(2) ** (112 - 8 * L) for L in range(10, 15))
         assert dropped * Fraction(2) ** -110 < K * Fraction(2) ** -61
     assert worst < 2.0 ** -54, np.log2(worst)
+
+
+# ---------------------------------------------------------------- digit planes
+# CPU restatement of the plane records of k_cut_planes (gcge_cuda_ozaki.cu): per
+# column and 64-row chunk, E (|x| < 2^E, one more when the largest m would not
+# fit seven biased bytes) and, per 16-row stage s and digit a, 16 bytes of
+# u = m + 0x0080808080808080 (byte 6 - a of row 16 s + r at 16 + 112 s + 16 a + r).
+PL_MAXM = 0x007F7F7F7F7F7F7F
+
+
+def cut_record(x):
+    """x: 64 values of one chunk -> (E, record bytes[464])."""
+    nz = np.abs(x[np.isfinite(x)])
+    nz = nz[nz >= np.finfo(np.float64).tiny]  # subnormals count as zero
+    if not np.all(np.isfinite(x)):
+        E = 4096
+    elif len(nz) == 0:
+        E = -2000
+    else:
+        E = int(np.frexp(nz.max())[1])
+    m = np.zeros(64, np.int64)
+    if -2000 < E < 4096:
+        keep = np.abs(x) >= np.finfo(np.float64).tiny
+        m = np.where(keep, np.trunc(np.ldexp(x, 55 - E)), 0).astype(np.int64)
+        if m.max() > PL_MAXM:
+            E += 1
+            m = np.where(keep, np.trunc(np.ldexp(x, 55 - E)), 0).astype(np.int64)
+    u = (m + np.int64(0x0080808080808080)).astype(np.uint64)
+    rec = np.zeros(464, np.uint8)
+    rec[:4] = np.frombuffer(np.int32(E).tobytes(), np.uint8)
+    for r in range(64):
+        s, rr = divmod(r, 16)
+        for a in range(NDIG):
+            rec[16 + 112 * s + 16 * a + rr] = (int(u[r]) >> (8 * (6 - a))) & 0xFF
+    return E, m, rec
+
+
+def f16_digit(b):
+    """The Gram kernel's conversion: the f16 with bits 0x6400 | b, minus 1152."""
+    h = np.array([0x6400 | int(b)], np.uint16).view(np.float16)[0]
+    return float(np.float16(h - np.float16(1152.0)))
+
+
+def test_plane_bytes_convert_to_exact_f16_digits():
+    assert all(f16_digit(b) == b - 128 for b in range(256))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_plane_records_rebuild_the_mantissa(seed):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(64) * np.exp2(rng.integers(-20, 20, 64))
+    if seed == 1:
+        x *= 2.0 ** 6 / np.abs(x).max()
+        x[5] = np.nextafter(2.0 ** 7, 0.0)  # largest m would be 2^55 - 4: needs E + 1
+    if seed == 2:
+        x[:] = -x.max()  # all negative at the scale: no bump needed
+    if seed == 3:
+        x[:3] = [0.0, 5e-324, -1e-310]
+    E, m, rec = cut_record(x)
+    assert int(m.max()) <= PL_MAXM
+    w = [256 ** (6 - a) for a in range(NDIG)]
+    for r in range(64):
+        s, rr = divmod(r, 16)
+        d = [int(rec[16 + 112 * s + 16 * a + rr]) - 128 for a in range(NDIG)]
+        assert sum(di * wi for di, wi in zip(d, w)) == int(m[r])
+    # truncation: at most one unit of 2^(E-55) (two when the exponent was bumped)
+    r = np.abs(x - np.ldexp(m.astype(np.float64), E - 55))
+    assert (r < np.ldexp(1.0, E - 55)).all()
+    if seed == 1:
+        assert E == 8
+    # planes agree with the per-call digits wherever both apply
+    if seed != 1:
+        m2, _ = digits(x, E)
+        assert np.array_equal(m, m2)

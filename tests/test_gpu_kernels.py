@@ -242,6 +242,72 @@ def test_ozaki_gram_is_fp64_accurate(cuda_lib, k1, k2, sym, n):
         assert np.array_equal(got, got.T)
 
 
+@pytest.mark.parametrize("k1,k2,n,diag", [(80, 10, 100003, True), (90, 10, 65536, False),
+                                          (130, 20, 4099, True), (1, 1, 5, False),
+                                          (96, 16, 64 * 37 + 1, True), (200, 33, 777, False)])
+def test_plane_gram_is_fp64_accurate(cuda_lib, k1, k2, n, diag):
+    """The Gram from digit planes of V (cut once) against exact products:
+    columns of very different size, a chunk whose largest value sits just
+    below a power of two (its top digit would be 128: cut with one more
+    exponent bit), a zero column and ragged row counts; with and without a
+    diagonal weight (the B-inner product of a diagonal B)."""
+    import torch
+    rng = np.random.default_rng(k1 * 7 + k2 + n)
+    V = rng.standard_normal((k1, n)) * np.exp(rng.uniform(-4, 4, size=(k1, 1)))
+    V[:, : n // 3] *= 1e-3
+    if k1 > 2:
+        V[1] = 0.0
+        V[2, : min(n, 64)] = rng.uniform(-0.5, 0.5, min(n, 64))
+        V[2, 0] = np.nextafter(1.0, 0.0)  # m = 2^55 - 4 at E = 0: needs E = 1
+    W = rng.standard_normal((k2, n))
+    d = rng.uniform(0.5, 2.0, n) if diag else np.ones(n)
+    vs, vp = dev_cols(V)
+    ws, wp = dev_cols(W)
+    dt = torch.from_numpy(d).to("cuda") if diag else None
+    a = np.zeros((k2, k1 + 3))
+    assert cuda_lib.GCGE_CUDA_MultiVecInnerProdPlanes(
+        vp, k1, wp, k2, n, C.c_void_p(dt.data_ptr()) if diag else None, _ptr(a), k1 + 3) == 0
+    got = a[:, :k1].T
+    Wd = W * d[None, :]
+    ref = (V.astype(np.longdouble) @ Wd.T.astype(np.longdouble)).astype(np.float64)
+    bound = np.abs(V) @ np.abs(Wd).T
+    ok = bound > 0
+    assert np.all(got[~ok] == 0.0)
+    # each 64-row chunk is cut at its own column scales: the truncation error
+    # of a chunk is a few units of 2^-55 of (rows x largest |v| x largest |w d|)
+    # there, which on long columns is a few units of 2^-53 of sum |v| |w d|
+    nc = (n + 63) // 64
+    pad = nc * 64 - n
+    vm = np.abs(np.pad(V, ((0, 0), (0, pad)))).reshape(k1, nc, 64).max(axis=2)
+    wm = np.abs(np.pad(Wd, ((0, 0), (0, pad)))).reshape(k2, nc, 64).max(axis=2)
+    cbound = 64 * vm @ wm.T
+    assert np.max(np.abs(got[ok] - ref[ok]) / cbound[ok]) < 4 * 2.0 ** -53
+    if n > 10_000:
+        assert np.max(np.abs(got[ok] - ref[ok]) / bound[ok]) < 16 * 2.0 ** -52
+    # the same products through the per-call digit path
+    b = np.zeros((k2, k1))
+    if not diag:
+        assert cuda_lib.GCGE_CUDA_MultiVecInnerProdOzaki(vp, k1, wp, k2, n, _ptr(b), k1, 0) == 0
+        assert np.max(np.abs(got - b.T)[ok] / cbound[ok]) < 8 * 2.0 ** -53
+
+
+def test_plane_gram_non_finite_column(cuda_lib):
+    """A NaN in a column of V turns that column's products into NaN only."""
+    n, k1, k2 = 5000, 12, 3
+    rng = np.random.default_rng(3)
+    V = rng.standard_normal((k1, n))
+    V[4, 777] = np.nan
+    W = rng.standard_normal((k2, n))
+    vs, vp = dev_cols(V)
+    ws, wp = dev_cols(W)
+    a = np.zeros((k2, k1))
+    assert cuda_lib.GCGE_CUDA_MultiVecInnerProdPlanes(vp, k1, wp, k2, n, None, _ptr(a), k1) == 0
+    got = a.T
+    assert np.all(np.isnan(got[4]))
+    rest = np.delete(np.arange(k1), 4)
+    np.testing.assert_allclose(got[rest], V[rest] @ W.T, rtol=1e-13, atol=1e-12)
+
+
 def test_ozaki_lincomb_unbalanced_columns(cuda_lib):
     """W R^{-1} of a CholQR step near convergence: the columns of W span
     eight orders of magnitude and R^{-1} undoes it; the balanced tensor-core
