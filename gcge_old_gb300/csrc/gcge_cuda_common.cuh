@@ -114,15 +114,18 @@ void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2,
              int ldg, bool sym, double* partial, cudaStream_t st, const double* wdiag = nullptr);
 // Digit planes (gcge_cuda_ozaki.cu): the FP64-accurate digits of a block of
 // columns cut once, for Gram products that multiply the same columns again.
-// Column c of a plane set starts at planes + c * planes_stride(n) (16-byte
-// aligned).
-size_t planes_stride(int n);
-void cut_planes(const ColList<double>& X, int k, int n, uint8_t* planes, size_t pstride,
-                cudaStream_t st);
-// gram_oz with V = plane columns voff .. voff + k1 - 1 (not symmetric).
-void gram_oz_planes(const uint8_t* planes, size_t pstride, int voff, int k1,
-                    const ColList<double>& W, int k2, int n, double* G, int ldg, double* partial,
-                    cudaStream_t st, const double* wdiag = nullptr);
+// A plane set of ldp columns takes planes_bytes(n, ldp) bytes (16-byte
+// aligned base).
+size_t planes_bytes(int n, int ldp);
+// columns of X (rows weighted by d when given) -> plane columns c0 .. c0 + k - 1
+void cut_planes(const ColList<double>& X, int k, int n, uint8_t* planes, int ldp, int c0,
+                cudaStream_t st, const double* d = nullptr);
+// gram_oz with V = plane columns voff .. voff + k1 - 1 of a set of ldv and
+// W = plane columns woff .. woff + k2 - 1 of a set of ldw (not symmetric);
+// partial: gram_oz_partial_doubles(k1, k2) doubles.
+void gram_oz_planes(const uint8_t* vpl, int ldv, int voff, int k1, const uint8_t* wpl, int ldw,
+                    int woff, int k2, int n, double* G, int ldg, double* partial,
+                    cudaStream_t st);
 // G[i + j*ldg] = sum_b partial[b*k1*k2 + i + j*k1] (fixed order); sym mirrors
 // the upper triangle.
 void gram_reduce_partials(int k1, int k2, int nblk, bool sym, const double* partial, double* G,

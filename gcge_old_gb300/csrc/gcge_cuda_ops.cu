@@ -12,6 +12,8 @@
 #include "gcge_cuda_dense.cuh"
 
 
+int gcge_record_error(int code, const char* msg);
+
 namespace {
 
 std::mutex g_mu;
@@ -337,21 +339,58 @@ extern "C" int GCGE_CUDA_MultiVecInnerProdPlanes(double* const* V, int k1, doubl
   if (k1 == 0 || k2 == 0) return GCGE_CUDA_OK;
   std::lock_guard<std::mutex> lk(g_mu);
   const size_t part = gcge::gram_oz_partial_doubles(k1, k2);
-  const size_t ps = gcge::planes_stride(n);
-  const size_t pl_doubles = (ps * k1 + 7) / 8 + 2;
+  const size_t pl_doubles = (gcge::planes_bytes(n, k1) + gcge::planes_bytes(n, k2) + 7) / 8 + 4;
   double* buf;
   if (scratch(part + (size_t)k1 * k2 + pl_doubles, &buf)) return GCGE_CUDA_ERR_ALLOC;
   double* G = buf + part;
   uint8_t* planes = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(G + (size_t)k1 * k2) + 15) & ~(uintptr_t)15);
-  gcge::cut_planes(mk(V, k1), k1, n, planes, ps, 0);
-  gcge::gram_oz_planes(planes, ps, 0, k1, mk(W, k2), k2, n, G, k1, buf, 0, wdiag);
+  uint8_t* wplanes = planes + (gcge::planes_bytes(n, k1) + 15) / 16 * 16;
+  gcge::cut_planes(mk(V, k1), k1, n, planes, k1, 0, 0);
+  gcge::cut_planes(mk(W, k2), k2, n, wplanes, k2, 0, 0, wdiag);
+  gcge::gram_oz_planes(planes, k1, 0, k1, wplanes, k2, 0, k2, n, G, k1, buf, 0);
   std::vector<double> h((size_t)k1 * k2);
   if (cudaMemcpy(h.data(), G, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
     return GCGE_CUDA_ERR_CUDA;
   for (int j = 0; j < k2; j++)
     for (int i = 0; i < k1; i++) a[i + (size_t)j * lda] = h[i + (size_t)j * k1];
   return finish();
+}
+
+extern "C" size_t GCGE_CUDA_PlanesBytes(int n, int ldp) {
+  return (n > 0 && ldp > 0) ? gcge::planes_bytes(n, ldp) : 0;
+}
+
+extern "C" size_t GCGE_CUDA_PlanesGramScratchDoubles(int k1, int k2) {
+  return (k1 > 0 && k2 > 0) ? gcge::gram_oz_partial_doubles(k1, k2) : 0;
+}
+
+extern "C" int GCGE_CUDA_PlanesCut(double* const* X, int k, int n, const double* wdiag,
+                                   void* planes, int ldp, int c0, void* stream) {
+  if (!X || !planes || k < 0 || k > GCGE_MAXCOLS || n <= 0 || c0 < 0 || c0 + k > ldp ||
+      ((uintptr_t)planes & 15) != 0)
+    return gcge_record_error(GCGE_CUDA_ERR_ARG, "PlanesCut: bad arguments");
+  gcge::cut_planes(mk(X, k), k, n, static_cast<uint8_t*>(planes), ldp, c0, (cudaStream_t)stream,
+                   wdiag);
+  return cudaPeekAtLastError() == cudaSuccess
+             ? GCGE_CUDA_OK
+             : gcge_record_error(GCGE_CUDA_ERR_CUDA, "PlanesCut: launch failed");
+}
+
+extern "C" int GCGE_CUDA_PlanesGram(const void* vplanes, int ldv, int voff, int k1,
+                                    const void* wplanes, int ldw, int woff, int k2, int n,
+                                    double* a, int lda, double* partial, void* stream) {
+  if (!vplanes || !wplanes || !a || !partial || k1 <= 0 || k2 <= 0 || k1 > GCGE_MAXCOLS ||
+      k2 > GCGE_MAXCOLS || n <= 0 || voff < 0 || woff < 0 || voff + k1 > ldv ||
+      woff + k2 > ldw || lda < k1 || ((uintptr_t)vplanes & 15) != 0 ||
+      ((uintptr_t)wplanes & 15) != 0)
+    return gcge_record_error(GCGE_CUDA_ERR_ARG, "PlanesGram: bad arguments");
+  gcge::gram_oz_planes(static_cast<const uint8_t*>(vplanes), ldv, voff, k1,
+                       static_cast<const uint8_t*>(wplanes), ldw, woff, k2, n, a, lda, partial,
+                       (cudaStream_t)stream);
+  return cudaPeekAtLastError() == cudaSuccess
+             ? GCGE_CUDA_OK
+             : gcge_record_error(GCGE_CUDA_ERR_CUDA, "PlanesGram: launch failed");
 }
 
 extern "C" int GCGE_CUDA_MultiVecLinearComb(double* const* x, int k1, double* const* y, int k2,

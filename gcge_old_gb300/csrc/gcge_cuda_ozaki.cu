@@ -788,10 +788,9 @@ int gram_tc_all(const ColList<double>& V, int k1, const ColList<double>& W, int 
 // ---------------------------------------------------------------- digit planes
 // The Gram blocks of one GCG iteration (the block Gram-Schmidt passes of the W
 // orthogonalisation and the Rayleigh-Ritz projection) all multiply the same
-// basis columns [X, P] (and W once it is orthonormal).  Cutting those columns
-// into digits in every product is what bounds k_gram_tc (integer work on its
-// slicer warps), so they are cut once into "digit planes": per column and
-// 64-row chunk a record of PL_REC bytes,
+// basis columns [X, P] (and W once it is orthonormal), so those columns are
+// cut into digits once, into "digit planes": per column and 64-row chunk a
+// record of PL_REC bytes,
 //   bytes 0..3    the chunk exponent E (|x| < 2^E over the chunk; -2000 for
 //                 an all-zero chunk, 4096 when the chunk holds a NaN or Inf),
 //   bytes 16..    4 stages of 16 rows, each stage 7 digit rows of 16 bytes:
@@ -803,6 +802,9 @@ int gram_tc_all(const ColList<double>& V, int k1, const ColList<double>& W, int 
 // 2^E is cut with E + 1 instead (54 bits of it kept).  Rows past n are zero.
 // The Gram kernel turns a byte b into the f16 value (1024 + b) - 1152 = b - 128
 // with one byte permute and one half2 subtraction per two digits.
+// Layout of a plane set: chunk-major, the records of chunk q for columns
+// 0 .. ldp-1 side by side at planes + (q * ldp + c) * PL_REC, so the records of
+// a run of columns for one chunk are one contiguous block (one bulk copy).
 constexpr int PL_K = 64;              // rows per record (the Gram's chunk)
 constexpr int PL_HDR = 16;            // header bytes
 constexpr int PL_STB = D8_S * TC_KS;  // bytes per 16-row stage (112)
@@ -823,16 +825,19 @@ __device__ __forceinline__ long long d8_mant(double x, int E) {
 
 // One warp per (column, chunk): lane l holds rows 2l, 2l+1 of the chunk.  The
 // record is assembled in shared memory and written as 29 16-byte stores.
-// Grid: (chunk groups, columns), PL_WARPS warps per block.
+// Grid: (chunk groups, columns), PL_WARPS warps per block; column y of X goes
+// to plane column c0 + y.  d (optional): the rows are weighted first,
+// x[r] * d[r] rounded to FP64 (the B-inner product of a diagonal B).
 __global__ void __launch_bounds__(PL_WARPS * 32)
-    k_cut_planes(ColList<double> X, int n, int nchunks, uint8_t* __restrict__ planes,
-                 size_t pstride) {
+    k_cut_planes(ColList<double> X, const double* __restrict__ d, int n, int nchunks,
+                 uint8_t* __restrict__ planes, int ldp, int c0) {
   __shared__ __align__(16) uint8_t rec[PL_WARPS][PL_REC];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double* x = X.p[blockIdx.y];
-  uint8_t* out = planes + (size_t)blockIdx.y * pstride;
+  uint8_t* out = planes + (size_t)(c0 + (int)blockIdx.y) * PL_REC;
+  const size_t qstride = (size_t)ldp * PL_REC;
   uint8_t* sb = rec[warp];
-  const bool vec = ((uintptr_t)x & 15) == 0;
+  const bool vec = ((uintptr_t)x & 15) == 0 && ((uintptr_t)d & 15) == 0;
   for (int q = blockIdx.x * PL_WARPS + warp; q < nchunks; q += gridDim.x * PL_WARPS) {
     const int r = q * PL_K + 2 * lane;
     double v0 = 0.0, v1 = 0.0;
@@ -840,9 +845,14 @@ __global__ void __launch_bounds__(PL_WARPS * 32)
       const double2 t = __ldg(reinterpret_cast<const double2*>(x + r));
       v0 = t.x;
       v1 = t.y;
+      if (d) {
+        const double2 w = __ldg(reinterpret_cast<const double2*>(d + r));
+        v0 *= w.x;
+        v1 *= w.y;
+      }
     } else {
-      if (r < n) v0 = __ldg(x + r);
-      if (r + 1 < n) v1 = __ldg(x + r + 1);
+      if (r < n) v0 = __ldg(x + r) * (d ? __ldg(d + r) : 1.0);
+      if (r + 1 < n) v1 = __ldg(x + r + 1) * (d ? __ldg(d + r + 1) : 1.0);
     }
     const int f0 = (__double2hiint(v0) >> 20) & 0x7FF, f1 = (__double2hiint(v1) >> 20) & 0x7FF;
     const int fmax = __reduce_max_sync(0xffffffffu, max(f0 == 0x7FF ? 0 : f0, f1 == 0x7FF ? 0 : f1));
@@ -871,7 +881,7 @@ __global__ void __launch_bounds__(PL_WARPS * 32)
     if (lane < 4) reinterpret_cast<int*>(sb)[lane] = lane == 0 ? E : 0;
     __syncwarp();
     if (lane < PL_REC / 16)
-      reinterpret_cast<uint4*>(out + (size_t)q * PL_REC)[lane] = reinterpret_cast<const uint4*>(sb)[lane];
+      reinterpret_cast<uint4*>(out + (size_t)q * qstride)[lane] = reinterpret_cast<const uint4*>(sb)[lane];
     __syncwarp();
   }
 }
@@ -883,52 +893,61 @@ __device__ __forceinline__ uint32_t pl_f16x2(uint32_t word, uint32_t sel) {
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// d8_slice4 with f16 digits (the operand type of the plane-fed Gram)
-__device__ __forceinline__ void d8h_slice4(const double* v, const int* E, uint8_t* dst,
-                                           int dstride) {
-  float f[4][D8_S];
-#pragma unroll
-  for (int q = 0; q < 4; q++) d8_digits(v[q], E[q], f[q]);
+// G = V^T W with both operands given as digit planes: V = plane columns
+// voff .. voff + k1 - 1 of a set of ldv columns, W = plane columns
+// woff .. woff + k2 - 1 of a set of ldw columns (a diagonal weight is folded
+// into W's planes when they are cut).  One CTA per SM owns up to GC_MI columns
+// of V (MMA M, TMEM lane) and GC_N columns of W (MMA N) over a contiguous run
+// of 64-row chunks.  Per chunk one bulk copy brings V's records and one W's
+// (the chunk-major plane layout makes each a contiguous block) into a ring of
+// raw buffers.  Roles:
+//  * 12 converter warps: per 16-row stage they turn the digit bytes of both
+//    operands into f16 digits in a double-buffered stage; after a named
+//    barrier over the 384 converters, thread 0 issues the stage's skewed MMAs
+//    into the chunk's level accumulators in tensor memory (two sets alternate)
+//    and commits them; thread 0 also issues the bulk copies;
+//  * 8 fold warps (two per TMEM lane quadrant, 8 W columns each): per chunk
+//    the exact level sums into a 64-bit fixed-point accumulator per output,
+//    rounded into an FP64 partial only when the chunk exponent changes.
+constexpr int GP_CW = 12;                       // converter warps
+constexpr int GP_FW = 8;                        // fold warps
+constexpr int GP_THREADS = (GP_CW + GP_FW) * 32;
+constexpr int GP_FIXED = 1024 + 3 * GC_CE * 4 + (8 + GC_MAXRAW) * 8 + 16;
+
+__host__ __device__ __forceinline__ int gp_nraw(int mi, int nj) {
+  const int room = GC_SMEM_CAP - 2 * GC_SB - GC_FOLDB - GP_FIXED;
+  const int k = room / ((mi + nj) * PL_REC);
+  return k < GC_MAXRAW ? k : GC_MAXRAW;
+}
+size_t gp_smem(int mi, int nj) {
+  return (size_t)2 * GC_SB + GC_FOLDB + GP_FIXED + (size_t)gp_nraw(mi, nj) * (mi + nj) * PL_REC;
+}
+
+// the digit bytes of rows 4q .. 4q+3 of a record's stage -> 7 f16 digit pairs
+// (8 bytes each) at dst + a * dstride
+__device__ __forceinline__ void pl_quad(const uint8_t* rec, int st, int q, uint8_t* dst,
+                                        int dstride) {
+  const uint8_t* src = rec + PL_HDR + st * PL_STB + q * 4;
 #pragma unroll
   for (int a = 0; a < D8_S; a++) {
-    const __half2 lo = __floats2half2_rn(f[0][a], f[1][a]);
-    const __half2 hi = __floats2half2_rn(f[2][a], f[3][a]);
-    uint2 w;
-    w.x = *reinterpret_cast<const uint32_t*>(&lo);
-    w.y = *reinterpret_cast<const uint32_t*>(&hi);
-    *reinterpret_cast<uint2*>(dst + a * dstride) = w;
+    const uint32_t w = *reinterpret_cast<const uint32_t*>(src + a * TC_KS);
+    uint2 o;
+    o.x = pl_f16x2(w, 0x4140);
+    o.y = pl_f16x2(w, 0x4342);
+    *reinterpret_cast<uint2*>(dst + a * dstride) = o;
   }
 }
 
-// G = V^T diag(wd) W with V given as digit planes (column i of V: the records
-// at vpl + (voff + i) * pstride) and W as FP64 columns.  The roles and the
-// fold are k_gram_tc's; the slicer warps only turn V's digit bytes into f16
-// digits (V quads) and cut W (W quads), and the MMAs run on f16 operands.
-// The raw ring holds, per chunk, V's records (PL_REC bytes each, header
-// included) then W's raw columns and the diagonal (GC_RAWLD bytes each).
-__host__ __device__ __forceinline__ int gp_nraw(int mi, int wcols) {
-  const int room = GC_SMEM_CAP - 2 * GC_SB - GC_FOLDB - GC_FIXED;
-  const int k = room / (mi * PL_REC + wcols * GC_RAWLD);
-  return k < GC_MAXRAW ? k : GC_MAXRAW;
-}
-size_t gp_smem(int mi, int wcols) {
-  return (size_t)2 * GC_SB + GC_FOLDB + GC_FIXED +
-         (size_t)gp_nraw(mi, wcols) * (mi * PL_REC + wcols * GC_RAWLD);
-}
-
-template <bool BULK>
-__global__ void __launch_bounds__(GC_THREADS, 1)
-    k_gram_pl(const uint8_t* __restrict__ vpl, size_t pstride, int voff, int k1, ColList<double> W,
-              int k2, int n, int ntn, const double* __restrict__ wd, double* __restrict__ partial,
-              int nchunks, int nraw) {
+__global__ void __launch_bounds__(GP_THREADS, 1)
+    k_gram_pp(const uint8_t* __restrict__ vpl, int ldv, int voff, int k1,
+              const uint8_t* __restrict__ wpl, int ldw, int woff, int k2, int ntn,
+              double* __restrict__ partial, int nchunks, int nraw) {
   extern __shared__ __align__(1024) uint8_t smgc[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int mt = blockIdx.y / ntn, nt = blockIdx.y % ntn;
   const int i0 = mt * GC_MI, j0 = nt * GC_N;
   const int mi = min(GC_MI, k1 - i0), nj = min(GC_N, k2 - j0);
-  const int wcols = nj + (wd ? 1 : 0);     // raw FP64 columns: W, then the diagonal
-  const int VB = mi * PL_REC;               // V record bytes per chunk
-  const int RC = VB + wcols * GC_RAWLD;
+  const int VB = mi * PL_REC, RC = VB + nj * PL_REC;
   constexpr uint32_t ncols = 2 * D8_NL * GC_N;
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smgc) + 1023) & ~(uintptr_t)1023);
@@ -937,31 +956,25 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   int* gE = reinterpret_cast<int*>(gT + TC_M * GC_N);
   uint8_t* rawbase = reinterpret_cast<uint8_t*>(gE + TC_M * GC_N);
   int* cex = reinterpret_cast<int*>(rawbase + nraw * RC);
-  uint64_t* mfull = reinterpret_cast<uint64_t*>(cex + 3 * GC_CE);
-  uint64_t* mempty = mfull + 2;
-  uint64_t* maccf = mfull + 4;
-  uint64_t* macce = mfull + 6;
-  uint64_t* mraw = mfull + 8;
+  uint64_t* mempty = reinterpret_cast<uint64_t*>(cex + 3 * GC_CE);  // stage MMAs done (2)
+  uint64_t* maccf = mempty + 2;   // chunk accumulators complete (2)
+  uint64_t* macce = mempty + 4;   // chunk accumulators folded (2)
+  uint64_t* mraw = mempty + 6;    // raw chunk arrived (nraw)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mraw + GC_MAXRAW);
   const int cbase = nchunks / (int)gridDim.x, crem = nchunks % (int)gridDim.x;
   const int nch = cbase + ((int)blockIdx.x < crem ? 1 : 0);
   const int cfirst = (int)blockIdx.x * cbase + min((int)blockIdx.x, crem);
-  auto wptr = [&](int c) -> const double* { return c < nj ? W.p[j0 + c] : wd; };
-  auto vrec = [&](int i, int chunk) -> const uint8_t* {
-    return vpl + (size_t)(voff + i0 + i) * pstride + (size_t)chunk * PL_REC;
-  };
 
   if (warp == 0) gcge::tc::tmem_alloc(tslot, ncols);
   if (tid == 0) {
     for (int b = 0; b < 2; b++) {
-      gcge::tc::mbar_init(&mfull[b], GC_SW);
       gcge::tc::mbar_init(&mempty[b], 1);
       gcge::tc::mbar_init(&maccf[b], 1);
-      gcge::tc::mbar_init(&macce[b], GC_FW);
+      gcge::tc::mbar_init(&macce[b], GP_FW);
     }
     for (int b = 0; b < nraw; b++) gcge::tc::mbar_init(&mraw[b], 1);
   }
-  for (int e = tid; e < TC_M * GC_N; e += GC_THREADS) {
+  for (int e = tid; e < TC_M * GC_N; e += GP_THREADS) {
     gS[e] = 0.0;
     gT[e] = 0;
     gE[e] = -1000000;
@@ -972,56 +985,87 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   const uint32_t tmem = *tslot;
   bool ok = true;
 
-  if (warp == GC_PW) {
-    // ------------------------------------------------ producer / MMA warp
-    auto issue_raw = [&](int cc) {
-      const int chunk = cfirst + cc;
-      const int row0 = chunk * GC_K;
-      const int valid = min(GC_K, n - row0);
-      const int rows = BULK ? (valid & ~1) : 0;
-      uint64_t* mb = &mraw[cc % nraw];
-      if (lane == 0) gcge::tc::mbar_arrive_expect_tx(mb, (uint32_t)(VB + wcols * rows * 8));
-      __syncwarp();
-      uint8_t* dst = rawbase + (cc % nraw) * RC;
-      for (int i = lane; i < mi; i += 32)
-        gcge::tc::bulk_g2s(dst + i * PL_REC, vrec(i, chunk), (uint32_t)PL_REC, mb);
-      if (rows > 0)
-        for (int c = lane; c < wcols; c += 32)
-          gcge::tc::bulk_g2s(dst + VB + c * GC_RAWLD, wptr(c) + row0, (uint32_t)(rows * 8), mb);
-    };
-    for (int cc = 0; cc < nraw && cc < nch; cc++) issue_raw(cc);
+  // chunk cc of this CTA's run into raw buffer cc % nraw (thread 0)
+  auto issue_raw = [&](int cc) {
+    const int chunk = cfirst + cc;
+    uint64_t* mb = &mraw[cc % nraw];
+    uint8_t* dst = rawbase + (cc % nraw) * RC;
+    gcge::tc::mbar_arrive_expect_tx(mb, (uint32_t)RC);
+    gcge::tc::bulk_g2s(dst, vpl + ((size_t)chunk * ldv + voff + i0) * PL_REC, (uint32_t)VB, mb);
+    gcge::tc::bulk_g2s(dst + VB, wpl + ((size_t)chunk * ldw + woff + j0) * PL_REC,
+                       (uint32_t)(nj * PL_REC), mb);
+  };
+
+  if (warp < GP_CW) {
+    // ------------------------------------------------ converter warps
+    if (tid == 0)
+      for (int cc = 0; cc < nraw && cc < nch; cc++) issue_raw(cc);
+    const int nwq = 4 * nj, nvq = 4 * mi;
     for (int c = 0; c < nch; c++) {
-      const int tb = c & 1;
-      if (c >= 2 && !gcge::tc::mbar_wait_warp(&macce[tb], ((c >> 1) - 1) & 1, TC_WAIT)) ok = false;
+      const int tb = c & 1, rb = c % nraw;
+      const uint8_t* rbuf = rawbase + rb * RC;
+      if (!gcge::tc::mbar_wait_warp(&mraw[rb], (c / nraw) & 1, TC_WAIT)) ok = false;
+      int* ce = cex + (c % 3) * GC_CE;
+      for (int i = tid; i < mi + nj; i += GP_CW * 32) {
+        const int e = *reinterpret_cast<const int*>(rbuf + i * PL_REC);
+        ce[i < mi ? i : TC_M + i - mi] = e;
+      }
       for (int st = 0; st < GC_ST; st++) {
         const int g = c * GC_ST + st, buf = g & 1;
-        if (!gcge::tc::mbar_wait_warp(&mfull[buf], (g >> 1) & 1, TC_WAIT)) ok = false;
-        if (lane == 0) {
-          gcge::tc::fence_after();
-          uint8_t* As = base + buf * GC_SB;
-          d8_issue<true>(tmem + (uint32_t)(tb * D8_NL * GC_N), gcge::tc::smem_u32(As),
-                         TC_M * TC_KS * 2, gcge::tc::smem_u32(As + TC_ABYTES), GC_N, st == 0);
-          gcge::tc::commit(&mempty[buf]);
-          if (st == GC_ST - 1) gcge::tc::commit(&maccf[tb]);
+        if (g >= 2 && !gcge::tc::mbar_wait_warp(&mempty[buf], ((g >> 1) - 1) & 1, TC_WAIT))
+          ok = false;
+        uint8_t* As = base + buf * GC_SB;
+        uint8_t* Bs = As + TC_ABYTES;
+        for (int u = tid; u < nwq + nvq; u += GP_CW * 32) {
+          if (u < nwq) {
+            const int col = u >> 2, q = u & 3;
+            pl_quad(rbuf + VB + col * PL_REC, st, q,
+                    Bs + (q >> 1) * (D8_S * GC_N * 16) + (col >> 3) * 128 + (col & 7) * 16 +
+                        (q & 1) * 8,
+                    GC_N * 16);
+          } else {
+            const int vq = u - nwq, col = vq >> 2, q = vq & 3;
+            pl_quad(rbuf + col * PL_REC, st, q,
+                    As + (q >> 1) * (TC_M / 8 * 128) + (col >> 3) * 128 + (col & 7) * 16 +
+                        (q & 1) * 8,
+                    TC_M * TC_KS * 2);
+          }
         }
-        __syncwarp();
+        gcge::tc::fence_proxy_async();
+        gcge::tc::named_sync(1, GP_CW * 32);
+        if (tid == 0) {
+          // the accumulator set of this chunk was folded (chunk c - 2)
+          if (st == 0 && c >= 2 &&
+              !gcge::tc::mbar_wait(&macce[tb], ((c >> 1) - 1) & 1, TC_WAIT))
+            ok = false;
+          gcge::tc::fence_after();
+          d8_issue<true>(tmem + (uint32_t)(tb * D8_NL * GC_N), gcge::tc::smem_u32(As),
+                         TC_M * TC_KS * 2, gcge::tc::smem_u32(Bs), GC_N, st == 0);
+          gcge::tc::commit(&mempty[buf]);
+          if (st == GC_ST - 1) {
+            gcge::tc::commit(&maccf[tb]);
+            // every converter is past this chunk's raw buffer: refill it
+            if (c + nraw < nch) issue_raw(c + nraw);
+          }
+        }
+        __syncwarp();  // warp 0 converges again before its next aligned barrier
       }
-      if (c + nraw < nch) issue_raw(c + nraw);
     }
-  } else if (warp >= GC_SW) {
-    // ------------------------------------------------ fold warps (as k_gram_tc)
-    const int q4 = warp - GC_SW;
+  } else {
+    // ------------------------------------------------ fold warps
+    const int fw = warp - GP_CW;
+    const int q4 = warp & 3, jh = fw >> 2;  // lane quadrant, W column half
     const int i = 32 * q4 + lane;
     for (int c = 0; c < nch; c++) {
       const int tb = c & 1;
       if (!gcge::tc::mbar_wait_warp(&maccf[tb], (c >> 1) & 1, TC_WAIT)) ok = false;
       gcge::tc::fence_after();
-      if (32 * q4 < mi) {
+      if (32 * q4 < mi && 8 * jh < nj) {
         const int* ce = cex + (c % 3) * GC_CE;
         const int ea = ce[i];
         const uint32_t tacc = tmem + (uint32_t)(tb * D8_NL * GC_N) + ((uint32_t)(32 * q4) << 16);
 #pragma unroll
-        for (int c0 = 0; c0 < GC_N; c0 += 4) {
+        for (int c0 = 8 * jh; c0 < 8 * jh + 8; c0 += 4) {
           uint32_t acc[D8_NL][4];
 #pragma unroll
           for (int l = 0; l < D8_NL; l++)
@@ -1061,107 +1105,11 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
       __syncwarp();
       if (lane == 0) gcge::tc::mbar_arrive(&macce[tb]);
     }
-  } else {
-    // ------------------------------------------------ slicer warps
-    // per stage: W quads first (the costly cuts, on threads 0 ..), then V
-    // quads (byte -> f16), lane = (column c, quad q = rows 4q .. 4q+3)
-    const int nwq = 4 * nj, nvq = 4 * mi;
-    const int st0 = warp * 32 + lane;
-    for (int c = 0; c < nch; c++) {
-      const int cb = cfirst + c;
-      const int row0 = cb * GC_K;
-      const int valid = min(GC_K, n - row0);
-      const int rb = c % nraw;
-      uint8_t* rbuf = rawbase + rb * RC;
-      double* raw = reinterpret_cast<double*>(rbuf + VB);
-      if (!gcge::tc::mbar_wait_warp(&mraw[rb], (c / nraw) & 1, TC_WAIT)) ok = false;
-      const int rfill = BULK ? (valid & ~1) : 0;
-      if (rfill < GC_K) {  // W rows the bulk copy did not bring: tail row, zero padding
-        const int nr = GC_K - rfill;
-        for (int e = st0; e < wcols * nr; e += GC_SW * 32) {
-          const int col = e / nr, rr = rfill + e % nr;
-          raw[col * (GC_RAWLD / 8) + rr] = rr < valid ? __ldg(wptr(col) + row0 + rr) : 0.0;
-        }
-        gcge::tc::named_sync(1, GC_SW * 32);
-      }
-      int* ce = cex + (c % 3) * GC_CE;
-      // V exponents from the record headers; W exponents as in k_gram_tc
-      for (int i = st0; i < mi; i += GC_SW * 32) ce[i] = *reinterpret_cast<const int*>(rbuf + i * PL_REC);
-      for (int col = warp; col < nj; col += GC_SW) {
-        const double2 v2 = *reinterpret_cast<const double2*>(raw + col * (GC_RAWLD / 8) + 2 * lane);
-        int f0 = (__double2hiint(v2.x) >> 20) & 0x7FF, f1 = (__double2hiint(v2.y) >> 20) & 0x7FF;
-        int bad = (f0 == 0x7FF) | (f1 == 0x7FF);
-        if (wd) {
-          const double2 w2 = *reinterpret_cast<const double2*>(raw + nj * (GC_RAWLD / 8) + 2 * lane);
-          const int g0 = (__double2hiint(w2.x) >> 20) & 0x7FF,
-                    g1 = (__double2hiint(w2.y) >> 20) & 0x7FF;
-          bad |= (g0 == 0x7FF) | (g1 == 0x7FF);
-          f0 = (f0 == 0 || g0 == 0) ? 0 : max(f0 + g0 - 1022, 1);
-          f1 = (f1 == 0 || g1 == 0) ? 0 : max(f1 + g1 - 1022, 1);
-        }
-        const int fmax = __reduce_max_sync(0xffffffffu, max(f0, f1));
-        const int anybad = __reduce_or_sync(0xffffffffu, bad);
-        if (lane == 0) ce[TC_M + col] = anybad ? 4096 : (fmax == 0 ? -2000 : fmax - 1022);
-      }
-      gcge::tc::named_sync(1, GC_SW * 32);
-      for (int st = 0; st < GC_ST; st++) {
-        const int g = c * GC_ST + st, buf = g & 1;
-        if (g >= 2 && !gcge::tc::mbar_wait_warp(&mempty[buf], ((g >> 1) - 1) & 1, TC_WAIT))
-          ok = false;
-        uint8_t* As = base + buf * GC_SB;
-        uint8_t* Bs = As + TC_ABYTES;
-        for (int u = st0; u < nwq + nvq; u += GC_SW * 32) {
-          if (u < nwq) {
-            const GcQuad q = gc_quad(u, nj);
-            const double* src = raw + q.col * (GC_RAWLD / 8) + st * TC_KS + q.roff;
-            const double2 a01 = *reinterpret_cast<const double2*>(src);
-            const double2 a23 = *reinterpret_cast<const double2*>(src + 2);
-            double v[4] = {a01.x, a01.y, a23.x, a23.y};
-            if (wd) {
-              const double* ws = raw + nj * (GC_RAWLD / 8) + st * TC_KS + q.roff;
-              const double2 w01 = *reinterpret_cast<const double2*>(ws);
-              const double2 w23 = *reinterpret_cast<const double2*>(ws + 2);
-              v[0] *= w01.x;
-              v[1] *= w01.y;
-              v[2] *= w23.x;
-              v[3] *= w23.y;
-            }
-            const int E0 = ce[TC_M + q.col];
-            int E[4];
-#pragma unroll
-            for (int t = 0; t < 4; t++) {
-              E[t] = E0;
-              if (E0 >= 4096) v[t] = 0.0;
-            }
-            uint8_t* dst = Bs + q.g * (D8_S * GC_N * 16) + (q.col >> 3) * 128 + (q.col & 7) * 16 +
-                           q.h * 8;
-            d8h_slice4(v, E, dst, GC_N * 16);
-          } else {
-            const int vq = u - nwq;
-            const int col = vq >> 2, qq = vq & 3;
-            const uint8_t* src = rbuf + col * PL_REC + PL_HDR + st * PL_STB + qq * 4;
-            uint8_t* dst = As + (qq >> 1) * (TC_M / 8 * 128) + (col >> 3) * 128 + (col & 7) * 16 +
-                           (qq & 1) * 8;
-#pragma unroll
-            for (int a = 0; a < D8_S; a++) {
-              const uint32_t w = *reinterpret_cast<const uint32_t*>(src + a * TC_KS);
-              uint2 o;
-              o.x = pl_f16x2(w, 0x4140);
-              o.y = pl_f16x2(w, 0x4342);
-              *reinterpret_cast<uint2*>(dst + a * (TC_M * TC_KS * 2)) = o;
-            }
-          }
-        }
-        gcge::tc::fence_proxy_async();
-        __syncwarp();
-        if (lane == 0) gcge::tc::mbar_arrive(&mfull[buf]);
-      }
-    }
   }
   const int anybad = __syncthreads_or(ok ? 0 : 1);
   if (anybad && tid == 0) atomicExch(&g_oz_tc_status, 1);
   double* out = partial + (size_t)blockIdx.x * k1 * k2;
-  for (int e = tid; e < mi * nj; e += GC_THREADS) {
+  for (int e = tid; e < mi * nj; e += GP_THREADS) {
     const int ii = e % mi, jj = e / mi;
     const int o = jj * TC_M + ii;
     gc_flush(gT + o, gE + o, gS + o);
@@ -1176,23 +1124,20 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   }
 }
 
-template <bool BULK>
-int gram_pl_all(const uint8_t* vpl, size_t pstride, int voff, int k1, const ColList<double>& W,
-                int k2, int n, const double* wd, double* partial, cudaStream_t st) {
+int gram_pp_all(const uint8_t* vpl, int ldv, int voff, int k1, const uint8_t* wpl, int ldw,
+                int woff, int k2, int n, double* partial, cudaStream_t st) {
   const int ntm = (k1 + GC_MI - 1) / GC_MI, ntn = (k2 + GC_N - 1) / GC_N;
   const int nchunks = (n + GC_K - 1) / GC_K;
-  const int mi = k1 < GC_MI ? k1 : GC_MI;
-  const int wcols = (k2 < GC_N ? k2 : GC_N) + (wd ? 1 : 0);
-  const int nraw = gp_nraw(mi, wcols);
+  const int mi = k1 < GC_MI ? k1 : GC_MI, nj = k2 < GC_N ? k2 : GC_N;
+  const int nraw = gp_nraw(mi, nj);
   const int nblk = nchunks < 152 ? nchunks : 152;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_gram_pl<BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         GC_SMEM_CAP);
+    cudaFuncSetAttribute(k_gram_pp, cudaFuncAttributeMaxDynamicSharedMemorySize, GC_SMEM_CAP);
     attr = true;
   }
-  k_gram_pl<BULK><<<dim3(nblk, ntm * ntn), GC_THREADS, gp_smem(mi, wcols), st>>>(
-      vpl, pstride, voff, k1, W, k2, n, ntn, wd, partial, nchunks, nraw);
+  k_gram_pp<<<dim3(nblk, ntm * ntn), GP_THREADS, gp_smem(mi, nj), st>>>(
+      vpl, ldv, voff, k1, wpl, ldw, woff, k2, ntn, partial, nchunks, nraw);
   return nblk;
 }
 
@@ -1279,26 +1224,27 @@ void gram_oz(const ColList<double>& V, int k1, const ColList<double>& W, int k2,
   gram_reduce_partials(k1, k2, nblk, sym, partial, G, ldg, st);
 }
 
-size_t planes_stride(int n) { return (size_t)((n + PL_K - 1) / PL_K) * PL_REC; }
+size_t planes_bytes(int n, int ldp) {
+  return (size_t)((n + PL_K - 1) / PL_K) * (size_t)ldp * PL_REC;
+}
 
-// Digit planes of the k columns of X into planes (column c at c * pstride).
-void cut_planes(const ColList<double>& X, int k, int n, uint8_t* planes, size_t pstride,
-                cudaStream_t st) {
+// Digit planes of the k columns of X into plane columns c0 .. c0 + k - 1 of a
+// set of ldp columns.
+void cut_planes(const ColList<double>& X, int k, int n, uint8_t* planes, int ldp, int c0,
+                cudaStream_t st, const double* d) {
   if (k <= 0 || n <= 0) return;
   const int nchunks = (n + PL_K - 1) / PL_K;
   const int gx = (nchunks + 4 * PL_WARPS - 1) / (4 * PL_WARPS);
-  k_cut_planes<<<dim3(gx, k), PL_WARPS * 32, 0, st>>>(X, n, nchunks, planes, pstride);
+  k_cut_planes<<<dim3(gx, k), PL_WARPS * 32, 0, st>>>(X, d, n, nchunks, planes, ldp, c0);
 }
 
-// G = V^T diag(wdiag) W with V = the plane columns voff .. voff + k1 - 1.
-void gram_oz_planes(const uint8_t* planes, size_t pstride, int voff, int k1,
-                    const ColList<double>& W, int k2, int n, double* G, int ldg, double* partial,
-                    cudaStream_t st, const double* wdiag) {
+// G = V^T W with V = plane columns voff .. voff + k1 - 1 of a set of ldv and
+// W = plane columns woff .. woff + k2 - 1 of a set of ldw.
+void gram_oz_planes(const uint8_t* vpl, int ldv, int voff, int k1, const uint8_t* wpl, int ldw,
+                    int woff, int k2, int n, double* G, int ldg, double* partial,
+                    cudaStream_t st) {
   if (k1 <= 0 || k2 <= 0 || n <= 0) return;
-  bool vec = ((uintptr_t)wdiag & 15) == 0;
-  for (int j = 0; j < k2; j++) vec = vec && ((uintptr_t)W.p[j] & 15) == 0;
-  const int nblk = vec ? gram_pl_all<true>(planes, pstride, voff, k1, W, k2, n, wdiag, partial, st)
-                       : gram_pl_all<false>(planes, pstride, voff, k1, W, k2, n, wdiag, partial, st);
+  const int nblk = gram_pp_all(vpl, ldv, voff, k1, wpl, ldw, woff, k2, n, partial, st);
   gram_reduce_partials(k1, k2, nblk, false, partial, G, ldg, st);
 }
 

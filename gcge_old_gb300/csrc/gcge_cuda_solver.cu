@@ -280,7 +280,7 @@ struct GCGE_CUDA_SOLVER_ {
   // by its Gram passes and the Rayleigh-Ritz Gram of the same iteration;
   // plane_n = 0 outside that window
   uint8_t* planes = nullptr;
-  size_t pstride = 0;
+  uint8_t* wplanes = nullptr;  // the other operand's planes (bs columns)
   int plane_n = 0;
   std::vector<double*> plane_src;
   size_t partial_len = 0;
@@ -575,7 +575,8 @@ static void free_ws(Solver* s) {
   cudaFree(s->oz_scratch);
   s->oz_scratch = nullptr;
   cudaFree(s->planes);
-  s->planes = nullptr;
+  cudaFree(s->wplanes);
+  s->planes = s->wplanes = nullptr;
   s->plane_n = 0;
   cudaFree(s->d_int);
   cudaFree(s->bcg_mem);
@@ -758,8 +759,8 @@ extern "C" int GCGE_CUDA_SOLVER_Setup(GCGE_CUDA_SOLVER* s) {
   CU(cudaMalloc(&s->jac_work, sizeof(double) * gcge::jacobi_work_doubles(s->mx)));
   CU(cudaMalloc(&s->oz_scratch, gcge::lincomb_oz_scratch_bytes(s->mx, s->mx)));
   if (s->para.gemm == 1 || s->para.gemm == 3) {
-    s->pstride = gcge::planes_stride(s->n);
-    CU(cudaMalloc(&s->planes, s->pstride * (size_t)s->mx));
+    CU(cudaMalloc(&s->planes, gcge::planes_bytes(s->n, s->mx)));
+    CU(cudaMalloc(&s->wplanes, gcge::planes_bytes(s->n, s->bs)));
     s->plane_src.assign(s->mx, nullptr);
   }
   s->plane_n = 0;
@@ -879,8 +880,8 @@ static void gram(Solver* s, const ColList<double>& V, int k1, const ColList<doub
 static bool planes_cover(Solver* s, int k) {
   if (!s->planes || k <= 0) return false;
   if (k > s->plane_n) {
-    gcge::cut_planes(cols(s->V, s->plane_n, k), k - s->plane_n, s->n,
-                     s->planes + (size_t)s->plane_n * s->pstride, s->pstride, s->st);
+    gcge::cut_planes(cols(s->V, s->plane_n, k), k - s->plane_n, s->n, s->planes, s->mx,
+                     s->plane_n, s->st);
     s->launches++;
     for (int i = s->plane_n; i < k; i++) s->plane_src[i] = s->V[i];
     s->plane_n = k;
@@ -994,7 +995,7 @@ static int w_orth(Solver* s, int start, int* end) {
   // [X, P] is fixed during the orthogonalisation and the Rayleigh-Ritz step
   // that follows: its digit planes are cut once here
   s->plane_n = 0;
-  const bool pl = oz && start > 0 && planes_cover(s, start);
+  const bool pl = oz && start > 0 && *end - start <= s->bs && planes_cover(s, start);
   if (start > 0) {
     double vi = 1.0;
     int it = 0;
@@ -1005,13 +1006,16 @@ static int w_orth(Solver* s, int start, int* end) {
       ColList<double> W = cols(s->V, start, *end);
       ColList<double> T = cols(s->V_tmp, 0, l2);
       ColList<double> V1 = cols(s->V, 0, start);
-      if (pl && (bdiag || !s->B)) {
-        KL(gcge::gram_oz_planes(s->planes, s->pstride, 0, start, W, l2, s->n, s->sub_tmp2, start,
-                                s->partial, s->st, bdiag));
-      } else if (pl) {
-        KL(gcge::apply_b_f64(Bptr(s), W, T, l2, s->n, s->st));
-        KL(gcge::gram_oz_planes(s->planes, s->pstride, 0, start, T, l2, s->n, s->sub_tmp2, start,
-                                s->partial, s->st));
+      if (pl) {
+        // W's planes (B W, or W weighted by a diagonal B), then the plane Gram
+        if (bdiag || !s->B) {
+          KL(gcge::cut_planes(W, l2, s->n, s->wplanes, s->bs, 0, s->st, bdiag));
+        } else {
+          KL(gcge::apply_b_f64(Bptr(s), W, T, l2, s->n, s->st));
+          KL(gcge::cut_planes(T, l2, s->n, s->wplanes, s->bs, 0, s->st));
+        }
+        KL(gcge::gram_oz_planes(s->planes, s->mx, 0, start, s->wplanes, s->bs, 0, l2, s->n,
+                                s->sub_tmp2, start, s->partial, s->st));
       } else if (oz && (bdiag || !s->B)) {
         KL(gcge::gram_oz(V1, start, W, l2, s->n, s->sub_tmp2, start, false, s->partial, s->st,
                          bdiag));
@@ -1062,10 +1066,11 @@ static int vtaw(Solver* s, int start_W, int start_V, int end_V, double* smat) {
   // one Gram [V[start_V:xpl], W]^T (A W), then the W^T A W block is made
   // symmetric from its upper triangle (the "sym" product of the reference)
   ColList<double> VV = cols(s->V, start_V, end_V);
-  if (planes_valid(s, start_V, end_V))
-    KL(gcge::gram_oz_planes(s->planes, s->pstride, start_V, end_V - start_V, AW, wl, s->n,
-                            smat + start_V, end_V, s->partial, s->st));
-  else
+  if (planes_valid(s, start_V, end_V) && wl <= s->bs) {
+    KL(gcge::cut_planes(AW, wl, s->n, s->wplanes, s->bs, 0, s->st));
+    KL(gcge::gram_oz_planes(s->planes, s->mx, start_V, end_V - start_V, s->wplanes, s->bs, 0, wl,
+                            s->n, smat + start_V, end_V, s->partial, s->st));
+  } else
     KL(gram(s, VV, end_V - start_V, AW, wl, smat + start_V, end_V, false));
   KL((k_mirror_upper<<<(wl * wl + 127) / 128, 128, 0, s->st>>>(smat + xpl, end_V, wl)));
   return GCGE_CUDA_OK;

@@ -108,6 +108,13 @@ SIGNATURES = {
     "GCGE_CUDA_MultiVecGetToHost": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]),
     "GCGE_CUDA_OpsGetError": (C.c_int, []),
     "GCGE_CUDA_OpsClearError": (None, []),
+    "GCGE_CUDA_PlanesBytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "GCGE_CUDA_PlanesGramScratchDoubles": (C.c_size_t, [C.c_int, C.c_int]),
+    "GCGE_CUDA_PlanesCut": (C.c_int, [c_pp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.c_int, C.c_void_p]),
+    "GCGE_CUDA_PlanesGram": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                       C.c_void_p]),
     "GCGE_CUDA_MultiVecInnerProdPlanes": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,
                                                     C.c_void_p, C.c_void_p, C.c_int]),
     "GCGE_CUDA_MultiVecInnerProdNoAlloc": (C.c_int, [c_pp, C.c_int, c_pp, C.c_int, C.c_int,

@@ -228,6 +228,27 @@ int GCGE_CUDA_MultiVecInnerProdOzaki(double* const* V, int k1, double* const* W,
  * with the B-inner product of a diagonal B folded in). */
 int GCGE_CUDA_MultiVecInnerProdPlanes(double* const* V, int k1, double* const* W, int k2, int n,
                                       const double* wdiag, double* a, int lda);
+/* Digit planes, for a caller that multiplies the same block of columns by
+ * several others (the solver does: the basis [X, P] against each block
+ * Gram-Schmidt pass and the Rayleigh-Ritz block of one GCG iteration).  A
+ * plane set of ldp columns over n rows takes GCGE_CUDA_PlanesBytes(n, ldp)
+ * bytes of device memory (16-byte aligned); GCGE_CUDA_PlanesCut writes the
+ * columns X[0..k) (rows weighted by the device array wdiag when it is not
+ * NULL) as plane columns c0 .. c0+k-1; GCGE_CUDA_PlanesGram writes
+ * a[i + j*lda] = V_i . W_j (a DEVICE array) for V = plane columns
+ * voff .. voff+k1-1 of one set and W = plane columns woff .. woff+k2-1 of
+ * another, with FP64 accuracy (the digit scheme of
+ * GCGE_CUDA_MultiVecInnerProdOzaki), using `partial`
+ * (GCGE_CUDA_PlanesGramScratchDoubles(k1, k2) device doubles).  Both run
+ * asynchronously on the given cudaStream_t.  No counterpart in the reference
+ * (its MultiVecInnerProd, src/gcge_ops.h:113-114, is one call per product). */
+size_t GCGE_CUDA_PlanesBytes(int n, int ldp);
+size_t GCGE_CUDA_PlanesGramScratchDoubles(int k1, int k2);
+int GCGE_CUDA_PlanesCut(double* const* X, int k, int n, const double* wdiag, void* planes,
+                        int ldp, int c0, void* stream);
+int GCGE_CUDA_PlanesGram(const void* vplanes, int ldv, int voff, int k1, const void* wplanes,
+                         int ldw, int woff, int k2, int n, double* a, int lda, double* partial,
+                         void* stream);
 /* Allocation-free FP64 inner products (no counterpart in the reference):
  * the same a[i + j*lda] = V[i] . W[j] as GCGE_CUDA_MultiVecInnerProd, for
  * callers that must not allocate device memory (a fixed memory budget owned
