@@ -315,22 +315,63 @@ def reference_iters():
     return None, None
 
 
+CPU_FULL_RUN_FILE = os.path.join(HERE, "profiles", "cpu_port_full_solve_lap3d128.json")
+
+
+def cpu_calibration():
+    """The committed full (not sampled) solve of the oracle port on this
+    workload, for the extrapolation error of the bounded sample."""
+    if os.path.exists(CPU_FULL_RUN_FILE):
+        return json.load(open(CPU_FULL_RUN_FILE))
+    return None
+
+
 def cpu_sample(A, B, nev, x0, threads, fallback_iters, full_size=True,
-               fallback_src="GPU FP64 iteration count"):
-    """Oracle port on the host: start phase + one GCG iteration, extrapolated
-    to the full iteration count (the reference's own count on the full-size
-    workload, else fallback_iters)."""
+               fallback_src="GPU FP64 iteration count", loop_iters=3):
+    """Oracle port on the host: the start phase plus loop_iters GCG iterations
+    (their mean cost per iteration), extrapolated to the full iteration count
+    (the reference's own count on the full-size workload, else fallback_iters)."""
     from oracle import oracle as O
     p = O.default_para(nev, ev_tol=1e-10, ev_max_it=1000)
-    r = O.port_solve(A, B, nev, x0, p, max_outer=1, threads=threads)
+    r = O.port_solve(A, B, nev, x0, p, max_outer=loop_iters, threads=threads)
     iters, src = reference_iters() if full_size else (None, None)
     if iters is None:
         iters, src = fallback_iters, fallback_src
     t_iter = r["t_loop"] / max(1, r["loop_iters"])
     est = r["t_init"] + max(0, iters - 2) * t_iter
-    sample = ("oracle port, %d threads: start phase (X orth, RR, [X,W] step) %.2f s + 1 GCG iteration "
-              "%.2f s, extrapolated to %d iterations (%s)" % (threads, r["t_init"], t_iter, iters, src))
+    sample = ("oracle port, %d threads: start phase (X orth, RR, [X,W] step) %.2f s + %d GCG "
+              "iterations %.2f s each, extrapolated to %d iterations (%s)"
+              % (threads, r["t_init"], r["loop_iters"], t_iter, iters, src))
     return est, r["t_init"] + r["t_loop"], sample
+
+
+def cpu_full_run(args):
+    """--calibrate-cpu: one complete oracle-port solve of the workload on all
+    host threads, written to profiles/ as the calibration of the sampled CPU
+    baseline (a few minutes on 16 cores)."""
+    import platform
+    from oracle import oracle as O
+    A, B, nev, x0, m = workload(args.small)
+    threads = os.cpu_count() or 1
+    p = O.default_para(nev, ev_tol=1e-10, ev_max_it=1000)
+    r = O.port_solve(A, B, nev, x0, p, threads=threads)
+    est, _, sample = cpu_sample(A, B, nev, x0, threads, r["iters"], full_size=not args.small)
+    out = {"workload": "laplace3d_7pt_%d^3_diagmass_nev50_tol1e-10" % m,
+           "host": "%d threads, %s" % (threads, platform.machine()),
+           "full_solve_s": r["seconds"], "iters": r["iters"],
+           "sampled_estimate_s": est, "sample": sample,
+           "extrapolation_error": est / r["seconds"] - 1.0,
+           "command": "python bench.py --calibrate-cpu"}
+    if not args.small:
+        json.dump(out, open(CPU_FULL_RUN_FILE, "w"), indent=1)
+    print(json.dumps(out))
+    return 0
+
+
+def workload_config(A, nev, m):
+    return {"workload": "laplace3d_7pt_%d^3_diagmass_nev50_tol1e-10" % m, "n": A.n,
+            "nnz": A.nnz, "nev": nev, "block_size": 10, "parallelism": "replicas only",
+            "l2": "inputs larger than L2 (A 175 MB, basis 1.5 GB)"}
 
 
 def run_reference_arm(args):
@@ -344,7 +385,7 @@ def run_reference_arm(args):
     sample = ""
     for it in range(args.warmup + args.steps):
         est, w, sample = cpu_sample(A, B, nev, x0, threads, 60, full_size=not args.small,
-                                    fallback_src="an assumed 60 iterations")
+                                    fallback_src="an assumed 60 iterations", loop_iters=2)
         if it >= args.warmup:
             vals.append(est)
             wall.append(w)
@@ -353,10 +394,9 @@ def run_reference_arm(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(wall),
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded generator)",
-           "config": {"workload": "laplace3d_7pt_%d^3_diagmass_nev50_tol1e-10" % m,
-                      "n": A.n, "nnz": A.nnz, "nev": nev, "block_size": 10},
+           "config": workload_config(A, nev, m),
            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port",
-                            "sample": sample},
+                            "sample": sample, "calibration": cpu_calibration()},
            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
@@ -614,12 +654,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="48^3 grid (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--calibrate-cpu", action="store_true",
+                    help="run one full oracle-port solve and record it in profiles/")
     ap.add_argument("--c5n", type=int, default=8_000_000, help="graph size of --config 5")
     ap.add_argument("--c5it", type=int, default=100, help="GCG iteration cap of --config 5")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
                     help="3: the 160^3 27-point mixed-precision configuration (one solve each); "
                          "4: the 512^2 differentiation configuration (gradient checks)")
     args = ap.parse_args()
+    if args.calibrate_cpu:
+        return cpu_full_run(args)
     if args.impl == "reference":
         return run_reference_arm(args)
     if args.config == 3:
@@ -702,7 +746,8 @@ def main():
         threads = os.cpu_count() or 1
         est, wall, sample = cpu_sample(A, B, nev, x0, threads, st_fp64[-1]["num_iter"],
                                        full_size=not args.small)
-        cpu = {"value": est, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
+        cpu = {"value": est, "unit": "s", "cores": threads, "kind": "port", "sample": sample,
+               "calibration": cpu_calibration()}
 
     traffic = None
     tf = os.path.join(HERE, "profiles", "spmm_traffic.json")
@@ -715,9 +760,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1e3 * v_mixed, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (seeded generator)",
-        "config": {"workload": "laplace3d_7pt_%d^3_diagmass_nev50_tol1e-10" % m, "n": A.n,
-                   "nnz": A.nnz, "nev": nev, "block_size": 10, "parallelism": "replicas only",
-                   "l2": "inputs larger than L2 (A 175 MB, basis 1.5 GB)"},
+        "config": workload_config(A, nev, m),
         "fp64_s": v_fp64, "mixed_s": v_mixed, "mixed_speedup_vs_fp64": v_fp64 / v_mixed,
         "fp64_fma_products_s": t_fma[0],
         "tuned_inner_solve": dict(tuned, mixed_speedup_vs_fp64=tuned["fp64"]["s"] / tuned["mixed"]["s"]),
