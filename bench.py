@@ -12,16 +12,21 @@ value: seconds per solve of the mixed-precision form (FP32 block CG, FP64
 everything else) with the matrices and the initial block resident in HBM,
 timed with CUDA events on the solver's stream; fp64_s: the all-FP64 form
 (FP64 block CG; tall-skinny products FP64-accurate on the tensor cores in both
-forms); fp64_fma_products_s: one FP64 solve with those products on FP64 FMA
+forms); fp64_correction_form_s: the FP64 form with the mixed form's W step (the
+block-CG correction alone as the W block), so that mixed vs it differs in the
+precision of the block CG only; fp64_fma_products_s: one FP64 solve with those products on FP64 FMA
 units instead; tuned_inner_solve: one solve of each form with the block size
 and block-CG step cap that suit it (mixed 12 / 40, FP64 15 / 40; the
 reference's defaults 10 / 20 are what value uses).
 e2e: the same solve through the C ABI with HOST buffers: matrix upload,
 initial block upload and eigenvector download inside the timed region.
-roofline: the SpMM of the mixed solve's block CG: FP32 CSR SpMM on
-row-interleaved blocks (k = block size = 10), algorithmic bytes
-nnz*8 + 4(n+1) + 2*k*n*4 per launch; the FP64 SpMM rate (bound by GB300's
-FP64 FMA rate) is reported beside it.
+roofline: the Gram pass of the W orthogonalisation, the solve's largest
+kernel family: the digit-plane cut of W (diagonal B folded in) and the plane
+Gram [X,P]^T diag(b) W at 80 x 10 columns, algorithmic bytes (80+10+1)*n*8
+per pass; the per-iteration cut of the basis planes beside it.  rooflines:
+the SpMM of the mixed solve's block CG (FP32 CSR SpMM on row-interleaved
+blocks, k = 10, algorithmic bytes nnz*8 + 4(n+1) + 2*k*n*4 per launch) and
+the FP64 and FP32 column SpMMs.
 cpu_baseline: the oracle port (C restatement of the reference, OpenMP on all
 host cores) on a bounded sample of the same solve: the start phase plus one
 GCG iteration, extrapolated to the reference's iteration count.
@@ -32,8 +37,11 @@ sample, and prints the same metric.
 --config 3 instead runs the mixed-precision configuration of the headline
 once in each precision: 27-point Q1 variable-coefficient diffusion (per-cell
 kappa = exp(N(0,1))) with its consistent mass on a 160^3 grid (n = 4,096,000,
-nnz = 109,215,352), nev = 100, and reports both times and the per-pair
-difference of the mixed result from the FP64 one (not the default line).
+nnz = 109,215,352), nev = 100, at --c3tol (default 1e-11: with a mass matrix
+of size h^3 the residual bound 1e-10 leaves the eigenvalues free by more than
+1e-10 relative), and reports both times, the per-pair difference of the mixed
+result from the FP64 one and of each from the oracle port's solve
+(tests/golden/cfg3_port_summary.json) (not the default line).
 
 --config 4 runs the differentiation configuration: 2D anisotropic diffusion
 (5-point, per-cell kappa ~ U(0.5, 2), y-edges weighted 10) on a 512 x 512
@@ -147,8 +155,8 @@ class ClockSampler:
 def time_solves(torch, S, L, dA, dB, nev, x0_dev, precision, warmup, steps, gemm="ozaki", **kw):
     """Solves with device-resident inputs; returns (times_s, stats, eval, evec_dev)."""
     lib = L.load()
-    s = S.GCGESolver(dA, dB, nev, ev_tol=1e-10, ev_max_it=1000, precision=precision, gemm=gemm,
-                     **kw)
+    kw.setdefault("ev_tol", 1e-10)
+    s = S.GCGESolver(dA, dB, nev, ev_max_it=1000, precision=precision, gemm=gemm, **kw)
     evec_dev = torch.empty_like(x0_dev)
     L.check(lib.GCGE_CUDA_SOLVER_SetEigenvectorsDevice(s.handle, C.c_void_p(evec_dev.data_ptr())),
             "SetEigenvectorsDevice")
@@ -235,6 +243,64 @@ def spmm_roofline(torch, L, dA, A, k, launches=20):
     return t, nbytes, t32, nbytes32, trows
 
 
+def gram_roofline(torch, L, n, k1=80, k2=10, launches=10):
+    """The Gram of one block Gram-Schmidt pass of the W orthogonalisation at
+    the solve's shape, G = [X, P]^T diag(b) W (k1 = 80 basis columns, k2 = 10
+    W columns, a diagonal B): per pass the solver cuts W's digit planes (the
+    diagonal folded in, k_cut_planes) and runs the plane Gram (k_gram_pp and
+    its fixed-order reduction); the basis planes are cut once per GCG
+    iteration for all of that iteration's Gram products.  Algorithmic bytes of
+    the pass: (k1 + k2 + 1) n 8 (the FP64 operands and the diagonal, once)."""
+    lib = L.load()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    V = [torch.randn(n, dtype=torch.float64, device="cuda", generator=g) for _ in range(k1)]
+    W = [torch.randn(n, dtype=torch.float64, device="cuda", generator=g) for _ in range(k2)]
+    d = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) + 0.5
+    vp = (C.c_void_p * k1)(*[C.c_void_p(t.data_ptr()) for t in V])
+    wp = (C.c_void_p * k2)(*[C.c_void_p(t.data_ptr()) for t in W])
+    vpl = torch.empty(int(lib.GCGE_CUDA_PlanesBytes(n, k1)), dtype=torch.uint8, device="cuda")
+    wpl = torch.empty(int(lib.GCGE_CUDA_PlanesBytes(n, k2)), dtype=torch.uint8, device="cuda")
+    part = torch.empty(int(lib.GCGE_CUDA_PlanesGramScratchDoubles(k1, k2)), dtype=torch.float64,
+                       device="cuda")
+    G = torch.empty(k2, k1, dtype=torch.float64, device="cuda")
+    st = torch.cuda.Stream()
+    sp = C.c_void_p(st.cuda_stream)
+
+    def cut_v():
+        L.check(lib.GCGE_CUDA_PlanesCut(vp, k1, n, None, C.c_void_p(vpl.data_ptr()), k1, 0, sp),
+                "PlanesCut V")
+
+    def one_pass():
+        L.check(lib.GCGE_CUDA_PlanesCut(wp, k2, n, C.c_void_p(d.data_ptr()),
+                                        C.c_void_p(wpl.data_ptr()), k2, 0, sp), "PlanesCut W")
+        L.check(lib.GCGE_CUDA_PlanesGram(C.c_void_p(vpl.data_ptr()), k1, 0, k1,
+                                         C.c_void_p(wpl.data_ptr()), k2, 0, k2, n,
+                                         C.c_void_p(G.data_ptr()), k1, C.c_void_p(part.data_ptr()),
+                                         sp), "PlanesGram")
+
+    def timed(f, reps):
+        for _ in range(2):
+            f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            f()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    t_cut_v = timed(cut_v, launches)
+    t_pass = timed(one_pass, launches)
+    ref = torch.stack(V) @ (torch.stack(W) * d[None, :]).T
+    err = float(((G.T - ref).abs().max() / ref.abs().max()).item())
+    assert err < 1e-13, err
+    nbytes = (k1 + k2 + 1) * n * 8
+    cut_bytes = k1 * n * 8 + int(lib.GCGE_CUDA_PlanesBytes(n, k1))
+    return {"t_pass": t_pass, "bytes": nbytes, "t_cut_basis": t_cut_v, "cut_bytes": cut_bytes,
+            "max_rel_err_vs_fp64_matmul": err}
+
+
 def e2e_solves(torch, S, L, A, B, nev, x0, precision, warmup, steps):
     """Through the public C ABI with pinned HOST buffers: MatCreate (H2D of
     the CSR arrays), Solve reading the host initial block and writing host
@@ -307,6 +373,20 @@ def true_residuals_gpu(torch, A, B, ev, evec_rows):
     del a
     R = AX - lam[None, :] * BX
     return (R.norm(dim=0) / (lam.abs() * X.norm(dim=0))).cpu().numpy()
+
+
+GRAM_TRAFFIC_FILE = os.path.join(HERE, "profiles", "gram_traffic.json")
+CFG3_PORT_FILE = os.path.join(HERE, "tests", "golden", "cfg3_port_summary.json")
+
+
+def gram_traffic(n):
+    """DRAM bytes per W-orthogonalisation Gram pass from the committed ncu
+    capture (a smaller grid, scaled by the rows processed: the traffic of both
+    kernels grows in proportion), or None."""
+    if not os.path.exists(GRAM_TRAFFIC_FILE):
+        return None
+    d = json.load(open(GRAM_TRAFFIC_FILE))
+    return d["bytes_per_pass"] * n / d["n"]
 
 
 def reference_iters():
@@ -417,24 +497,34 @@ def run_config3(args):
     dA, dB = S.DeviceMatrix(A), S.DeviceMatrix(B)
     x0_dev = torch.from_numpy(x0).to("cuda")
     res = {}
+    evs = {}
     for prec in ("mixed", "fp64"):
-        t, st, ev, vec = time_solves(torch, S, L, dA, dB, nev, x0_dev, prec, 0, 1)
+        t, st, ev, vec = time_solves(torch, S, L, dA, dB, nev, x0_dev, prec, 0, 1,
+                                     ev_tol=args.c3tol)
         r = true_residuals_gpu(torch, A, B, ev, vec)
         res[prec] = {"s": t[0], "gcg_iterations": st[0]["num_iter"], "bcg_steps": st[0]["bcg_steps"],
-                     "max_residual": float(r.max()), "ev": ev,
+                     "max_residual": float(r.max()),
                      "phase_s": {k: round(v, 3) for k, v in st[0].items() if k.startswith("t_")}}
+        evs[prec] = ev
         del vec
         torch.cuda.empty_cache()
-    ev_m, ev_d = res["mixed"].pop("ev"), res["fp64"].pop("ev")
+    ev_m, ev_d = evs["mixed"], evs["fp64"]
     rel = np.abs(ev_m - ev_d) / np.abs(ev_d)
     out = {"metric": METRIC, "config": {"workload": "diffusion27_q1_lognormal_%d^3_consistent_mass_"
-                                                    "nev100_tol1e-10" % m,
+                                                    "nev100" % m, "ev_tol": args.c3tol,
                                         "n": A.n, "nnz_A": A.nnz, "nnz_B": B.nnz, "nev": nev},
            "unit": "s", "mixed": res["mixed"], "fp64": res["fp64"],
            "mixed_speedup_vs_fp64": res["fp64"]["s"] / res["mixed"]["s"],
            "per_pair_eigenvalue_rel_diff_mixed_vs_fp64": {"max": float(rel.max()),
                                                           "median": float(np.median(rel))},
            "generator_s": gen_s, "data": "synthetic (seeded generator)"}
+    # per pair against the oracle port's solve of the same matrices and start
+    if os.path.exists(CFG3_PORT_FILE):
+        ref = np.array(json.load(open(CFG3_PORT_FILE))["eval"])
+        out["per_pair_eigenvalue_rel_diff_vs_oracle_port"] = {
+            p: float(np.max(np.abs(evs[p] - ref) / np.abs(ref))) for p in evs}
+    if args.c3save:
+        np.savez(args.c3save, mixed=ev_m, fp64=ev_d, ev_tol=args.c3tol)
     print(json.dumps(out))
     return 0
 
@@ -658,6 +748,9 @@ def main():
                     help="run one full oracle-port solve and record it in profiles/")
     ap.add_argument("--c5n", type=int, default=8_000_000, help="graph size of --config 5")
     ap.add_argument("--c5it", type=int, default=100, help="GCG iteration cap of --config 5")
+    ap.add_argument("--c3tol", type=float, default=1e-11, help="ev_tol of --config 3")
+    ap.add_argument("--c3save", default="", help="--config 3: write both precisions' eigenvalues "
+                                                "to this .npz")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
                     help="3: the 160^3 27-point mixed-precision configuration (one solve each); "
                          "4: the 512^2 differentiation configuration (gradient checks)")
@@ -703,6 +796,11 @@ def main():
                                                          args.warmup, args.steps)
     t_fp64, st_fp64, ev_fp64, vec_fp64 = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64",
                                                      max(1, args.warmup // 3), max(1, args.steps // 2))
+    # the FP64 solve with the mixed form's W step (the correction e alone as the
+    # W block): mixed vs this is the ratio that only the precision changes
+    t_fcor, st_fcor, _, vec_fcor = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64", 0, 1,
+                                               w_form="correction")
+    del vec_fcor
     # the same FP64 solve with the tall-skinny products on FP64 FMA units instead of
     # the FP64-accurate tensor-core products (one solve: what the tensor cores buy)
     t_fma, st_fma, _, vec_fma = time_solves(torch, S, L, dA, dB, nev, x0_dev, "fp64", 0, 1,
@@ -735,6 +833,8 @@ def main():
     # algorithmic bytes of the k = 10 FP32 SpMM: A once, x and y once each
     # (the 2 padding floats of a 12-float row count as waste, not as work)
     ach = b_spmm32 / t_rows / 1e9
+    gr = gram_roofline(torch, L, A.n)
+    ach_g = gr["bytes"] / gr["t_pass"] / 1e9
 
     e2e_t, h2d, d2h, _, _ = e2e_solves(torch, S, L, A, B, nev, x0, "mixed", 1, max(1, args.steps // 2))
     e2e_v = statistics.mean(e2e_t)
@@ -762,22 +862,38 @@ def main():
         "data": "synthetic (seeded generator)",
         "config": workload_config(A, nev, m),
         "fp64_s": v_fp64, "mixed_s": v_mixed, "mixed_speedup_vs_fp64": v_fp64 / v_mixed,
+        "fp64_correction_form_s": t_fcor[0],
+        "mixed_speedup_vs_fp64_same_w_form": t_fcor[0] / v_mixed,
+        "mixed_speedup_vs_best_fp64": min(v_fp64, t_fcor[0]) / v_mixed,
         "fp64_fma_products_s": t_fma[0],
         "tuned_inner_solve": dict(tuned, mixed_speedup_vs_fp64=tuned["fp64"]["s"] / tuned["mixed"]["s"]),
-        "gcg_iterations": {"mixed": st_mixed[-1]["num_iter"], "fp64": st_fp64[-1]["num_iter"]},
+        "gcg_iterations": {"mixed": st_mixed[-1]["num_iter"], "fp64": st_fp64[-1]["num_iter"],
+                           "fp64_correction_form": st_fcor[0]["num_iter"]},
         "max_residual": {"mixed": float(res_m.max()), "fp64": float(res_d.max())},
         "eigenvalue_rel_diff_mixed_vs_fp64": ev_rel,
         "phase_s_mixed": {k: round(v, 4) for k, v in st_mixed[-1].items() if k.startswith("t_")},
         "w_orth_passes": {"mixed": st_mixed[-1]["w_orth_passes"],
                           "fp64": st_fp64[-1]["w_orth_passes"]},
-        "roofline": {"kernel": "k_rows_spmm<12> (FP32 CSR SpMM of the block CG, k=10, "
-                               "row-interleaved)", "bound": "hbm",
-                     "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes": b_spmm32, "us_per_launch": t_rows * 1e6,
-                     "fp32_column_spmm_gbs": b_spmm32 / t_spmm32 / 1e9,
-                     "fp64_column_spmm_gbs": b_spmm / t_spmm / 1e9,
-                     "fp64_note": "FP64 SpMM is bound by GB300's FP64 FMA rate (~1 TFLOP/s)"},
+        "roofline": {"kernel": "W-orthogonalisation Gram pass: k_cut_planes (W with the "
+                               "diagonal of B) + k_gram_pp + reduction, [X,P]^T diag(b) W, "
+                               "80 x 10 columns", "bound": "hbm",
+                     "achieved": ach_g, "peak": peak, "unit": "GB/s", "frac": ach_g / peak,
+                     "peak_source": peak_src, "traffic": gram_traffic(A.n),
+                     "algorithmic_bytes": gr["bytes"], "us_per_launch": gr["t_pass"] * 1e6,
+                     "basis_plane_cut": {"us": gr["t_cut_basis"] * 1e6, "bytes": gr["cut_bytes"],
+                                         "gbs": gr["cut_bytes"] / gr["t_cut_basis"] / 1e9,
+                                         "per": "GCG iteration (80 columns)"},
+                     "max_rel_err_vs_fp64_matmul": gr["max_rel_err_vs_fp64_matmul"]},
+        "rooflines": [
+            {"kernel": "k_rows_spmm<12> (FP32 CSR SpMM of the block CG, k=10, row-interleaved)",
+             "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+             "traffic": traffic, "algorithmic_bytes": b_spmm32, "us_per_launch": t_rows * 1e6},
+            {"kernel": "k_spmm<double> (FP64 CSR SpMM, k=10, columns)", "bound": "fp64 fma",
+             "achieved": b_spmm / t_spmm / 1e9, "unit": "GB/s",
+             "note": "bound by GB300's FP64 FMA rate (~1 TFLOP/s), not by HBM"},
+            {"kernel": "FP32 CSR SpMM, k=10, columns", "bound": "hbm",
+             "achieved": b_spmm32 / t_spmm32 / 1e9, "unit": "GB/s",
+             "frac": b_spmm32 / t_spmm32 / 1e9 / peak}],
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},

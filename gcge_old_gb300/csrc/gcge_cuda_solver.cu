@@ -828,12 +828,18 @@ static __global__ void k_maxdiff(ColList<double> A, ColList<double> B, int k, in
   atomicMax(out + 1, (unsigned long long)__double_as_longlong(v));
 }
 
+// Products with at most this many outputs (k1 k2; the CholQR2 Gram and
+// W R^-1 of a 10-column block) run on the FP64 FMA units: their FP64 work is
+// below the fixed per-chunk cost of the tensor-core pipelines, and plain FP64
+// is the reference's own arithmetic.
+constexpr int kSmallProduct = 256;
+
 // Tall-skinny Y = X C (+ beta Y) with the configured arithmetic.  With the
 // environment variable GCGE_CUDA_CHECK_GEMM set, every tensor-core product is
 // recomputed in FP64 and the largest difference is printed (diagnostics).
 static void lincomb(Solver* s, const ColList<double>& X, int k1, const double* C, int ldc,
                     const ColList<double>& Y, int k2, double beta, bool balance = false) {
-  if ((s->para.gemm == 1 || s->para.gemm == 2) && k1 > 0) {
+  if ((s->para.gemm == 1 || s->para.gemm == 2) && k1 > 0 && k1 * k2 > kSmallProduct) {
     static const bool check = getenv("GCGE_CUDA_CHECK_GEMM") != nullptr;
     if (check && beta == 0.0 && k2 <= (int)s->evec.size()) {
       // FP64 result into evec-sized debug columns
@@ -868,7 +874,7 @@ static void lincomb(Solver* s, const ColList<double>& X, int k1, const double* C
 // Tall-skinny G = V^T W with the configured arithmetic.
 static void gram(Solver* s, const ColList<double>& V, int k1, const ColList<double>& W, int k2,
                  double* G, int ldg, bool sym) {
-  if (s->para.gemm == 1 || s->para.gemm == 3)
+  if ((s->para.gemm == 1 || s->para.gemm == 3) && k1 * k2 > kSmallProduct)
     gcge::gram_oz(V, k1, W, k2, s->n, G, ldg, sym, s->partial, s->st);
   else
     gcge::gram_f64(V, k1, W, k2, s->n, G, ldg, sym, s->partial, s->st);

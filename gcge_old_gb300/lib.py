@@ -29,6 +29,13 @@ class PCGParam(C.Structure):
     _fields_ = [("max_it", C.c_int), ("rate", C.c_double)]
 
 
+class ChebParam(C.Structure):
+    """GCGE_CUDA_CHEB_PARAM: steps, residual target, polynomial degree and the
+    lower end of the Chebyshev interval (a fraction of the Gershgorin bound)."""
+    _fields_ = [("max_it", C.c_int), ("rate", C.c_double), ("degree", C.c_int),
+                ("lower_frac", C.c_double)]
+
+
 # GCGE_CUDA_MULTI_LINEAR_SOLVER(ctx, A, rhs, x, k, n, stream)
 MultiLinearSolver = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                 C.c_void_p)
@@ -87,6 +94,8 @@ SIGNATURES = {
     "GCGE_CUDA_MatDotMultiVecF32Async": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int, C.c_void_p]),
     "GCGE_CUDA_SOLVER_SetMultiLinearSolver": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "GCGE_CUDA_JacobiPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
+                                      C.c_void_p]),
+    "GCGE_CUDA_ChebyshevPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                       C.c_void_p]),
     "GCGE_CUDA_EigvecAdjointSolve": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_double_p, C.c_int,
                                               c_pp, c_pp, c_double_p, C.c_int, C.c_double,

@@ -123,6 +123,13 @@ class GCGESolver:
         self._pcg = L.PCGParam(max_it, rate)
         self.set_linear_solver(self._lib.GCGE_CUDA_JacobiPCG, self._pcg)
 
+    def use_chebyshev_pcg(self, max_it: int = 20, rate: float = 1e-2, degree: int = 4,
+                          lower_frac: float = 0.05):
+        """W step by GCGE_CUDA_ChebyshevPCG: block CG preconditioned by a
+        Chebyshev polynomial in diag(A)^-1 A."""
+        self._cheb = L.ChebParam(max_it, rate, degree, lower_frac)
+        self.set_linear_solver(self._lib.GCGE_CUDA_ChebyshevPCG, self._cheb)
+
     def solve(self, x0: np.ndarray | None = None):
         """x0: initial block, shape (nev, n) (= column-major n x nev); its first
         num_init_evec columns are used and the rest start pseudo-random (x0 =

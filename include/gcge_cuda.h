@@ -157,6 +157,23 @@ typedef struct GCGE_CUDA_PCG_PARAM_ {
 } GCGE_CUDA_PCG_PARAM;
 int GCGE_CUDA_JacobiPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs, double* const* x,
                         int k, int n, void* stream);
+/* A stock GCGE_CUDA_MULTI_LINEAR_SOLVER with a polynomial preconditioner, the
+ * GPU counterpart of the hypre app's preconditioned W-step solver
+ * (app/hypre/gcge_app_hypre.c:305-331): per column, CG preconditioned by
+ * `degree` steps of the Chebyshev semi-iteration in diag(A)^-1 A on
+ * [lower_frac b, b] (b the Gershgorin bound of diag(A)^-1 A; degree 0: the
+ * diagonal alone), stopping at ||r|| < rate ||r_0|| or max_it steps.  The step
+ * scalars stay on the device; the host reads the active-column count every
+ * 4 steps.  ctx points to a GCGE_CUDA_CHEB_PARAM (NULL: 20 steps, rate 1e-2,
+ * degree 4, lower_frac 0.05).  rhs is overwritten. */
+typedef struct GCGE_CUDA_CHEB_PARAM_ {
+  int max_it;
+  double rate;
+  int degree;
+  double lower_frac;
+} GCGE_CUDA_CHEB_PARAM;
+int GCGE_CUDA_ChebyshevPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs,
+                           double* const* x, int k, int n, void* stream);
 /* The CUDA stream (cudaStream_t) the solver runs on, for event timing. */
 int GCGE_CUDA_SOLVER_GetStream(GCGE_CUDA_SOLVER* solver, void** stream);
 int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* solver, int argc, char** argv);

@@ -101,6 +101,7 @@ def test_new_entry_points_check_arguments_without_gpu():
     assert lib.GCGE_CUDA_SOLVER_SetMultiLinearSolver(None, None, None) == 1
     assert lib.GCGE_CUDA_SOLVER_Free(C.byref(s)) == 0
     assert lib.GCGE_CUDA_JacobiPCG(None, None, None, None, 1, 10, None) == 1
+    assert lib.GCGE_CUDA_ChebyshevPCG(None, None, None, None, 1, 10, None) == 1
     ev = np.array([1.0, 2.0])
     assert lib.GCGE_CUDA_EigvecAdjointSolve(None, None, None, ev.ctypes.data_as(L.c_double_p), 2,
                                             None, None, None, 10, 1e-8, None) == 1

@@ -114,3 +114,42 @@ def test_jacobi_pcg_direct(cuda_lib):
         res = np.linalg.norm(bs[j] - As @ xs[j]) / np.linalg.norm(bs[j])
         assert res < 1e-7, (j, res)
     dA.close()
+
+
+def _residual_after(lib, A, b, steps, degree, rate=1e-14):
+    """||b - A x|| / ||b|| after `steps` Chebyshev-PCG steps from x = 0."""
+    from gpu_util import dev_cols, host
+    from gcge_old_gb300.solver import DeviceMatrix
+    dA = DeviceMatrix(A)
+    rs, rp = dev_cols(b[None, :].copy())
+    xs, xp = dev_cols(np.zeros((1, A.n)))
+    prm = L.ChebParam(steps, rate, degree, 0.05)
+    rc = lib.GCGE_CUDA_ChebyshevPCG(C.cast(C.pointer(prm), C.c_void_p), dA.handle, rp, xp, 1, A.n,
+                                    None)
+    assert rc == 0, lib.GCGE_CUDA_GetLastErrorMessage()
+    x = host(xs)[0]
+    return np.linalg.norm(b - A.to_scipy() @ x) / np.linalg.norm(b)
+
+
+def test_chebyshev_preconditioner_reduces_the_residual_faster(cuda_lib, problem):
+    """On the log-normal-coefficient 27-point matrix the polynomial preconditioner
+    takes the residual further in the same number of CG steps than diag(A)
+    alone, and the solve converges to the target."""
+    A, _, _ = problem
+    b = np.random.default_rng(0).standard_normal(A.n)
+    r_jac = _residual_after(cuda_lib, A, b, 12, 0)
+    r_cheb = _residual_after(cuda_lib, A, b, 12, 4)
+    assert r_cheb < 0.5 * r_jac, (r_cheb, r_jac)
+    assert _residual_after(cuda_lib, A, b, 200, 4, rate=1e-10) < 1e-10
+
+
+def test_chebyshev_pcg_w_step_matches_builtin(cuda_lib, problem):
+    """The W step by ChebyshevPCG (device-resident step scalars) gives the
+    built-in block CG's eigenpairs to the solve tolerance."""
+    A, B, x0 = problem
+    ev0, r0, st0 = _solve(A, B, x0)
+    ev1, r1, st1 = _solve(A, B, x0, setup=lambda s: s.use_chebyshev_pcg(max_it=40, rate=1e-3,
+                                                                       degree=4))
+    assert r0.max() < 1e-10 and r1.max() < 1e-10, (r0, r1)
+    np.testing.assert_allclose(ev1, ev0, rtol=1e-9)
+    assert st1["num_iter"] <= st0["num_iter"] + 2, (st1["num_iter"], st0["num_iter"])
