@@ -1230,7 +1230,15 @@ static int compute_w(Solver* s) {
   KL((k_scale_copy<<<g, 256, 0, s->st>>>(X, Wc, scalars(wsc), wl, s->n)));
   int launches = 0, steps;
   if (s->mls) {
-    // a user block solver replaces the block CG (GCGE_OPS.MultiLinearSolver)
+    // a user block solver replaces the block CG (GCGE_OPS.MultiLinearSolver);
+    // in the correction form (mixed precision, or w_form 1) it gets
+    // rhs - A w0 and a zero start, and its solution e is the W block
+    if (s->para.precision == 1 || s->para.w_form == 1) {
+      ColList<double> AW = cols(s->evec, 0, wl);
+      KL(gcge::spmm_f64(*Aop, Wc, AW, wl, s->st));
+      KL(gcge::axpby_f64(-1.0, AW, 1.0, R, wl, s->n, s->st));
+      for (int i = 0; i < wl; i++) CU(cudaMemsetAsync(Wc.p[i], 0, sizeof(double) * s->n, s->st));
+    }
     const int rc = s->mls(s->mls_ctx, s->A, R.p, Wc.p, wl, s->n, (void*)s->st);
     if (rc != 0) return set_err(GCGE_CUDA_ERR_NUMERIC, "user linear solver returned %d", rc);
     return GCGE_CUDA_OK;

@@ -36,6 +36,15 @@ class ChebParam(C.Structure):
                 ("lower_frac", C.c_double)]
 
 
+class AMGParam(C.Structure):
+    """GCGE_CUDA_AMG_PARAM: hierarchy depth and coarsest size, aggregation
+    strength, smoothed (1) or plain (0) prolongation, Chebyshev smoother degree
+    and interval ratio, AMG-PCG step cap and residual target."""
+    _fields_ = [("max_levels", C.c_int), ("coarse_size", C.c_int), ("strength", C.c_double),
+                ("smooth_p", C.c_int), ("cheb_degree", C.c_int), ("cheb_ratio", C.c_double),
+                ("pcg_max_it", C.c_int), ("pcg_rate", C.c_double)]
+
+
 # GCGE_CUDA_MULTI_LINEAR_SOLVER(ctx, A, rhs, x, k, n, stream)
 MultiLinearSolver = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                 C.c_void_p)
@@ -97,6 +106,19 @@ SIGNATURES = {
                                       C.c_void_p]),
     "GCGE_CUDA_ChebyshevPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                       C.c_void_p]),
+    "GCGE_CUDA_AMG_DefaultParam": (None, [C.c_void_p]),
+    "GCGE_CUDA_AMG_Create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "GCGE_CUDA_AMG_Destroy": (C.c_int, [C.c_void_p]),
+    "GCGE_CUDA_AMG_GetNumLevels": (C.c_int, [C.c_void_p, c_int_p]),
+    "GCGE_CUDA_AMG_GetLevelInfo": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_int_p,
+                                             c_double_p]),
+    "GCGE_CUDA_AMG_GetLevelCSR": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_int_p, c_int_p,
+                                            c_double_p]),
+    "GCGE_CUDA_AMG_GetAggregates": (C.c_int, [C.c_void_p, C.c_int, c_int_p]),
+    "GCGE_CUDA_AMG_Apply": (C.c_int, [C.c_void_p, c_pp, c_pp, C.c_int, C.c_void_p]),
+    "GCGE_CUDA_AMGPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
+                                   C.c_void_p]),
+    "GCGE_CUDA_AMG_GetLastSteps": (C.c_int, [C.c_void_p, c_int_p]),
     "GCGE_CUDA_EigvecAdjointSolve": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_double_p, C.c_int,
                                               c_pp, c_pp, c_double_p, C.c_int, C.c_double,
                                               c_int_p]),

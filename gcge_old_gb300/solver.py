@@ -63,6 +63,81 @@ class DeviceMatrix:
             pass
 
 
+class AMG:
+    """Smoothed-aggregation AMG hierarchy of a DeviceMatrix (GCGE_CUDA_AMG),
+    built on the GPU; the GPU counterpart of the BoomerAMG hierarchy the
+    reference reaches through its hypre app.  ``params``: fields of
+    GCGE_CUDA_AMG_PARAM (max_levels, coarse_size, strength, smooth_p,
+    cheb_degree, cheb_ratio, pcg_max_it, pcg_rate); the rest keep their
+    defaults.  The matrix must outlive the hierarchy."""
+
+    def __init__(self, A: DeviceMatrix, **params):
+        self._lib = L.load()
+        self.A = A
+        self.param = L.AMGParam()
+        self._lib.GCGE_CUDA_AMG_DefaultParam(C.byref(self.param))
+        for k, v in params.items():
+            if k not in dict(L.AMGParam._fields_):
+                raise ValueError("unknown AMG parameter %r" % k)
+            setattr(self.param, k, v)
+        h = C.c_void_p()
+        L.check(self._lib.GCGE_CUDA_AMG_Create(C.byref(h), A.handle, C.byref(self.param)),
+                "AMG_Create")
+        self.handle = h
+
+    @property
+    def num_levels(self) -> int:
+        n = C.c_int()
+        L.check(self._lib.GCGE_CUDA_AMG_GetNumLevels(self.handle, C.byref(n)), "AMG_GetNumLevels")
+        return n.value
+
+    def level_info(self, l: int) -> dict:
+        n, na, npp, lm = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        L.check(self._lib.GCGE_CUDA_AMG_GetLevelInfo(self.handle, l, C.byref(n), C.byref(na),
+                                                     C.byref(npp), C.byref(lm)), "AMG_GetLevelInfo")
+        return {"n": n.value, "nnz_a": na.value, "nnz_p": npp.value, "lmax": lm.value}
+
+    def level_csr(self, l: int, which: str = "A"):
+        """A_l, P_l or R_l (= P_l^T) as a scipy CSR matrix."""
+        import scipy.sparse as sp
+        info = self.level_info(l)
+        nxt = self.level_info(l + 1)["n"] if which in ("P", "R") else info["n"]
+        rows, cols, nnz = {"A": (info["n"], info["n"], info["nnz_a"]),
+                           "P": (info["n"], nxt, info["nnz_p"]),
+                           "R": (nxt, info["n"], info["nnz_p"])}[which]
+        rp = np.zeros(rows + 1, dtype=np.int32)
+        ci = np.zeros(max(nnz, 1), dtype=np.int32)
+        v = np.zeros(max(nnz, 1))
+        L.check(self._lib.GCGE_CUDA_AMG_GetLevelCSR(
+            self.handle, l, {"A": 0, "P": 1, "R": 2}[which], rp.ctypes.data_as(L.c_int_p),
+            ci.ctypes.data_as(L.c_int_p), v.ctypes.data_as(L.c_double_p)), "AMG_GetLevelCSR")
+        return sp.csr_matrix((v[:nnz], ci[:nnz], rp), shape=(rows, cols))
+
+    def aggregates(self, l: int = 0) -> np.ndarray:
+        a = np.zeros(self.level_info(l)["n"], dtype=np.int32)
+        L.check(self._lib.GCGE_CUDA_AMG_GetAggregates(self.handle, l, a.ctypes.data_as(L.c_int_p)),
+                "AMG_GetAggregates")
+        return a
+
+    @property
+    def last_steps(self) -> int:
+        s = C.c_int()
+        L.check(self._lib.GCGE_CUDA_AMG_GetLastSteps(self.handle, C.byref(s)), "AMG_GetLastSteps")
+        return s.value
+
+    def close(self):
+        if self.handle:
+            h = self.handle
+            self._lib.GCGE_CUDA_AMG_Destroy(C.byref(h))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class GCGESolver:
     """GCG eigensolver for A x = lambda B x on one GPU.
 
@@ -129,6 +204,13 @@ class GCGESolver:
         Chebyshev polynomial in diag(A)^-1 A."""
         self._cheb = L.ChebParam(max_it, rate, degree, lower_frac)
         self.set_linear_solver(self._lib.GCGE_CUDA_ChebyshevPCG, self._cheb)
+
+    def use_amg_pcg(self, amg: "AMG | None" = None, **params):
+        """W step by GCGE_CUDA_AMGPCG: CG preconditioned by one V-cycle of an AMG
+        hierarchy of A (built here from ``params`` when not given)."""
+        self._amg = amg if amg is not None else AMG(self.A, **params)
+        self.set_linear_solver(self._lib.GCGE_CUDA_AMGPCG, self._amg.handle)
+        return self._amg
 
     def solve(self, x0: np.ndarray | None = None):
         """x0: initial block, shape (nev, n) (= column-major n x nev); its first

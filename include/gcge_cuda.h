@@ -174,6 +174,57 @@ typedef struct GCGE_CUDA_CHEB_PARAM_ {
 } GCGE_CUDA_CHEB_PARAM;
 int GCGE_CUDA_ChebyshevPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs,
                            double* const* x, int k, int n, void* stream);
+
+/* ---------------------------------------------------------------- algebraic multigrid
+ * A smoothed-aggregation AMG hierarchy of a device matrix, built on the GPU,
+ * and the W-step solver that uses it.  The reference reaches an AMG through
+ * its hypre app: BoomerAMG-preconditioned solvers behind MultiLinearSolver
+ * (app/hypre/gcge_app_hypre.c:305-331, called at src/gcge_xpw.c:178-191) and
+ * the BoomerAMG hierarchy its multilevel eigensolver builds
+ * (pase/src/pase_mg.c:101-131).  Set-up: aggregation by a distance-2 maximal
+ * independent set of the strength graph, prolongation P = (I - w D^-1 A) T,
+ * Galerkin operators P^T A P, dense inverse of the coarsest level.  Solve:
+ * Chebyshev-smoothed V-cycles in FP32 on row-interleaved blocks.  The
+ * hierarchy keeps pointers to A's arrays: A must outlive it. */
+typedef struct GCGE_CUDA_AMG_ GCGE_CUDA_AMG;
+typedef struct GCGE_CUDA_AMG_PARAM_ {
+  int max_levels;     /* hierarchy depth cap, 1..16 (default 10) */
+  int coarse_size;    /* stop coarsening at this many rows or fewer, 1..512 (default 256) */
+  double strength;    /* aggregation graph: |a_ij| >= strength sqrt(a_ii a_jj) (default 0) */
+  int smooth_p;       /* 1 smoothed prolongation (default), 0 plain aggregation */
+  int cheb_degree;    /* Chebyshev smoother degree, pre and post, 1..16 (default 2) */
+  double cheb_ratio;  /* smoother interval [lambda_max / ratio, lambda_max] (default 30) */
+  int pcg_max_it;     /* AMG-PCG steps per call (default 20) */
+  double pcg_rate;    /* a column stops at ||r|| < pcg_rate ||r_0|| (default 1e-2) */
+} GCGE_CUDA_AMG_PARAM;
+void GCGE_CUDA_AMG_DefaultParam(GCGE_CUDA_AMG_PARAM* prm);
+/* Builds the hierarchy of A (symmetric, positive diagonal); prm NULL: defaults. */
+int GCGE_CUDA_AMG_Create(GCGE_CUDA_AMG** amg, const GCGE_CUDA_MAT* A,
+                         const GCGE_CUDA_AMG_PARAM* prm);
+int GCGE_CUDA_AMG_Destroy(GCGE_CUDA_AMG** amg);
+int GCGE_CUDA_AMG_GetNumLevels(const GCGE_CUDA_AMG* amg, int* nlev);
+/* Level l: rows, nonzeros of A_l and of P_l (0 on the coarsest level), and the
+ * lambda_max(D^-1 A_l) bound of its smoother; NULL outputs are skipped. */
+int GCGE_CUDA_AMG_GetLevelInfo(const GCGE_CUDA_AMG* amg, int l, int* n, int* nnz_a, int* nnz_p,
+                               double* lmax);
+/* Copies A_l (which = 0), P_l (1) or R_l = P_l^T (2) into host CSR arrays
+ * sized from GetLevelInfo (rows + 1 row pointers). */
+int GCGE_CUDA_AMG_GetLevelCSR(const GCGE_CUDA_AMG* amg, int l, int which, int* rowptr, int* col,
+                              double* val);
+/* The aggregate of every row of level l < nlev - 1, into host agg[n_l]. */
+int GCGE_CUDA_AMG_GetAggregates(const GCGE_CUDA_AMG* amg, int l, int* agg);
+/* One V-cycle x = M^-1 b for k <= 32 FP64 device columns, asynchronous on stream. */
+int GCGE_CUDA_AMG_Apply(GCGE_CUDA_AMG* amg, double* const* b, double* const* x, int k,
+                        void* stream);
+/* A stock GCGE_CUDA_MULTI_LINEAR_SOLVER: per column, CG on A x = rhs
+ * preconditioned by one V-cycle, stopping at ||r|| < pcg_rate ||r_0|| or after
+ * pcg_max_it steps; ctx is a GCGE_CUDA_AMG built on this A.  The residual of
+ * the start x is formed in FP64 (skipped when x is zero), the FP32 correction
+ * is added to x; rhs is overwritten.  k <= 32. */
+int GCGE_CUDA_AMGPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs, double* const* x,
+                     int k, int n, void* stream);
+/* AMG-PCG steps of the last GCGE_CUDA_AMGPCG call on this hierarchy. */
+int GCGE_CUDA_AMG_GetLastSteps(const GCGE_CUDA_AMG* amg, int* steps);
 /* The CUDA stream (cudaStream_t) the solver runs on, for event timing. */
 int GCGE_CUDA_SOLVER_GetStream(GCGE_CUDA_SOLVER* solver, void** stream);
 int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* solver, int argc, char** argv);

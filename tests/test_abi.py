@@ -102,6 +102,13 @@ def test_new_entry_points_check_arguments_without_gpu():
     assert lib.GCGE_CUDA_SOLVER_Free(C.byref(s)) == 0
     assert lib.GCGE_CUDA_JacobiPCG(None, None, None, None, 1, 10, None) == 1
     assert lib.GCGE_CUDA_ChebyshevPCG(None, None, None, None, 1, 10, None) == 1
+    assert lib.GCGE_CUDA_AMG_Create(None, None, None) == 1
+    assert lib.GCGE_CUDA_AMGPCG(None, None, None, None, 1, 10, None) == 1
+    assert lib.GCGE_CUDA_AMG_Apply(None, None, None, 1, None) == 1
+    prm = L.AMGParam()
+    lib.GCGE_CUDA_AMG_DefaultParam(C.byref(prm))
+    assert (prm.max_levels, prm.coarse_size, prm.smooth_p, prm.cheb_degree) == (10, 256, 1, 2)
+    assert (prm.pcg_max_it, prm.pcg_rate) == (20, 1e-2)
     ev = np.array([1.0, 2.0])
     assert lib.GCGE_CUDA_EigvecAdjointSolve(None, None, None, ev.ctypes.data_as(L.c_double_p), 2,
                                             None, None, None, 10, 1e-8, None) == 1

@@ -162,6 +162,28 @@ def test_solver_headline_workload_matches_reference(cuda_lib, precision):
     assert abs(st["num_iter"] - ref["iters"]) <= 5
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solver_diffusion27_workload_matches_oracle_port(cuda_lib, precision):
+    """The full-size 27-point workload (160^3 Q1 diffusion with log-normal
+    cell coefficients and its consistent mass, n = 4,096,000, nev 100) at
+    ev_tol 1e-11: eigenvalues against the oracle port's solve of the same
+    matrices and start (tests/golden/cfg3_port_summary.json, ev_tol 1e-12) to
+    1e-10 relative per pair, every pair at relative residual <= 1e-10."""
+    import json
+    import os
+    from conftest import GOLDEN
+    path = os.path.join(GOLDEN, "cfg3_port_summary.json")
+    if not os.path.exists(path):
+        pytest.skip("no oracle summary of the 27-point workload")
+    ref = json.load(open(path))
+    A, B = M.diffusion27(160, seed=0)
+    x0 = M.initial_block(A.n, 100, seed=0)
+    ev, vec, st = S.solve(A, B, 100, x0, ev_tol=1e-11, ev_max_it=1000, precision=precision)
+    rel = np.abs(ev - np.array(ref["eval"])) / np.abs(np.array(ref["eval"]))
+    assert rel.max() < EV_RTOL, rel.max()
+    assert O.true_residuals(A, B, ev, vec).max() <= 1e-10
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_solver_nev128_analytic(cuda_lib, precision):
     """nev = 128 (a 198-column basis: the projected matrices and the Cholesky
