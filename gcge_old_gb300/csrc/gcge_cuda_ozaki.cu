@@ -901,26 +901,33 @@ __device__ __forceinline__ uint32_t pl_f16x2(uint32_t word, uint32_t sel) {
 // of 64-row chunks.  Per chunk one bulk copy brings V's records and one W's
 // (the chunk-major plane layout makes each a contiguous block) into a ring of
 // raw buffers.  Roles:
-//  * 12 converter warps: per 16-row stage they turn the digit bytes of both
-//    operands into f16 digits in a double-buffered stage; after a named
-//    barrier over the 384 converters, thread 0 issues the stage's skewed MMAs
-//    into the chunk's level accumulators in tensor memory (two sets alternate)
-//    and commits them; thread 0 also issues the bulk copies;
+//  * warp 0, one thread: issues the bulk copies and, per 16-row stage once the
+//    stage is converted, the stage's skewed MMAs into the chunk's level
+//    accumulators in tensor memory (two sets alternate), committing them to
+//    the stage buffer's "empty" barrier;
+//  * 11 converter warps: per stage they turn the digit bytes of both operands
+//    into f16 digits (32-byte swizzled K-major operand layout) in a ring of
+//    GP_NS stage buffers and arrive on the buffer's "full" barrier; they run
+//    ahead of the MMAs by up to GP_NS stages, so conversion and MMA execution
+//    overlap;
 //  * 8 fold warps (two per TMEM lane quadrant, 8 W columns each): per chunk
 //    the exact level sums into a 64-bit fixed-point accumulator per output,
-//    rounded into an FP64 partial only when the chunk exponent changes.
-constexpr int GP_CW = 12;                       // converter warps
-constexpr int GP_FW = 8;                        // fold warps
-constexpr int GP_THREADS = (GP_CW + GP_FW) * 32;
-constexpr int GP_FIXED = 1024 + 3 * GC_CE * 4 + (8 + GC_MAXRAW) * 8 + 16;
+//    rounded into an FP64 partial only when the chunk exponent changes; each
+//    fold thread keeps its 8 outputs' state in registers and writes them at
+//    the end.
+constexpr int GP_CW = 11;                       // converter warps (warps 1 .. 11)
+constexpr int GP_FW = 8;                        // fold warps (warps 12 .. 19)
+constexpr int GP_THREADS = (1 + GP_CW + GP_FW) * 32;
+constexpr int GP_NS = 3;                        // stage buffers
+constexpr int GP_FIXED = 1024 + 3 * GC_CE * 4 + (2 * GP_NS + 4 + GC_MAXRAW) * 8 + 16;
 
 __host__ __device__ __forceinline__ int gp_nraw(int mi, int nj) {
-  const int room = GC_SMEM_CAP - 2 * GC_SB - GC_FOLDB - GP_FIXED;
+  const int room = GC_SMEM_CAP - GP_NS * GC_SB - GP_FIXED;
   const int k = room / ((mi + nj) * PL_REC);
   return k < GC_MAXRAW ? k : GC_MAXRAW;
 }
 size_t gp_smem(int mi, int nj) {
-  return (size_t)2 * GC_SB + GC_FOLDB + GP_FIXED + (size_t)gp_nraw(mi, nj) * (mi + nj) * PL_REC;
+  return (size_t)GP_NS * GC_SB + GP_FIXED + (size_t)gp_nraw(mi, nj) * (mi + nj) * PL_REC;
 }
 
 // the digit bytes of rows 4q .. 4q+3 of a record's stage -> 7 f16 digit pairs
@@ -938,6 +945,43 @@ __device__ __forceinline__ void pl_quad(const uint8_t* rec, int st, int q, uint8
   }
 }
 
+// The skewed MMAs of one 16-row stage on operands in the 32-byte swizzled
+// K-major layout: digit a of A (TC_M rows) at abase + (a - 1) * TC_M * 32,
+// digit b of B (GC_N rows) at bbase + (b - 1) * GC_N * 32.  Level L = a + b
+// accumulates at TMEM column (L - 2) * GC_N; FIRST (the chunk's first stage)
+// starts every level afresh.  Shapes and offsets are compile-time; the
+// descriptors are the base descriptors plus start-address increments (the
+// 14-bit address field does not carry: shared addresses are below 256 KB).
+template <bool FIRST>
+__device__ __forceinline__ void gp_issue(uint32_t tacc, uint32_t abase, uint32_t bbase) {
+  const uint64_t ad0 = gcge::tc::smem_desc_sw32(abase, 256);
+  const uint64_t bd0 = gcge::tc::smem_desc_sw32(bbase, 256);
+#pragma unroll
+  for (int a = 1; a <= D8_S; a++) {
+    const uint64_t ad = ad0 + (uint64_t)(((a - 1) * TC_M * 32) >> 4);
+    const int bmax = (9 - a) < D8_S ? (9 - a) : D8_S;
+    // levels a + 1 .. a + bmax; on the first stage level 2 (a = 1) and level
+    // 9 (a = 2, b = 7) are written first by a = 1 / a = 2 and must start fresh
+    if (FIRST && a == 2) {
+      gcge::tc::mma_bf16(tacc + (uint32_t)((a - 1) * GC_N), ad, bd0,
+                         gcge::tc::idesc_f16(TC_M, (bmax - 1) * GC_N), 1u);
+      gcge::tc::mma_bf16(tacc + (uint32_t)((a + D8_S - 2) * GC_N), ad,
+                         bd0 + (uint64_t)(((D8_S - 1) * GC_N * 32) >> 4),
+                         gcge::tc::idesc_f16(TC_M, GC_N), 0u);
+    } else {
+      gcge::tc::mma_bf16(tacc + (uint32_t)((a - 1) * GC_N), ad, bd0,
+                         gcge::tc::idesc_f16(TC_M, bmax * GC_N), (FIRST && a == 1) ? 0u : 1u);
+    }
+  }
+}
+
+// the fold state of one output: FP64 sum, 64-bit fixed-point value, exponent
+__device__ __forceinline__ void gp_flush(long long& T, int& E, double& S) {
+  if (T != 0) S += d8_to_double(T, E - 48);
+  T = 0;
+  E = -1000000;
+}
+
 __global__ void __launch_bounds__(GP_THREADS, 1)
     k_gram_pp(const uint8_t* __restrict__ vpl, int ldv, int voff, int k1,
               const uint8_t* __restrict__ wpl, int ldw, int woff, int k2, int ntn,
@@ -951,15 +995,13 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
   constexpr uint32_t ncols = 2 * D8_NL * GC_N;
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smgc) + 1023) & ~(uintptr_t)1023);
-  double* gS = reinterpret_cast<double*>(base + 2 * GC_SB);
-  long long* gT = reinterpret_cast<long long*>(gS + TC_M * GC_N);
-  int* gE = reinterpret_cast<int*>(gT + TC_M * GC_N);
-  uint8_t* rawbase = reinterpret_cast<uint8_t*>(gE + TC_M * GC_N);
+  uint8_t* rawbase = base + GP_NS * GC_SB;
   int* cex = reinterpret_cast<int*>(rawbase + nraw * RC);
-  uint64_t* mempty = reinterpret_cast<uint64_t*>(cex + 3 * GC_CE);  // stage MMAs done (2)
-  uint64_t* maccf = mempty + 2;   // chunk accumulators complete (2)
-  uint64_t* macce = mempty + 4;   // chunk accumulators folded (2)
-  uint64_t* mraw = mempty + 6;    // raw chunk arrived (nraw)
+  uint64_t* mfull = reinterpret_cast<uint64_t*>(cex + 3 * GC_CE);  // stage converted (GP_NS)
+  uint64_t* mempty = mfull + GP_NS;  // stage MMAs done (GP_NS)
+  uint64_t* maccf = mempty + GP_NS;  // chunk accumulators complete (2)
+  uint64_t* macce = maccf + 2;       // chunk accumulators folded (2)
+  uint64_t* mraw = macce + 2;        // raw chunk arrived (nraw)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mraw + GC_MAXRAW);
   const int cbase = nchunks / (int)gridDim.x, crem = nchunks % (int)gridDim.x;
   const int nch = cbase + ((int)blockIdx.x < crem ? 1 : 0);
@@ -967,80 +1009,72 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
 
   if (warp == 0) gcge::tc::tmem_alloc(tslot, ncols);
   if (tid == 0) {
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < GP_NS; b++) {
+      gcge::tc::mbar_init(&mfull[b], GP_CW);
       gcge::tc::mbar_init(&mempty[b], 1);
+    }
+    for (int b = 0; b < 2; b++) {
       gcge::tc::mbar_init(&maccf[b], 1);
       gcge::tc::mbar_init(&macce[b], GP_FW);
     }
     for (int b = 0; b < nraw; b++) gcge::tc::mbar_init(&mraw[b], 1);
   }
-  for (int e = tid; e < TC_M * GC_N; e += GP_THREADS) {
-    gS[e] = 0.0;
-    gT[e] = 0;
-    gE[e] = -1000000;
-  }
+  // operand rows past the block's columns (V columns mi .. TC_M - 1, W
+  // columns nj .. GC_N - 1) are never converted: they stay zero
+  for (int e = tid; e < GP_NS * GC_SB / 16; e += GP_THREADS)
+    reinterpret_cast<uint4*>(base)[e] = make_uint4(0u, 0u, 0u, 0u);
+  gcge::tc::fence_proxy_async();
   gcge::tc::fence_before();
   __syncthreads();
   gcge::tc::fence_after();
   const uint32_t tmem = *tslot;
   bool ok = true;
 
-  // chunk cc of this CTA's run into raw buffer cc % nraw (thread 0)
-  auto issue_raw = [&](int cc) {
-    const int chunk = cfirst + cc;
-    uint64_t* mb = &mraw[cc % nraw];
-    uint8_t* dst = rawbase + (cc % nraw) * RC;
-    gcge::tc::mbar_arrive_expect_tx(mb, (uint32_t)RC);
-    gcge::tc::bulk_g2s(dst, vpl + ((size_t)chunk * ldv + voff + i0) * PL_REC, (uint32_t)VB, mb);
-    gcge::tc::bulk_g2s(dst + VB, wpl + ((size_t)chunk * ldw + woff + j0) * PL_REC,
-                       (uint32_t)(nj * PL_REC), mb);
-  };
+  // fold threads: outputs (i, 8 jh + u), u < 8, in registers
+  const int fw = warp - 1 - GP_CW;
+  const int q4 = warp & 3, jh = fw >> 2;  // lane quadrant, W column half
+  const int fi = 32 * q4 + lane;
+  double rS[8];
+  long long rT[8];
+  int rE[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) {
+    rS[u] = 0.0;
+    rT[u] = 0;
+    rE[u] = -1000000;
+  }
 
-  if (warp < GP_CW) {
-    // ------------------------------------------------ converter warps
-    if (tid == 0)
+  if (warp == 0) {
+    // ------------------------------------------------ copy + MMA thread
+    if (lane == 0) {
+      // chunk cc of this CTA's run into raw buffer cc % nraw
+      auto issue_raw = [&](int cc) {
+        const int chunk = cfirst + cc;
+        uint64_t* mb = &mraw[cc % nraw];
+        uint8_t* dst = rawbase + (cc % nraw) * RC;
+        gcge::tc::mbar_arrive_expect_tx(mb, (uint32_t)RC);
+        gcge::tc::bulk_g2s(dst, vpl + ((size_t)chunk * ldv + voff + i0) * PL_REC, (uint32_t)VB,
+                           mb);
+        gcge::tc::bulk_g2s(dst + VB, wpl + ((size_t)chunk * ldw + woff + j0) * PL_REC,
+                           (uint32_t)(nj * PL_REC), mb);
+      };
       for (int cc = 0; cc < nraw && cc < nch; cc++) issue_raw(cc);
-    const int nwq = 4 * nj, nvq = 4 * mi;
-    for (int c = 0; c < nch; c++) {
-      const int tb = c & 1, rb = c % nraw;
-      const uint8_t* rbuf = rawbase + rb * RC;
-      if (!gcge::tc::mbar_wait_warp(&mraw[rb], (c / nraw) & 1, TC_WAIT)) ok = false;
-      int* ce = cex + (c % 3) * GC_CE;
-      for (int i = tid; i < mi + nj; i += GP_CW * 32) {
-        const int e = *reinterpret_cast<const int*>(rbuf + i * PL_REC);
-        ce[i < mi ? i : TC_M + i - mi] = e;
-      }
-      for (int st = 0; st < GC_ST; st++) {
-        const int g = c * GC_ST + st, buf = g & 1;
-        if (g >= 2 && !gcge::tc::mbar_wait_warp(&mempty[buf], ((g >> 1) - 1) & 1, TC_WAIT))
-          ok = false;
-        uint8_t* As = base + buf * GC_SB;
-        uint8_t* Bs = As + TC_ABYTES;
-        for (int u = tid; u < nwq + nvq; u += GP_CW * 32) {
-          if (u < nwq) {
-            const int col = u >> 2, q = u & 3;
-            pl_quad(rbuf + VB + col * PL_REC, st, q,
-                    Bs + (q >> 1) * (D8_S * GC_N * 16) + (col >> 3) * 128 + (col & 7) * 16 +
-                        (q & 1) * 8,
-                    GC_N * 16);
-          } else {
-            const int vq = u - nwq, col = vq >> 2, q = vq & 3;
-            pl_quad(rbuf + col * PL_REC, st, q,
-                    As + (q >> 1) * (TC_M / 8 * 128) + (col >> 3) * 128 + (col & 7) * 16 +
-                        (q & 1) * 8,
-                    TC_M * TC_KS * 2);
-          }
-        }
-        gcge::tc::fence_proxy_async();
-        gcge::tc::named_sync(1, GP_CW * 32);
-        if (tid == 0) {
+      for (int c = 0; c < nch && ok; c++) {
+        const int tb = c & 1;
+        for (int st = 0; st < GC_ST; st++) {
+          const int g = c * GC_ST + st, buf = g % GP_NS;
+          if (!gcge::tc::mbar_wait(&mfull[buf], (g / GP_NS) & 1, TC_WAIT)) ok = false;
           // the accumulator set of this chunk was folded (chunk c - 2)
-          if (st == 0 && c >= 2 &&
-              !gcge::tc::mbar_wait(&macce[tb], ((c >> 1) - 1) & 1, TC_WAIT))
+          if (st == 0 && c >= 2 && !gcge::tc::mbar_wait(&macce[tb], ((c >> 1) - 1) & 1, TC_WAIT))
             ok = false;
+          if (!ok) break;
           gcge::tc::fence_after();
-          d8_issue<true>(tmem + (uint32_t)(tb * D8_NL * GC_N), gcge::tc::smem_u32(As),
-                         TC_M * TC_KS * 2, gcge::tc::smem_u32(Bs), GC_N, st == 0);
+          uint8_t* As = base + buf * GC_SB;
+          const uint32_t acc = tmem + (uint32_t)(tb * D8_NL * GC_N);
+          if (st == 0)
+            gp_issue<true>(acc, gcge::tc::smem_u32(As), gcge::tc::smem_u32(As + TC_ABYTES));
+          else
+            gp_issue<false>(acc, gcge::tc::smem_u32(As), gcge::tc::smem_u32(As + TC_ABYTES));
           gcge::tc::commit(&mempty[buf]);
           if (st == GC_ST - 1) {
             gcge::tc::commit(&maccf[tb]);
@@ -1048,37 +1082,76 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
             if (c + nraw < nch) issue_raw(c + nraw);
           }
         }
-        __syncwarp();  // warp 0 converges again before its next aligned barrier
       }
+    }
+    __syncwarp();
+  } else if (warp <= GP_CW) {
+    // ------------------------------------------------ converter warps
+    const int ctid = tid - 32;
+    const int nwq = 4 * nj, nvq = 4 * mi;
+    for (int c = 0; c < nch; c++) {
+      const int rb = c % nraw;
+      const uint8_t* rbuf = rawbase + rb * RC;
+      if (!gcge::tc::mbar_wait_warp(&mraw[rb], (c / nraw) & 1, TC_WAIT)) ok = false;
+      if (!ok) break;
+      int* ce = cex + (c % 3) * GC_CE;
+      for (int i = ctid; i < mi + nj; i += GP_CW * 32) {
+        const int e = *reinterpret_cast<const int*>(rbuf + i * PL_REC);
+        ce[i < mi ? i : TC_M + i - mi] = e;
+      }
+      for (int st = 0; st < GC_ST; st++) {
+        const int g = c * GC_ST + st, buf = g % GP_NS;
+        // the buffer's previous use (stage g - GP_NS) has finished its MMAs
+        if (g >= GP_NS &&
+            !gcge::tc::mbar_wait_warp(&mempty[buf], ((g / GP_NS) - 1) & 1, TC_WAIT))
+          ok = false;
+        if (!ok) break;
+        uint8_t* As = base + buf * GC_SB;
+        uint8_t* Bs = As + TC_ABYTES;
+        // operands in the 32-byte swizzled K-major layout: digit planes of
+        // TC_M rows (A: V columns) and GC_N rows (B: W columns)
+        for (int u = ctid; u < nwq + nvq; u += GP_CW * 32) {
+          if (u < nwq) {
+            const int col = u >> 2, q = u & 3;
+            pl_quad(rbuf + VB + col * PL_REC, st, q, Bs + gcge::tc::sw32_off(col, 4 * q),
+                    GC_N * 32);
+          } else {
+            const int vq = u - nwq, col = vq >> 2, q = vq & 3;
+            pl_quad(rbuf + col * PL_REC, st, q, As + gcge::tc::sw32_off(col, 4 * q), TC_M * 32);
+          }
+        }
+        gcge::tc::fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) gcge::tc::mbar_arrive(&mfull[buf]);
+      }
+      if (!ok) break;
     }
   } else {
     // ------------------------------------------------ fold warps
-    const int fw = warp - GP_CW;
-    const int q4 = warp & 3, jh = fw >> 2;  // lane quadrant, W column half
-    const int i = 32 * q4 + lane;
     for (int c = 0; c < nch; c++) {
       const int tb = c & 1;
       if (!gcge::tc::mbar_wait_warp(&maccf[tb], (c >> 1) & 1, TC_WAIT)) ok = false;
+      if (!ok) break;
       gcge::tc::fence_after();
       if (32 * q4 < mi && 8 * jh < nj) {
         const int* ce = cex + (c % 3) * GC_CE;
-        const int ea = ce[i];
+        const int ea = ce[fi];
         const uint32_t tacc = tmem + (uint32_t)(tb * D8_NL * GC_N) + ((uint32_t)(32 * q4) << 16);
 #pragma unroll
-        for (int c0 = 8 * jh; c0 < 8 * jh + 8; c0 += 4) {
-          uint32_t acc[D8_NL][4];
+        for (int h = 0; h < 4; h++) {
+          const int c0 = 8 * jh + 2 * h;
+          uint32_t acc[D8_NL][2];
 #pragma unroll
           for (int l = 0; l < D8_NL; l++)
-            gcge::tc::tmem_ld4(tacc + (uint32_t)(l * GC_N + c0), acc[l]);
+            gcge::tc::tmem_ld2(tacc + (uint32_t)(l * GC_N + c0), acc[l]);
           gcge::tc::tmem_wait_ld();
 #pragma unroll
-          for (int jj = 0; jj < 4; jj++) {
-            const int j = c0 + jj;
-            if (i >= mi || j >= nj) continue;
+          for (int jj = 0; jj < 2; jj++) {
+            const int j = c0 + jj, u = 2 * h + jj;
+            if (fi >= mi || j >= nj) continue;
             const int eb = ce[TC_M + j];
-            const int o = j * TC_M + i;
             if (ea >= 4096 || eb >= 4096) {
-              gS[o] = __longlong_as_double(0x7ff8000000000000ll);
+              rS[u] = __longlong_as_double(0x7ff8000000000000ll);
             } else if (ea > -2000 && eb > -2000) {
               int lv[D8_NL];
 #pragma unroll
@@ -1089,13 +1162,13 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
                                   (long long)((p2 + 32) >> 6) +
                                   (long long)((p3 + (1 << 21)) >> 22);
               const int E = ea + eb;
-              const long long t = gT[o], r = t + T;
-              if (gE[o] != E || ((t ^ r) & (T ^ r)) < 0) {
-                gc_flush(gT + o, gE + o, gS + o);
-                gT[o] = T;
-                gE[o] = E;
+              const long long t = rT[u], r = t + T;
+              if (rE[u] != E || ((t ^ r) & (T ^ r)) < 0) {
+                gp_flush(rT[u], rE[u], rS[u]);
+                rT[u] = T;
+                rE[u] = E;
               } else {
-                gT[o] = r;
+                rT[u] = r;
               }
             }
           }
@@ -1108,13 +1181,17 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
   }
   const int anybad = __syncthreads_or(ok ? 0 : 1);
   if (anybad && tid == 0) atomicExch(&g_oz_tc_status, 1);
-  double* out = partial + (size_t)blockIdx.x * k1 * k2;
-  for (int e = tid; e < mi * nj; e += GP_THREADS) {
-    const int ii = e % mi, jj = e / mi;
-    const int o = jj * TC_M + ii;
-    gc_flush(gT + o, gE + o, gS + o);
-    out[(i0 + ii) + (size_t)(j0 + jj) * k1] =
-        anybad ? __longlong_as_double(0x7ff8000000000000ll) : gS[o];
+  if (warp > GP_CW && fi < mi) {
+    double* out = partial + (size_t)blockIdx.x * k1 * k2;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int j = 8 * jh + u;
+      if (j < nj) {
+        gp_flush(rT[u], rE[u], rS[u]);
+        out[(i0 + fi) + (size_t)(j0 + j) * k1] =
+            anybad ? __longlong_as_double(0x7ff8000000000000ll) : rS[u];
+      }
+    }
   }
   gcge::tc::fence_before();
   __syncthreads();

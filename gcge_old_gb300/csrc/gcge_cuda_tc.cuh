@@ -32,6 +32,27 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
+// Shared-memory matrix descriptor of a K-major tile in the 32-byte swizzled
+// layout (one K slab of 16 bf16 / f16 per row: 8-row x 32-byte atoms, the
+// 16-byte halves of rows 4..7 of an atom exchanged, atoms `sbo` bytes apart;
+// the tile starts on a 256-byte boundary): layout type 6 in bits 61-63.
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;  // leading byte offset: unused by a one-atom-wide K extent
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)6 << 61;
+  return d;
+}
+
+// Byte offset of the 8-byte group (row, k0 .. k0 + 3), k0 a multiple of 4, in
+// that layout (rows of 32 bytes; bit 4 of the address flipped by bit 7).
+__device__ __forceinline__ uint32_t sw32_off(int row, int k0) {
+  return (uint32_t)((row >> 3) * 256 + (row & 7) * 32 + ((((k0 >> 3) ^ (row >> 2)) & 1) << 4) +
+                    (k0 & 7) * 2);
+}
+
 // Instruction descriptor of kind::f16: D FP32, A and B bf16, both K-major.
 __host__ __device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
@@ -78,8 +99,9 @@ __device__ __forceinline__ uint32_t mbar_wait(uint64_t* mbar, uint32_t parity, i
   return done;
 }
 
-// Warp-wide wait: lane 0 polls (sleeping between polls, at most `limit`
-// polls), the warp then continues together.  Returns 0 when it gave up.
+// Warp-wide wait: lane 0 polls (at most `limit` polls; try_wait itself
+// suspends the thread for a while when the phase is not complete), the warp
+// then continues together.  Returns 0 when it gave up.
 __device__ __forceinline__ uint32_t mbar_wait_warp(uint64_t* mbar, uint32_t parity, int limit) {
   uint32_t done = 0;
   if ((threadIdx.x & 31) == 0) {
@@ -90,7 +112,6 @@ __device__ __forceinline__ uint32_t mbar_wait_warp(uint64_t* mbar, uint32_t pari
           : "=r"(done)
           : "r"(smem_u32(mbar)), "r"(parity)
           : "memory");
-      if (!done) __nanosleep(64);
     }
   }
   done = __shfl_sync(0xffffffffu, done, 0);
@@ -160,6 +181,12 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
                : "r"(taddr));
 }
 // warp-wide: 4 consecutive FP32 columns (valid after tmem_wait_ld())
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t* r) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
