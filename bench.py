@@ -529,6 +529,19 @@ def run_config3(args):
                                         if k.startswith("t_")}}
         evs["mixed_amg"] = ev
         del vec
+        if args.c3pase:
+            # the multilevel eigensolver on the same hierarchy (GCGE_CUDA_PASE_Solve)
+            out_t = torch.empty((nev, A.n), dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            t0 = time.time()
+            ev, _, pst = S.pase_solve(dA, dB, nev, amg=amg, evec_device=out_t, tol=1e-10)
+            torch.cuda.synchronize()
+            t_p = time.time() - t0
+            r = true_residuals_gpu(torch, A, B, ev, out_t)
+            res["pase"] = {"s": t_p, "cycles": pst["cycles"], "max_residual": float(r.max()),
+                           "phase_s": {k: round(v, 3) for k, v in pst.items() if k.startswith("t_")}}
+            evs["pase"] = ev
+            del out_t
         amg.close()
         torch.cuda.empty_cache()
     ev_m, ev_d = evs["mixed"], evs["fp64"]
@@ -546,9 +559,10 @@ def run_config3(args):
         ref = np.array(json.load(open(CFG3_PORT_FILE))["eval"])
         out["per_pair_eigenvalue_rel_diff_vs_oracle_port"] = {
             p: float(np.max(np.abs(evs[p] - ref) / np.abs(ref))) for p in evs}
-    if "mixed_amg" in evs:
-        out["per_pair_eigenvalue_rel_diff_mixed_amg_vs_fp64"] = float(
-            np.max(np.abs(evs["mixed_amg"] - ev_d) / np.abs(ev_d)))
+    for key in ("mixed_amg", "pase"):
+        if key in evs:
+            out["per_pair_eigenvalue_rel_diff_%s_vs_fp64" % key] = float(
+                np.max(np.abs(evs[key] - ev_d) / np.abs(ev_d)))
     if args.c3save:
         np.savez(args.c3save, ev_tol=args.c3tol, **evs)
     print(json.dumps(out))
@@ -777,6 +791,8 @@ def main():
     ap.add_argument("--c3tol", type=float, default=1e-11, help="ev_tol of --config 3")
     ap.add_argument("--c3amg", action="store_true", help="--config 3: also solve with the AMG-PCG "
                                                          "W step")
+    ap.add_argument("--c3pase", action="store_true", help="--config 3 (with --c3amg): also solve "
+                                                          "with the multilevel eigensolver")
     ap.add_argument("--c3save", default="", help="--config 3: write both precisions' eigenvalues "
                                                 "to this .npz")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
@@ -845,6 +861,15 @@ def main():
                                                  mls=amg)
     res_amg = true_residuals_gpu(torch, A, B, ev_amg, vec_amg)
     del vec_amg
+    # the multilevel eigensolver (GCGE_CUDA_PASE_Solve) on the same hierarchy
+    out_p = torch.empty((nev, A.n), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.time()
+    ev_pase, _, pst = S.pase_solve(dA, dB, nev, amg=amg, evec_device=out_p, tol=1e-10)
+    torch.cuda.synchronize()
+    t_pase = time.time() - t0
+    res_pase = true_residuals_gpu(torch, A, B, ev_pase, out_p)
+    del out_p
     amg.close()
     # each form with the block size and inner block-CG step cap that suit it
     # (found by a sweep; the reference's defaults are 10 and 20): more inner
@@ -912,6 +937,10 @@ def main():
                           "eigenvalue_rel_diff_vs_fp64": float(np.max(np.abs(ev_amg - ev_fp64)
                                                                       / np.abs(ev_fp64))),
                           "speedup_vs_mixed": v_mixed / statistics.mean(t_amg)},
+        "pase": {"s": t_pase, "cycles": pst["cycles"], "max_residual": float(res_pase.max()),
+                 "eigenvalue_rel_diff_vs_fp64": float(np.max(np.abs(ev_pase - ev_fp64)
+                                                             / np.abs(ev_fp64))),
+                 "phase_s": {k: round(v, 3) for k, v in pst.items() if k.startswith("t_")}},
         "tuned_inner_solve": dict(tuned, mixed_speedup_vs_fp64=tuned["fp64"]["s"] / tuned["mixed"]["s"]),
         "gcg_iterations": {"mixed": st_mixed[-1]["num_iter"], "fp64": st_fp64[-1]["num_iter"],
                            "fp64_correction_form": st_fcor[0]["num_iter"]},

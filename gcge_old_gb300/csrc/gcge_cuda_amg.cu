@@ -53,6 +53,7 @@
 #include <vector>
 
 #include "../../include/gcge_cuda.h"
+#include "gcge_cuda_amg.cuh"
 #include "gcge_cuda_bcg.cuh"
 #include "gcge_cuda_common.cuh"
 
@@ -1811,3 +1812,85 @@ extern "C" int GCGE_CUDA_AMG_GetLastSteps(const GCGE_CUDA_AMG* amg, int* steps) 
   *steps = amg->last_steps;
   return GCGE_CUDA_OK;
 }
+
+// ------------------------------------------------------------------ internal views
+namespace gcge {
+namespace amg {
+
+namespace {
+View view_of(const Mat& m) {
+  View v;
+  v.rows = m.rows;
+  v.cols = m.cols;
+  v.nnz = m.nnz;
+  v.rp = m.rp;
+  v.ci = m.ci;
+  v.v = m.v;
+  return v;
+}
+Mat mat_of(const View& v) {
+  Mat m;
+  m.rows = v.rows;
+  m.cols = v.cols;
+  m.nnz = v.nnz;
+  m.rp = v.rp;
+  m.ci = v.ci;
+  m.v = v.v;
+  return m;
+}
+
+__global__ void k_identity(int n, int* rp, int* ci, double* v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    ci[i] = i;
+    v[i] = 1.0;
+  }
+  if (i <= n) rp[i] = i;
+}
+}  // namespace
+
+int levels(const GCGE_CUDA_AMG* a) { return a ? a->nlev : 0; }
+View op(const GCGE_CUDA_AMG* a, int l) { return view_of(a->lev[l].A); }
+View prolong(const GCGE_CUDA_AMG* a, int l) { return view_of(a->lev[l].P); }
+View restrict_to(const GCGE_CUDA_AMG* a, int l) { return view_of(a->lev[l].R); }
+
+int galerkin(const View& R, const View& M, const View& P, View* C, cudaStream_t st) {
+  Mat c;
+  const int rc = ::galerkin(mat_of(R), mat_of(M), mat_of(P), c, st);
+  if (rc != GCGE_CUDA_OK) {
+    c.release();
+    return rc;
+  }
+  *C = view_of(c);
+  return GCGE_CUDA_OK;
+}
+
+int identity(int n, View* I, cudaStream_t st) {
+  View v;
+  v.rows = v.cols = v.nnz = n;
+  AMG_CHK(dalloc(&v.rp, (size_t)n + 1));
+  AMG_CHK(dalloc(&v.ci, (size_t)n));
+  AMG_CHK(dalloc(&v.v, (size_t)n));
+  k_identity<<<(n + 256) / 256, 256, 0, st>>>(n, v.rp, v.ci, v.v);
+  AMG_CU(cudaGetLastError());
+  *I = v;
+  return GCGE_CUDA_OK;
+}
+
+void free_view(View& v) {
+  cudaFree(v.rp);
+  cudaFree(v.ci);
+  cudaFree(v.v);
+  v = View();
+}
+
+void set_pcg(GCGE_CUDA_AMG* a, int max_it, double rate, int* old_max_it, double* old_rate) {
+  std::lock_guard<std::mutex> lk(g_amg_mu);
+  if (old_max_it) *old_max_it = a->prm.pcg_max_it;
+  if (old_rate) *old_rate = a->prm.pcg_rate;
+  a->prm.pcg_max_it = max_it;
+  a->prm.pcg_rate = rate;
+}
+
+}  // namespace amg
+}  // namespace gcge

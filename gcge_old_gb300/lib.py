@@ -45,6 +45,22 @@ class AMGParam(C.Structure):
                 ("pcg_max_it", C.c_int), ("pcg_rate", C.c_double)]
 
 
+class PASEParam(C.Structure):
+    """GCGE_CUDA_PASE_PARAM of the multilevel eigensolver."""
+    _fields_ = [("more_nev", C.c_int), ("aux_level", C.c_int), ("max_cycles", C.c_int),
+                ("smooth_steps", C.c_int), ("aux_max_it", C.c_int), ("initial_max_it", C.c_int),
+                ("tol", C.c_double), ("initial_tol", C.c_double), ("aux_tol", C.c_double)]
+
+
+class PASEStats(C.Structure):
+    """GCGE_CUDA_PASE_STATS: cycle and iteration counts, final residual, phase times (s)."""
+    _fields_ = [("cycles", C.c_int), ("initial_gcg_iterations", C.c_int),
+                ("aux_gcg_iterations", C.c_int), ("smoothing_steps", C.c_int),
+                ("max_residual", C.c_double), ("seconds", C.c_double),
+                ("t_initial", C.c_double), ("t_smooth", C.c_double), ("t_aux_build", C.c_double),
+                ("t_aux_solve", C.c_double), ("t_prolong", C.c_double), ("t_check", C.c_double)]
+
+
 # GCGE_CUDA_MULTI_LINEAR_SOLVER(ctx, A, rhs, x, k, n, stream)
 MultiLinearSolver = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                 C.c_void_p)
@@ -119,6 +135,9 @@ SIGNATURES = {
     "GCGE_CUDA_AMGPCG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_pp, C.c_int, C.c_int,
                                    C.c_void_p]),
     "GCGE_CUDA_AMG_GetLastSteps": (C.c_int, [C.c_void_p, c_int_p]),
+    "GCGE_CUDA_PASE_DefaultParam": (None, [C.c_void_p]),
+    "GCGE_CUDA_PASE_Solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                       c_double_p, C.c_void_p, C.c_void_p]),
     "GCGE_CUDA_EigvecAdjointSolve": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_double_p, C.c_int,
                                               c_pp, c_pp, c_double_p, C.c_int, C.c_double,
                                               c_int_p]),

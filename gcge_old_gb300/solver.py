@@ -138,6 +138,44 @@ class AMG:
             pass
 
 
+def pase_solve(A, B, nev: int, amg: "AMG | None" = None, amg_params: dict | None = None,
+               evec_device=None, **params):
+    """The multilevel eigensolver (GCGE_CUDA_PASE_Solve, the GPU form of the
+    reference's PASE_EigenSolver, pase/src/pase_solver.c:17-82) on the AMG
+    hierarchy of A.  A, B: CSRMatrix or DeviceMatrix (B None: identity);
+    params: fields of GCGE_CUDA_PASE_PARAM.  evec_device: optional torch
+    tensor (nev, n) on cuda to receive the eigenvectors (else they are copied
+    to the host).  Returns (eval, evec (nev, n) or the tensor, stats dict)."""
+    lib = L.load()
+    dA = A if isinstance(A, DeviceMatrix) else DeviceMatrix(A)
+    dB = None if B is None else (B if isinstance(B, DeviceMatrix) else DeviceMatrix(B))
+    own = amg is None
+    if own:
+        amg = AMG(dA, **(amg_params or {}))
+    prm = L.PASEParam()
+    lib.GCGE_CUDA_PASE_DefaultParam(C.byref(prm))
+    for k, v in params.items():
+        if k not in dict(L.PASEParam._fields_):
+            raise ValueError("unknown PASE parameter %r" % k)
+        setattr(prm, k, v)
+    ev = np.zeros(nev)
+    st = L.PASEStats()
+    if evec_device is None:
+        import torch
+        out = torch.empty((nev, dA.n), dtype=torch.float64, device="cuda")
+    else:
+        out = evec_device
+    try:
+        L.check(lib.GCGE_CUDA_PASE_Solve(dA.handle, dB.handle if dB else None, amg.handle, nev,
+                                         C.byref(prm), ev.ctypes.data_as(L.c_double_p),
+                                         C.c_void_p(out.data_ptr()), C.byref(st)), "PASE_Solve")
+    finally:
+        if own:
+            amg.close()
+    stats = {f: getattr(st, f) for f, _ in L.PASEStats._fields_}
+    return ev, (out if evec_device is not None else out.cpu().numpy()), stats
+
+
 class GCGESolver:
     """GCG eigensolver for A x = lambda B x on one GPU.
 

@@ -225,6 +225,42 @@ int GCGE_CUDA_AMGPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs, doub
                      int k, int n, void* stream);
 /* AMG-PCG steps of the last GCGE_CUDA_AMGPCG call on this hierarchy. */
 int GCGE_CUDA_AMG_GetLastSteps(const GCGE_CUDA_AMG* amg, int* steps);
+
+/* ---------------------------------------------------------------- multilevel eigensolver
+ * The multilevel correction method of the reference's PASE add-on
+ * (PASE_EigenSolver, pase/src/pase_solver.c:17-82; two-grid cycle :596-627)
+ * on one GPU, over the AMG hierarchy of A: B is carried down by Galerkin
+ * products, the GCG solver finds nev + more_nev pairs on the auxiliary level,
+ * and each cycle on the finest level smooths the vectors with AMG-PCG on
+ * A u = lambda B u and solves the auxiliary problem on (coarse space + current
+ * vectors) with the GCG solver.  The auxiliary level is fixed (the reference
+ * also searches it at run time); converged pairs are not locked. */
+typedef struct GCGE_CUDA_PASE_PARAM_ {
+  int more_nev;       /* pairs carried beyond nev (default 10, the reference's more_nev) */
+  int aux_level;      /* AMG level of the auxiliary coarse space, >= 1 (default 1) */
+  int max_cycles;     /* two-grid cycles on the finest level (default 60) */
+  int smooth_steps;   /* AMG-PCG steps per smoothing (default 2) */
+  int aux_max_it;     /* GCG iterations per auxiliary solve (default 3, the reference's
+                         max_direct_count_each_level) */
+  int initial_max_it; /* GCG iterations of the initial solve on the auxiliary level (default 300) */
+  double tol;         /* every wanted pair: ||A u - lambda B u|| / (|lambda| ||u||) < tol (default 1e-10) */
+  double initial_tol; /* ev_tol of the initial solve (default 1e-8, the reference's initial_rtol) */
+  double aux_tol;     /* ev_tol of the auxiliary solves (default 1e-12) */
+} GCGE_CUDA_PASE_PARAM;
+typedef struct GCGE_CUDA_PASE_STATS_ {
+  int cycles, initial_gcg_iterations, aux_gcg_iterations, smoothing_steps;
+  double max_residual, seconds;
+  double t_initial, t_smooth, t_aux_build, t_aux_solve, t_prolong, t_check;
+} GCGE_CUDA_PASE_STATS;
+void GCGE_CUDA_PASE_DefaultParam(GCGE_CUDA_PASE_PARAM* prm);
+/* The nev smallest pairs of A x = lambda B x (B NULL: identity); amg is the
+ * hierarchy of A (its AMG-PCG settings are used for the smoothing and
+ * restored).  eval: host array of nev; evec: DEVICE n x nev column-major
+ * (B-orthonormal columns).  GCGE_CUDA_ERR_NUMERIC (with the pairs so far) when
+ * max_cycles end above tol.  stats may be NULL. */
+int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT* B, GCGE_CUDA_AMG* amg,
+                         int nev, const GCGE_CUDA_PASE_PARAM* prm, double* eval, double* evec,
+                         GCGE_CUDA_PASE_STATS* stats);
 /* The CUDA stream (cudaStream_t) the solver runs on, for event timing. */
 int GCGE_CUDA_SOLVER_GetStream(GCGE_CUDA_SOLVER* solver, void** stream);
 int GCGE_CUDA_SOLVER_SetFromCommandLine(GCGE_CUDA_SOLVER* solver, int argc, char** argv);

@@ -109,6 +109,10 @@ def test_new_entry_points_check_arguments_without_gpu():
     lib.GCGE_CUDA_AMG_DefaultParam(C.byref(prm))
     assert (prm.max_levels, prm.coarse_size, prm.smooth_p, prm.cheb_degree) == (10, 256, 1, 2)
     assert (prm.pcg_max_it, prm.pcg_rate) == (20, 1e-2)
+    pp = L.PASEParam()
+    lib.GCGE_CUDA_PASE_DefaultParam(C.byref(pp))
+    assert (pp.more_nev, pp.aux_level, pp.smooth_steps, pp.aux_max_it, pp.tol) == (10, 1, 2, 3, 1e-10)
+    assert lib.GCGE_CUDA_PASE_Solve(None, None, None, 4, None, None, None, None) == 1
     ev = np.array([1.0, 2.0])
     assert lib.GCGE_CUDA_EigvecAdjointSolve(None, None, None, ev.ctypes.data_as(L.c_double_p), 2,
                                             None, None, None, 10, 1e-8, None) == 1
