@@ -416,25 +416,22 @@ __global__ void k_transpose_fill(int rows, const int* __restrict__ rp, const int
   }
 }
 
-// sorts each row of up to kSortMax entries by column (insertion sort, one
-// thread per row): the keys of a row are distinct, so the order is canonical
-__global__ void k_sort_rows(int rows, const int* __restrict__ rp, int* __restrict__ ci,
-                            double* __restrict__ v) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rows) return;
-  const int b = rp[i], e = rp[i + 1];
-  if (e - b > kSortMax) return;
-  for (int q = b + 1; q < e; q++) {
-    const int key = ci[q];
-    const double val = v[q];
-    int t = q - 1;
-    while (t >= b && ci[t] > key) {
-      ci[t + 1] = ci[t];
-      v[t + 1] = v[t];
-      t--;
-    }
-    ci[t + 1] = key;
-    v[t + 1] = val;
+// rows sorted by column into (ci2, v2), one warp per row: an entry's place is
+// the number of smaller columns in its row (the columns of a row are
+// distinct, so the order is canonical and the result deterministic)
+__global__ void k_rank_rows(int rows, const int* __restrict__ rp, const int* __restrict__ ci,
+                            const double* __restrict__ v, int* __restrict__ ci2,
+                            double* __restrict__ v2) {
+  const int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= rows) return;
+  const int b = rp[w], e = rp[w + 1];
+  for (int p = b + lane; p < e; p += 32) {
+    const int key = ci[p];
+    int rk = 0;
+    for (int t = b; t < e; t++) rk += ci[t] < key;
+    ci2[b + rk] = key;
+    v2[b + rk] = v[p];
   }
 }
 
@@ -784,6 +781,43 @@ __global__ void __launch_bounds__(kT) k_spmv(int n, const int* __restrict__ rp,
   st_row<KW>(y, r, t);
 }
 
+// y = M x for matrices with long rows (the restriction): one warp per row,
+// lanes over the row's entries, then a shuffle reduction per column
+template <int KW>
+__global__ void __launch_bounds__(kT) k_spmv_warp(int n, const int* __restrict__ rp,
+                                                  const int* __restrict__ ci,
+                                                  const float* __restrict__ mv,
+                                                  const float* __restrict__ x,
+                                                  float* __restrict__ y) {
+  const int r = (int)(((long long)blockIdx.x * kT + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  float acc[KW];
+#pragma unroll
+  for (int c = 0; c < KW; c++) acc[c] = 0.f;
+  const int e1 = rp[r + 1];
+  for (int e = rp[r] + lane; e < e1; e += 32) {
+    const float a = mv[e];
+    const float4* xr = reinterpret_cast<const float4*>(x + (size_t)ci[e] * KW);
+#pragma unroll
+    for (int q = 0; q < KW / 4; q++) {
+      const float4 t = __ldg(xr + q);
+      acc[4 * q] = fmaf(a, t.x, acc[4 * q]);
+      acc[4 * q + 1] = fmaf(a, t.y, acc[4 * q + 1]);
+      acc[4 * q + 2] = fmaf(a, t.z, acc[4 * q + 2]);
+      acc[4 * q + 3] = fmaf(a, t.w, acc[4 * q + 3]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < KW; c++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  }
+  if (lane < KW / 4)
+    reinterpret_cast<float4*>(y + (size_t)r * KW)[lane] =
+        make_float4(acc[4 * lane], acc[4 * lane + 1], acc[4 * lane + 2], acc[4 * lane + 3]);
+}
+
 template <int KW>
 __global__ void k_axpy_rows(int n, float* __restrict__ x, const float* __restrict__ d) {
   const int r = blockIdx.x * kT + threadIdx.x;
@@ -796,23 +830,32 @@ __global__ void k_axpy_rows(int n, float* __restrict__ x, const float* __restric
   st_row<KW>(x, r, a);
 }
 
-// x = C b with the dense coarsest inverse C (nc x nc, row-major)
+// x = C b with the dense coarsest inverse C (nc x nc, row-major): a warp per
+// row, lanes over the row, a shuffle reduction per column
 template <int KW>
 __global__ void k_dense_apply(int nc, const float* __restrict__ C, const float* __restrict__ b,
                               float* __restrict__ x) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (r >= nc) return;
   float acc[KW];
 #pragma unroll
   for (int c = 0; c < KW; c++) acc[c] = 0.f;
-  for (int j = 0; j < nc; j++) {
+  for (int j = lane; j < nc; j += 32) {
     const float a = C[(size_t)r * nc + j];
     float bb[KW];
     ld_row<KW>(b, j, bb);
 #pragma unroll
     for (int c = 0; c < KW; c++) acc[c] = fmaf(a, bb[c], acc[c]);
   }
-  st_row<KW>(x, r, acc);
+#pragma unroll
+  for (int c = 0; c < KW; c++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  }
+  if (lane < KW / 4)
+    reinterpret_cast<float4*>(x + (size_t)r * KW)[lane] =
+        make_float4(acc[4 * lane], acc[4 * lane + 1], acc[4 * lane + 2], acc[4 * lane + 3]);
 }
 
 // ------------------------------------------------------------------ PCG kernels (rows)
@@ -1059,11 +1102,17 @@ int transpose(const Mat& M, Mat& T, cudaStream_t st) {
   int* cur = nullptr;
   AMG_CHK(dalloc(&cur, (size_t)T.rows));
   AMG_CU(cudaMemsetAsync(cur, 0, sizeof(int) * T.rows, st));
-  k_transpose_fill<<<grid_of(M.rows), kT, 0, st>>>(M.rows, M.rp, M.ci, M.v, T.rp, cur, T.ci, T.v);
-  k_sort_rows<<<grid_of(T.rows), kT, 0, st>>>(T.rows, T.rp, T.ci, T.v);
+  int* ci_u = nullptr;
+  double* v_u = nullptr;
+  AMG_CHK(dalloc(&ci_u, (size_t)M.nnz));
+  AMG_CHK(dalloc(&v_u, (size_t)M.nnz));
+  k_transpose_fill<<<grid_of(M.rows), kT, 0, st>>>(M.rows, M.rp, M.ci, M.v, T.rp, cur, ci_u, v_u);
+  k_rank_rows<<<grid_of((long long)T.rows * 32), kT, 0, st>>>(T.rows, T.rp, ci_u, v_u, T.ci, T.v);
   AMG_CU(cudaGetLastError());
   AMG_CU(cudaStreamSynchronize(st));
   cudaFree(cur);
+  cudaFree(ci_u);
+  cudaFree(v_u);
   return GCGE_CUDA_OK;
 }
 
@@ -1434,6 +1483,11 @@ void spmv_rows(const Mat& M, const float* x, float* y, int add, cudaStream_t st,
     gcge::spmm_rows_f32(M.rp, M.ci, M.v32, M.rows, x, y, KW, st, heavy);
     return;
   }
+  if (!add && M.nnz >= 32ll * M.rows) {
+    // long rows (the restriction of a smoothed prolongation): a warp per row
+    k_spmv_warp<KW><<<grid_of((long long)M.rows * 32), kT, 0, st>>>(M.rows, M.rp, M.ci, M.v32, x, y);
+    return;
+  }
   k_spmv<KW><<<grid_of(M.rows), kT, 0, st>>>(M.rows, M.rp, M.ci, M.v32, x, y, add);
 }
 
@@ -1473,7 +1527,8 @@ void vcycle(const GCGE_CUDA_AMG_* amg, int l, const float* b, cudaStream_t st) {
   const int deg = amg->prm.cheb_degree;
   if (l == amg->nlev - 1) {
     if (amg->cinv) {
-      k_dense_apply<KW><<<(L.A.rows + 127) / 128, 128, 0, st>>>(L.A.rows, amg->cinv, b, L.x);
+      k_dense_apply<KW><<<grid_of((long long)L.A.rows * 32), kT, 0, st>>>(L.A.rows, amg->cinv, b,
+                                                                           L.x);
     } else {
       smooth<KW>(amg, L, b, 4 * deg, true, false, st);
     }

@@ -18,6 +18,13 @@ there whether or not it converged):
 
     python profile_solve.py --graph 1000000 --nev 128 --iters 3
     python profile_solve.py --aniso 512 --nev 32 --adjoint 200
+
+--diff27 M solves the 27-point variable-coefficient diffusion problem on an
+M^3 grid instead; --amg gives the W step to AMG-PCG on the AMG hierarchy of A
+(GCGE_CUDA_AMGPCG); --pase runs the multilevel eigensolver for --iters cycles:
+
+    python profile_solve.py --diff27 96 --nev 100 --iters 4 --amg
+    python profile_solve.py --diff27 96 --nev 100 --iters 3 --pase
 """
 import argparse
 
@@ -91,11 +98,16 @@ def main():
     ap.add_argument("--graph", type=int, default=0, help="Chung-Lu graph with this many nodes")
     ap.add_argument("--aniso", type=int, default=0, help="2D anisotropic grid size")
     ap.add_argument("--adjoint", type=int, default=0, help="eigenvector-adjoint CG steps")
+    ap.add_argument("--diff27", type=int, default=0, help="27-point diffusion grid size")
+    ap.add_argument("--amg", action="store_true", help="W step by AMG-PCG")
+    ap.add_argument("--pase", action="store_true", help="the multilevel eigensolver")
     a = ap.parse_args()
     if a.graph:
         A, B, _ = M.chung_lu(a.graph, seed=0)
     elif a.aniso:
         A, B, _, _ = M.aniso2d(a.aniso, seed=0)
+    elif a.diff27:
+        A, B = M.diffusion27(a.diff27, seed=0)
     else:
         A, B = M.laplace3d_mass(a.grid, seed=0)
     if a.adjoint:
@@ -104,10 +116,22 @@ def main():
     if a.spmm:
         spmm_only(A, a.spmm)
         return
+    if a.pase:
+        from gcge_old_gb300 import lib as L
+        try:
+            ev, vec, st = S.pase_solve(A, B, a.nev, tol=1e-10, max_cycles=a.iters)
+            print(st)
+        except L.GcgeCudaError as e:  # the cycle cap ends the run before convergence
+            print("pase stopped at the cycle cap:", e)
+        return
     x0 = M.initial_block(A.n, a.nev, seed=0)
-    ev, vec, st = S.solve(A, B, a.nev, x0, ev_tol=1e-10, ev_max_it=a.iters, precision=a.precision,
-                          gemm=a.gemm)
-    print(st)
+    s = S.GCGESolver(A, B, a.nev, ev_tol=1e-10, ev_max_it=a.iters, precision=a.precision,
+                     gemm=a.gemm)
+    if a.amg:
+        s.use_amg_pcg()
+    s.solve(x0)
+    print(s.stats())
+    s.close()
 
 
 if __name__ == "__main__":
