@@ -70,6 +70,11 @@ constexpr int kHashFill = kHashCap / 2;
 constexpr int kSortMax = 2048;       // rows sorted by column up to this length
 constexpr int kCheck = 4;            // AMG-PCG steps between host reads
 constexpr int kRedBlocks = 2 * 152;  // row blocks of the PCG reductions
+// resident 256-thread CTAs per SM for the row-gather kernels of width KW that
+// fit the cap without spills (the Chebyshev step and the PCG's A p spill under
+// it and ran slower: no cap there)
+template <int KW>
+constexpr int row_blocks_per_sm() { return KW <= 12 ? 6 : (KW <= 20 ? 4 : 2); }
 
 std::mutex g_amg_mu;
 
@@ -740,7 +745,7 @@ __global__ void __launch_bounds__(kT) k_cheb_step(int n, const int* __restrict__
 
 // r = b - A x; d = c0 D^-1 r (x is not written: it is being gathered)
 template <int KW>
-__global__ void __launch_bounds__(kT) k_resid_cheb0(int n, const int* __restrict__ rp,
+__global__ void __launch_bounds__(kT, row_blocks_per_sm<KW>()) k_resid_cheb0(int n, const int* __restrict__ rp,
                                                     const int* __restrict__ ci,
                                                     const float* __restrict__ av,
                                                     const float* __restrict__ x,
@@ -763,7 +768,7 @@ __global__ void __launch_bounds__(kT) k_resid_cheb0(int n, const int* __restrict
 
 // y = M x (plain) or y += M x (add)
 template <int KW>
-__global__ void __launch_bounds__(kT) k_spmv(int n, const int* __restrict__ rp,
+__global__ void __launch_bounds__(kT, row_blocks_per_sm<KW>()) k_spmv(int n, const int* __restrict__ rp,
                                              const int* __restrict__ ci,
                                              const float* __restrict__ mv,
                                              const float* __restrict__ x, float* __restrict__ y,

@@ -19,6 +19,11 @@ there whether or not it converged):
     python profile_solve.py --graph 1000000 --nev 128 --iters 3
     python profile_solve.py --aniso 512 --nev 32 --adjoint 200
 
+--gram P runs only P Gram passes of the W orthogonalisation (80 x 10 columns
+on grid^3 rows, the planes of the basis cut once):
+
+    python profile_solve.py --grid 96 --gram 3
+
 --diff27 M solves the 27-point variable-coefficient diffusion problem on an
 M^3 grid instead; --amg gives the W step to AMG-PCG on the AMG hierarchy of A
 (GCGE_CUDA_AMGPCG); --pase runs the multilevel eigensolver for --iters cycles:
@@ -61,6 +66,40 @@ def spmm_only(A, k):
     print("spmm n=%d nnz=%d k=%d done" % (A.n, A.nnz, k))
 
 
+def gram_passes(n, passes, k1=80, k2=10):
+    """The W-orthogonalisation's Gram pass at the solve's shape: the basis
+    planes cut once (80 columns), then `passes` times the cut of W's planes
+    (10 columns, a diagonal folded in) and the plane Gram [X,P]^T diag(b) W."""
+    import ctypes as C
+
+    import torch
+
+    from gcge_old_gb300 import lib as L
+    lib = L.load()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    V = [torch.randn(n, dtype=torch.float64, device="cuda", generator=g) for _ in range(k1)]
+    W = [torch.randn(n, dtype=torch.float64, device="cuda", generator=g) for _ in range(k2)]
+    d = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) + 0.5
+    vp = (C.c_void_p * k1)(*[C.c_void_p(t.data_ptr()) for t in V])
+    wp = (C.c_void_p * k2)(*[C.c_void_p(t.data_ptr()) for t in W])
+    vpl = torch.empty(int(lib.GCGE_CUDA_PlanesBytes(n, k1)), dtype=torch.uint8, device="cuda")
+    wpl = torch.empty(int(lib.GCGE_CUDA_PlanesBytes(n, k2)), dtype=torch.uint8, device="cuda")
+    part = torch.empty(int(lib.GCGE_CUDA_PlanesGramScratchDoubles(k1, k2)), dtype=torch.float64,
+                       device="cuda")
+    G = torch.empty(k2, k1, dtype=torch.float64, device="cuda")
+    L.check(lib.GCGE_CUDA_PlanesCut(vp, k1, n, None, C.c_void_p(vpl.data_ptr()), k1, 0, None),
+            "PlanesCut V")
+    for _ in range(passes):
+        L.check(lib.GCGE_CUDA_PlanesCut(wp, k2, n, C.c_void_p(d.data_ptr()),
+                                        C.c_void_p(wpl.data_ptr()), k2, 0, None), "PlanesCut W")
+        L.check(lib.GCGE_CUDA_PlanesGram(C.c_void_p(vpl.data_ptr()), k1, 0, k1,
+                                         C.c_void_p(wpl.data_ptr()), k2, 0, k2, n,
+                                         C.c_void_p(G.data_ptr()), k1, C.c_void_p(part.data_ptr()),
+                                         None), "PlanesGram")
+    torch.cuda.synchronize()
+    print("gram passes n=%d k1=%d k2=%d passes=%d done" % (n, k1, k2, passes))
+
+
 def adjoint_steps(A, B, nev, steps):
     import ctypes as C
 
@@ -101,7 +140,12 @@ def main():
     ap.add_argument("--diff27", type=int, default=0, help="27-point diffusion grid size")
     ap.add_argument("--amg", action="store_true", help="W step by AMG-PCG")
     ap.add_argument("--pase", action="store_true", help="the multilevel eigensolver")
+    ap.add_argument("--gram", type=int, default=0,
+                    help="only W-orthogonalisation Gram passes (80 x 10) at grid^3 rows")
     a = ap.parse_args()
+    if a.gram:
+        gram_passes(a.grid ** 3, a.gram)
+        return
     if a.graph:
         A, B, _ = M.chung_lu(a.graph, seed=0)
     elif a.aniso:
