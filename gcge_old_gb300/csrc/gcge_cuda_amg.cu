@@ -423,7 +423,8 @@ __global__ void k_transpose_fill(int rows, const int* __restrict__ rp, const int
 
 // rows sorted by column into (ci2, v2), one warp per row: an entry's place is
 // the number of smaller columns in its row (the columns of a row are
-// distinct, so the order is canonical and the result deterministic)
+// distinct, so the order is canonical and the result deterministic); rows of
+// more than kSortMax entries are copied as they are
 __global__ void k_rank_rows(int rows, const int* __restrict__ rp, const int* __restrict__ ci,
                             const double* __restrict__ v, int* __restrict__ ci2,
                             double* __restrict__ v2) {
@@ -431,6 +432,15 @@ __global__ void k_rank_rows(int rows, const int* __restrict__ rp, const int* __r
   const int lane = threadIdx.x & 31;
   if (w >= rows) return;
   const int b = rp[w], e = rp[w + 1];
+  if (e - b > kSortMax) {
+    // a very long row (a hub of a power-law graph): kept in fill order, since
+    // ranking by counting is quadratic in the row length
+    for (int p = b + lane; p < e; p += 32) {
+      ci2[p] = ci[p];
+      v2[p] = v[p];
+    }
+    return;
+  }
   for (int p = b + lane; p < e; p += 32) {
     const int key = ci[p];
     int rk = 0;
@@ -1121,8 +1131,13 @@ int transpose(const Mat& M, Mat& T, cudaStream_t st) {
   return GCGE_CUDA_OK;
 }
 
-// A_c = R A P
-int galerkin(const Mat& R, const Mat& A, const Mat& P, Mat& C, cudaStream_t st) {
+// A_c = R A P.  With dense_out != null the product is abandoned (and
+// *dense_out set) when more than max(64, nc / 16) coarse rows have more
+// distinct columns than the shared table holds: the coarse operator would fill
+// in (hub rows of power-law graphs make every aggregate a neighbour of every
+// other).
+int galerkin(const Mat& R, const Mat& A, const Mat& P, Mat& C, cudaStream_t st,
+             bool* dense_out = nullptr) {
   const int nc = R.rows;
   C.rows = C.cols = nc;
   int* cnt = nullptr;
@@ -1144,6 +1159,14 @@ int galerkin(const Mat& R, const Mat& A, const Mat& P, Mat& C, cudaStream_t st) 
   std::vector<int> over;
   for (int i = 0; i < nc; i++)
     if (hcnt[i] < 0) over.push_back(i);
+  if (dense_out) {
+    *dense_out = (long long)over.size() > std::max(64, nc / 16);
+    if (*dense_out) {
+      cudaFree(cnt);
+      cudaFree(bound);
+      return GCGE_CUDA_OK;
+    }
+  }
   auto gcap_of = [&](int row) {
     long long m = std::min<long long>((long long)nc, std::max<long long>(1, hbound[row]));
     long long c = 1;
@@ -1739,7 +1762,17 @@ extern "C" int GCGE_CUDA_AMG_Create(GCGE_CUDA_AMG** out, const GCGE_CUDA_MAT* A,
     if (rc != GCGE_CUDA_OK) return fail(rc);
     Level& C = amg->lev[l + 1];
     C.own_A = true;
-    rc = galerkin(L.R, L.A, L.P, C.A, st);
+    bool dense = false;
+    rc = galerkin(L.R, L.A, L.P, C.A, st, &dense);
+    if (rc == GCGE_CUDA_OK && dense) {
+      // the coarse operator would fill in: level l stays the coarsest
+      L.P.release();
+      L.R.release();
+      cudaFree(L.agg);
+      L.agg = nullptr;
+      C = Level();
+      break;
+    }
     amg->nlev = l + 2;
     if (rc != GCGE_CUDA_OK) return fail(rc);
   }

@@ -220,3 +220,34 @@ def test_amg_w_step_matches_builtin_in_fewer_iterations(cuda_lib, precision):
     assert r0.max() < 1e-10 and r1.max() < 1e-10, (r0.max(), r1.max())
     np.testing.assert_allclose(ev1, ev0, rtol=1e-10)
     assert st1["num_iter"] < 0.8 * st0["num_iter"], (st1["num_iter"], st0["num_iter"])
+
+
+def test_power_law_graph_stops_before_fill_in(cuda_lib):
+    """On a power-law graph (hubs make every aggregate a neighbour of every other)
+    the Galerkin operator fills in: at 300,000 nodes the first coarse operator
+    would hold 13,863 rows and 169 M entries (a two-minute set-up).  The
+    hierarchy stops coarsening before such a level, and AMG-PCG still reduces
+    the residual."""
+    import time
+    A, B, _ = M_chung_lu(300000)
+    dA = DeviceMatrix(A)
+    t0 = time.time()
+    amg = AMG(dA, pcg_max_it=80, pcg_rate=1e-3)
+    assert time.time() - t0 < 60
+    for l in range(amg.num_levels):
+        info = amg.level_info(l)
+        if info["n"] > 4096:
+            assert info["nnz_a"] <= 0.3 * info["n"] ** 2, (l, info)
+    lib = L.load()
+    b = np.random.default_rng(2).standard_normal((2, A.n))
+    x = _pcg(lib, dA, amg, b, 40, 1e-3)
+    As = A.to_scipy()
+    res = [np.linalg.norm(b[j] - As @ x[j]) / np.linalg.norm(b[j]) for j in range(2)]
+    assert max(res) < 1e-2, res
+    amg.close()
+    dA.close()
+
+
+def M_chung_lu(n):
+    from gcge_old_gb300.matrices import chung_lu
+    return chung_lu(n, seed=4)
