@@ -540,9 +540,10 @@ def run_config3(args):
         t_setup = time.time() - t0
         levels = [amg.level_info(l)["n"] for l in range(amg.num_levels)]
         t, st, ev, vec = time_solves(torch, S, L, dA, dB, nev, x0_dev, "mixed", 0, 1,
-                                     ev_tol=args.c3tol, mls=amg)
+                                     ev_tol=args.c3amgtol, mls=amg)
         r = true_residuals_gpu(torch, A, B, ev, vec)
-        res["mixed_amg"] = {"s": t[0], "amg_setup_s": t_setup, "levels": levels,
+        res["mixed_amg"] = {"s": t[0], "ev_tol": args.c3amgtol, "amg_setup_s": t_setup,
+                            "levels": levels,
                             "gcg_iterations": st[0]["num_iter"], "max_residual": float(r.max()),
                             "phase_s": {k: round(v, 3) for k, v in st[0].items()
                                         if k.startswith("t_")}}
@@ -553,11 +554,13 @@ def run_config3(args):
             out_t = torch.empty((nev, A.n), dtype=torch.float64, device="cuda")
             torch.cuda.synchronize()
             t0 = time.time()
-            ev, _, pst = S.pase_solve(dA, dB, nev, amg=amg, evec_device=out_t, tol=1e-10)
+            ev, _, pst = S.pase_solve(dA, dB, nev, amg=amg, evec_device=out_t, tol=args.c3pasetol,
+                                      max_cycles=120)
             torch.cuda.synchronize()
             t_p = time.time() - t0
             r = true_residuals_gpu(torch, A, B, ev, out_t)
-            res["pase"] = {"s": t_p, "cycles": pst["cycles"], "max_residual": float(r.max()),
+            res["pase"] = {"s": t_p, "tol": args.c3pasetol, "cycles": pst["cycles"],
+                           "max_residual": float(r.max()),
                            "phase_s": {k: round(v, 3) for k, v in pst.items() if k.startswith("t_")}}
             evs["pase"] = ev
             del out_t
@@ -812,6 +815,11 @@ def main():
                                                          "W step")
     ap.add_argument("--c3pase", action="store_true", help="--config 3 (with --c3amg): also solve "
                                                           "with the multilevel eigensolver")
+    ap.add_argument("--c3amgtol", type=float, default=3e-12,
+                    help="ev_tol of --config 3's AMG-PCG solve (other iterates than the "
+                         "reference's: a tighter bound keeps every eigenvalue within 1e-10)")
+    ap.add_argument("--c3pasetol", type=float, default=1e-11,
+                    help="residual tolerance of --config 3's multilevel solve")
     ap.add_argument("--c3save", default="", help="--config 3: write both precisions' eigenvalues "
                                                 "to this .npz")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
