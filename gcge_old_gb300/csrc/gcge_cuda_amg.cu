@@ -1678,7 +1678,7 @@ extern "C" void GCGE_CUDA_AMG_DefaultParam(GCGE_CUDA_AMG_PARAM* p) {
   p->coarse_size = 256;
   p->strength = 0.0;
   p->smooth_p = 1;
-  p->cheb_degree = 2;
+  p->cheb_degree = 3;
   p->cheb_ratio = 30.0;
   p->pcg_max_it = 20;
   p->pcg_rate = 1e-2;

@@ -192,7 +192,7 @@ typedef struct GCGE_CUDA_AMG_PARAM_ {
   int coarse_size;    /* stop coarsening at this many rows or fewer, 1..512 (default 256) */
   double strength;    /* aggregation graph: |a_ij| >= strength sqrt(a_ii a_jj) (default 0) */
   int smooth_p;       /* 1 smoothed prolongation (default), 0 plain aggregation */
-  int cheb_degree;    /* Chebyshev smoother degree, pre and post, 1..16 (default 2) */
+  int cheb_degree;    /* Chebyshev smoother degree, pre and post, 1..16 (default 3) */
   double cheb_ratio;  /* smoother interval [lambda_max / ratio, lambda_max] (default 30) */
   int pcg_max_it;     /* AMG-PCG steps per call (default 20) */
   double pcg_rate;    /* a column stops at ||r|| < pcg_rate ||r_0|| (default 1e-2) */

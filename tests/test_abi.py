@@ -107,7 +107,7 @@ def test_new_entry_points_check_arguments_without_gpu():
     assert lib.GCGE_CUDA_AMG_Apply(None, None, None, 1, None) == 1
     prm = L.AMGParam()
     lib.GCGE_CUDA_AMG_DefaultParam(C.byref(prm))
-    assert (prm.max_levels, prm.coarse_size, prm.smooth_p, prm.cheb_degree) == (10, 256, 1, 2)
+    assert (prm.max_levels, prm.coarse_size, prm.smooth_p, prm.cheb_degree) == (10, 256, 1, 3)
     assert (prm.pcg_max_it, prm.pcg_rate) == (20, 1e-2)
     pp = L.PASEParam()
     lib.GCGE_CUDA_PASE_DefaultParam(C.byref(pp))
