@@ -796,6 +796,115 @@ __global__ void __launch_bounds__(kT, row_blocks_per_sm<KW>()) k_spmv(int n, con
   st_row<KW>(y, r, t);
 }
 
+// warp-per-row forms of the smoothing kernels for levels with long rows (the
+// Galerkin operators of smoothed aggregation: a hundred or more entries a row):
+// the lanes share the row's gathers, a shuffle reduction gives every lane the
+// row's product, and lane q < KW / 4 finishes columns 4q .. 4q + 3
+template <int KW>
+__device__ __forceinline__ void warp_row_product(const int* __restrict__ rp,
+                                                 const int* __restrict__ ci,
+                                                 const float* __restrict__ av,
+                                                 const float* __restrict__ X, int r, int lane,
+                                                 float* t) {
+#pragma unroll
+  for (int c = 0; c < KW; c++) t[c] = 0.f;
+  const int e1 = rp[r + 1];
+  for (int e = rp[r] + lane; e < e1; e += 32) {
+    const float a = av[e];
+    const float4* xr = reinterpret_cast<const float4*>(X + (size_t)ci[e] * KW);
+#pragma unroll
+    for (int q = 0; q < KW / 4; q++) {
+      const float4 u = __ldg(xr + q);
+      t[4 * q] = fmaf(a, u.x, t[4 * q]);
+      t[4 * q + 1] = fmaf(a, u.y, t[4 * q + 1]);
+      t[4 * q + 2] = fmaf(a, u.z, t[4 * q + 2]);
+      t[4 * q + 3] = fmaf(a, u.w, t[4 * q + 3]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < KW; c++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t[c] += __shfl_xor_sync(0xffffffffu, t[c], o);
+  }
+}
+
+// the four product values of lane q's columns
+template <int KW>
+__device__ __forceinline__ float4 lane_quad(const float* t, int q) {
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int p = 0; p < KW / 4; p++)
+    if (p == q) v = make_float4(t[4 * p], t[4 * p + 1], t[4 * p + 2], t[4 * p + 3]);
+  return v;
+}
+
+template <int KW>
+__global__ void __launch_bounds__(kT) k_cheb_step_warp(int n, const int* __restrict__ rp,
+                                                       const int* __restrict__ ci,
+                                                       const float* __restrict__ av,
+                                                       const float* __restrict__ din,
+                                                       const float* rin, float* rout,
+                                                       const float* __restrict__ dinv, float c1,
+                                                       float c2, float* __restrict__ dout,
+                                                       float* __restrict__ x, int add_din) {
+  const int r = (int)(((long long)blockIdx.x * kT + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  float t[KW];
+  warp_row_product<KW>(rp, ci, av, din, r, lane, t);
+  if (lane >= KW / 4) return;
+  const float4 tq = lane_quad<KW>(t, lane);
+  const size_t o = (size_t)r * KW / 4 + lane;
+  float4 rr = reinterpret_cast<const float4*>(rin)[o];
+  rr.x -= tq.x;
+  rr.y -= tq.y;
+  rr.z -= tq.z;
+  rr.w -= tq.w;
+  reinterpret_cast<float4*>(rout)[o] = rr;
+  if (!dout) return;
+  const float4 dd = reinterpret_cast<const float4*>(din)[o];
+  const float s = c2 * dinv[r];
+  const float4 dn = make_float4(c1 * dd.x + s * rr.x, c1 * dd.y + s * rr.y, c1 * dd.z + s * rr.z,
+                                c1 * dd.w + s * rr.w);
+  reinterpret_cast<float4*>(dout)[o] = dn;
+  if (x) {
+    float4 xa = reinterpret_cast<float4*>(x)[o];
+    const float k = add_din ? 1.f : 0.f;
+    xa.x += k * dd.x + dn.x;
+    xa.y += k * dd.y + dn.y;
+    xa.z += k * dd.z + dn.z;
+    xa.w += k * dd.w + dn.w;
+    reinterpret_cast<float4*>(x)[o] = xa;
+  }
+}
+
+template <int KW>
+__global__ void __launch_bounds__(kT) k_resid_cheb0_warp(int n, const int* __restrict__ rp,
+                                                         const int* __restrict__ ci,
+                                                         const float* __restrict__ av,
+                                                         const float* __restrict__ x,
+                                                         const float* __restrict__ b,
+                                                         const float* __restrict__ dinv, float c0,
+                                                         float* __restrict__ rout,
+                                                         float* __restrict__ d) {
+  const int r = (int)(((long long)blockIdx.x * kT + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  float t[KW];
+  warp_row_product<KW>(rp, ci, av, x, r, lane, t);
+  if (lane >= KW / 4) return;
+  const float4 tq = lane_quad<KW>(t, lane);
+  const size_t o = (size_t)r * KW / 4 + lane;
+  float4 bb = reinterpret_cast<const float4*>(b)[o];
+  bb.x -= tq.x;
+  bb.y -= tq.y;
+  bb.z -= tq.z;
+  bb.w -= tq.w;
+  reinterpret_cast<float4*>(rout)[o] = bb;
+  const float s = c0 * dinv[r];
+  reinterpret_cast<float4*>(d)[o] = make_float4(s * bb.x, s * bb.y, s * bb.z, s * bb.w);
+}
+
 // y = M x for matrices with long rows (the restriction): one warp per row,
 // lanes over the row's entries, then a shuffle reduction per column
 template <int KW>
@@ -1527,25 +1636,39 @@ void smooth(const GCGE_CUDA_AMG_* amg, const Level& L, const float* b, int deg, 
   const int n = L.A.rows;
   const Cheb c = cheb_coef(L.lmax, amg->prm.cheb_ratio, deg);
   const int g = grid_of(n);
+  // levels with long rows (coarse Galerkin operators) take a warp per row
+  const bool wide = L.A.nnz >= 32ll * n;
+  const int gw = grid_of((long long)n * 32);
+  auto step = [&](const float* din, const float* rin_, float c1, float c2, float* dout, float* xx,
+                  int add) {
+    if (wide)
+      k_cheb_step_warp<KW><<<gw, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, din, rin_, L.r, L.dinv,
+                                              c1, c2, dout, xx, add);
+    else
+      k_cheb_step<KW><<<g, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, din, rin_, L.r, L.dinv, c1, c2,
+                                        dout, xx, add);
+  };
   float* d[2] = {L.d0, L.d1};
   const float* rin = b;
   if (zero_start) {
     k_cheb0<KW><<<g, kT, 0, st>>>(n, b, L.dinv, c.c0, d[0], L.x);
   } else {
-    k_resid_cheb0<KW><<<g, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, L.x, b, L.dinv, c.c0, L.r, d[0]);
+    if (wide)
+      k_resid_cheb0_warp<KW><<<gw, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, L.x, b, L.dinv, c.c0,
+                                                L.r, d[0]);
+    else
+      k_resid_cheb0<KW><<<g, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, L.x, b, L.dinv, c.c0, L.r,
+                                          d[0]);
     rin = L.r;
   }
   int cur = 0;
   for (int s = 1; s < deg; s++) {
-    k_cheb_step<KW><<<g, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, d[cur], rin, L.r, L.dinv, c.c1[s],
-                                      c.c2[s], d[cur ^ 1], L.x, (!zero_start && s == 1) ? 1 : 0);
+    step(d[cur], rin, c.c1[s], c.c2[s], d[cur ^ 1], L.x, (!zero_start && s == 1) ? 1 : 0);
     rin = L.r;
     cur ^= 1;
   }
   if (!zero_start && deg == 1) k_axpy_rows<KW><<<g, kT, 0, st>>>(n, L.x, d[0]);
-  if (want_resid)
-    k_cheb_step<KW><<<g, kT, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v32, d[cur], rin, L.r, L.dinv, 0.f, 0.f,
-                                      nullptr, nullptr, 0);
+  if (want_resid) step(d[cur], rin, 0.f, 0.f, nullptr, nullptr, 0);
 }
 
 // x_l = M_l^-1 b (b: level 0's input, or L.b on coarser levels)

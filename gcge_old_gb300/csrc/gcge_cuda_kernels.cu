@@ -311,7 +311,11 @@ __global__ void k_reduce_rows(const double* __restrict__ partial, int nblk, int 
 }
 
 // ||A x - lam B x||^2 and ||x||^2 per column (GCGE_CheckConvergence,
-// src/gcge_eigsol.c:689-707).
+// src/gcge_eigsol.c:689-707), RC columns per block: a thread walks its rows of
+// A and B once for the block's columns, so the matrices are read k / RC times
+// instead of k times (each column's sums keep the order they had column by
+// column).
+constexpr int RC = 4;
 __global__ void __launch_bounds__(kThreads) k_residual(int n, const int* __restrict__ arp,
                                                        const int* __restrict__ aci,
                                                        const double* __restrict__ av,
@@ -326,36 +330,71 @@ __global__ void __launch_bounds__(kThreads) k_residual(int n, const int* __restr
                                                        const int* __restrict__ bhidx,
                                                        const double* __restrict__ bhb, int k) {
   __shared__ double sh[32];
-  const int c = blockIdx.y;
-  const double* x = X.p[c];
-  const double l = lam[c];
-  double rs = 0.0, xs = 0.0;
+  const int c0 = blockIdx.y * RC;
+  const int kc = min(RC, k - c0);
+  const double* x[RC];
+  double l[RC], rs[RC], xs[RC];
+#pragma unroll
+  for (int q = 0; q < RC; q++) {
+    x[q] = X.p[c0 + (q < kc ? q : 0)];
+    l[q] = lam[c0 + (q < kc ? q : 0)];
+    rs[q] = 0.0;
+    xs[q] = 0.0;
+  }
   for (int r = blockIdx.x * kThreads + threadIdx.x; r < n; r += gridDim.x * kThreads) {
-    double ax = 0.0;
+    double ax[RC], bx[RC];
+#pragma unroll
+    for (int q = 0; q < RC; q++) ax[q] = 0.0;
     const int ha = ahidx ? __ldg(ahidx + r) : -1;
-    if (ha >= 0)
-      ax = ahb[(size_t)ha * k + c];
-    else
-      for (int j = __ldg(arp + r); j < __ldg(arp + r + 1); j++) ax = fma(__ldg(av + j), x[__ldg(aci + j)], ax);
-    double bx;
+    if (ha >= 0) {
+#pragma unroll
+      for (int q = 0; q < RC; q++)
+        if (q < kc) ax[q] = ahb[(size_t)ha * k + c0 + q];
+    } else {
+      for (int j = __ldg(arp + r); j < __ldg(arp + r + 1); j++) {
+        const double a = __ldg(av + j);
+        const int cj = __ldg(aci + j);
+#pragma unroll
+        for (int q = 0; q < RC; q++)
+          if (q < kc) ax[q] = fma(a, x[q][cj], ax[q]);
+      }
+    }
     const int hb_ = bhidx ? __ldg(bhidx + r) : -1;
     if (hb_ >= 0) {
-      bx = bhb[(size_t)hb_ * k + c];
+#pragma unroll
+      for (int q = 0; q < RC; q++)
+        if (q < kc) bx[q] = bhb[(size_t)hb_ * k + c0 + q];
     } else if (brp) {
-      bx = 0.0;
-      for (int j = __ldg(brp + r); j < __ldg(brp + r + 1); j++) bx = fma(__ldg(bv + j), x[__ldg(bci + j)], bx);
+#pragma unroll
+      for (int q = 0; q < RC; q++) bx[q] = 0.0;
+      for (int j = __ldg(brp + r); j < __ldg(brp + r + 1); j++) {
+        const double b = __ldg(bv + j);
+        const int cj = __ldg(bci + j);
+#pragma unroll
+        for (int q = 0; q < RC; q++)
+          if (q < kc) bx[q] = fma(b, x[q][cj], bx[q]);
+      }
     } else {
-      bx = x[r];
+#pragma unroll
+      for (int q = 0; q < RC; q++) bx[q] = q < kc ? x[q][r] : 0.0;
     }
-    const double rr = ax - l * bx;
-    rs = fma(rr, rr, rs);
-    xs = fma(x[r], x[r], xs);
+#pragma unroll
+    for (int q = 0; q < RC; q++) {
+      if (q < kc) {
+        const double rr = ax[q] - l[q] * bx[q];
+        rs[q] = fma(rr, rr, rs[q]);
+        xs[q] = fma(x[q][r], x[q][r], xs[q]);
+      }
+    }
   }
-  const double s1 = block_sum(rs, sh);
-  const double s2 = block_sum(xs, sh);
-  if (threadIdx.x == 0) {
-    partial[(size_t)(2 * c) * gridDim.x + blockIdx.x] = s1;
-    partial[(size_t)(2 * c + 1) * gridDim.x + blockIdx.x] = s2;
+#pragma unroll
+  for (int q = 0; q < RC; q++) {
+    const double s1 = block_sum(rs[q], sh);
+    const double s2 = block_sum(xs[q], sh);
+    if (threadIdx.x == 0 && q < kc) {
+      partial[(size_t)(2 * (c0 + q)) * gridDim.x + blockIdx.x] = s1;
+      partial[(size_t)(2 * (c0 + q) + 1) * gridDim.x + blockIdx.x] = s2;
+    }
   }
 }
 
@@ -487,7 +526,7 @@ void residual_f64(const GcgeDevCsr& A, const GcgeDevCsr* B, const ColList<double
   heavy_cols_f64(A, X, k, st);
   const bool bh = B && B->nheavy;
   if (bh) heavy_cols_f64(*B, X, k, st);
-  k_residual<<<dim3(nb, k), kThreads, 0, st>>>(n, A.rp, A.ci, A.v, B ? B->rp : nullptr,
+  k_residual<<<dim3(nb, (k + RC - 1) / RC), kThreads, 0, st>>>(n, A.rp, A.ci, A.v, B ? B->rp : nullptr,
                                                 B ? B->ci : nullptr, B ? B->v : nullptr, X, lam,
                                                 partial, A.nheavy ? A.hidx : nullptr, A.hb64,
                                                 bh ? B->hidx : nullptr, bh ? B->hb64 : nullptr, k);
