@@ -282,3 +282,26 @@ def test_amg_w_step_diffusion27_workload_matches_oracle_port(cuda_lib):
     assert rel.max() < 1e-10, rel.max()
     assert O.true_residuals(A, B, ev, vec).max() <= 1e-10
     assert st["num_iter"] < 0.5 * ref["iters"], st["num_iter"]
+
+
+@pytest.mark.parametrize("make,theta", [("diffusion27", 0.0), ("diffusion27", 0.1),
+                                        ("laplace3d_mass", 0.0), ("chung_lu", 0.0)])
+def test_aggregates_match_the_oracle_exactly(cuda_lib, make, theta):
+    """The device's distance-2 MIS aggregation is index work: on every level
+    with a prolongation, its aggregates equal the CPU restatement's
+    (oracle/amg_ref.py) exactly, computed from that level's operator."""
+    from oracle import amg_ref as R
+    from gcge_old_gb300.matrices import chung_lu
+    A = {"diffusion27": lambda: diffusion27(m=20, seed=5)[0],
+         "laplace3d_mass": lambda: laplace3d_mass(24, seed=2)[0],
+         "chung_lu": lambda: chung_lu(5000, seed=6)[0]}[make]()
+    dA = DeviceMatrix(A)
+    amg = AMG(dA, coarse_size=32, strength=theta)
+    Al = A.to_scipy().tocsr()
+    for l in range(amg.num_levels - 1):
+        ref = R.aggregates(Al.indptr, Al.indices, Al.data, theta)
+        got = amg.aggregates(l)
+        assert np.array_equal(got, ref), (l, int(np.sum(got != ref)))
+        Al = amg.level_csr(l + 1, "A")
+    amg.close()
+    dA.close()
