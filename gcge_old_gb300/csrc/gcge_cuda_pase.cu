@@ -409,9 +409,15 @@ extern "C" int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT*
   }
 
   // ---------------------------------------------------------------- cycles
-  int old_it = 0;
-  double old_rate = 0.0;
-  gcge::amg::set_pcg(amg, p.smooth_steps, 1e-12, &old_it, &old_rate);
+  // the smoothing runs AMG-PCG for exactly smooth_steps steps; the hierarchy's
+  // own settings come back however this function returns
+  struct PcgRestore {
+    GCGE_CUDA_AMG* amg;
+    int it = 0;
+    double rate = 0.0;
+    ~PcgRestore() { gcge::amg::set_pcg(amg, it, rate, nullptr, nullptr); }
+  } restore{amg};
+  gcge::amg::set_pcg(amg, p.smooth_steps, 1e-12, &restore.it, &restore.rate);
   int rc = GCGE_CUDA_OK;
   const GcgeDevCsr* Bm = B ? &B->m : nullptr;
   double maxres = 0.0;
@@ -499,7 +505,6 @@ extern "C" int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT*
     S.cycles = cyc + 1;
     if (maxres < p.tol) break;
   }
-  gcge::amg::set_pcg(amg, old_it, old_rate, nullptr, nullptr);
   if (rc) return rc;
   for (int i = 0; i < nev; i++) eval[i] = s.lam[i];
   PASE_CU(cudaMemcpyAsync(evec, s.U, sizeof(double) * n * nev, cudaMemcpyDeviceToDevice, s.st));

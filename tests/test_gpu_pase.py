@@ -65,3 +65,22 @@ def test_pase_rejects_bad_parameters(cuda_lib):
         S.pase_solve(A, B, 4, aux_level=0)
     with pytest.raises(Exception, match="PASE"):
         S.pase_solve(A, B, 4, tol=-1.0)
+
+
+def test_pase_leaves_the_hierarchy_settings(cuda_lib):
+    """The smoothing runs AMG-PCG with its own step count; the hierarchy's
+    settings are back afterwards (an AMG-PCG call then runs its own 7 steps)."""
+    import ctypes as C
+    from gpu_util import dev_cols
+    from gcge_old_gb300 import lib as L
+    A, B = M.laplace3d_mass(24, seed=3)
+    dA = S.DeviceMatrix(A)
+    amg = S.AMG(dA, pcg_max_it=7, pcg_rate=1e-12)
+    S.pase_solve(dA, B, 6, amg=amg, more_nev=4, tol=1e-10)
+    lib = L.load()
+    rs, rp = dev_cols(np.random.default_rng(0).standard_normal((2, A.n)))
+    xs, xp = dev_cols(np.zeros((2, A.n)))
+    assert lib.GCGE_CUDA_AMGPCG(amg.handle, dA.handle, rp, xp, 2, A.n, None) == 0
+    assert amg.last_steps == 7
+    amg.close()
+    dA.close()
