@@ -1975,11 +1975,22 @@ extern "C" int GCGE_CUDA_AMG_Apply(GCGE_CUDA_AMG* amg, double* const* b, double*
 extern "C" int GCGE_CUDA_AMGPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs,
                                 double* const* x, int k, int n, void* stream) {
   GCGE_CUDA_AMG_* amg = static_cast<GCGE_CUDA_AMG_*>(ctx);
-  if (!amg || !A || !rhs || !x || k < 1 || k > 32 || n != A->m.n || amg->lev[0].A.rows != n ||
-      amg->lev[0].A.rp != A->m.rp)
+  if (!amg || !A || !rhs || !x || k < 1 || k > GCGE_MAXCOLS || n != A->m.n ||
+      amg->lev[0].A.rows != n || amg->lev[0].A.rp != A->m.rp)
     return gcge_record_error(GCGE_CUDA_ERR_ARG,
                              "AMGPCG: bad arguments (ctx = a GCGE_CUDA_AMG built on this A, "
-                             "1 <= k <= 32)");
+                             "1 <= k <= 256)");
+  if (k > 32) {
+    // wider blocks in groups of 32 columns (the row-interleaved blocks' widest)
+    int steps = 0;
+    for (int c0 = 0; c0 < k; c0 += 32) {
+      const int rc = GCGE_CUDA_AMGPCG(ctx, A, rhs + c0, x + c0, std::min(32, k - c0), n, stream);
+      if (rc != GCGE_CUDA_OK) return rc;
+      steps = std::max(steps, amg->last_steps);
+    }
+    amg->last_steps = steps;
+    return GCGE_CUDA_OK;
+  }
   std::lock_guard<std::mutex> lk(g_amg_mu);
   cudaStream_t st = (cudaStream_t)stream;
   const int kw = gcge::bcg_rows_width(k);

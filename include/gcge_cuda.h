@@ -220,7 +220,9 @@ int GCGE_CUDA_AMG_Apply(GCGE_CUDA_AMG* amg, double* const* b, double* const* x, 
  * preconditioned by one V-cycle, stopping at ||r|| < pcg_rate ||r_0|| or after
  * pcg_max_it steps; ctx is a GCGE_CUDA_AMG built on this A.  The residual of
  * the start x is formed in FP64 (skipped when x is zero), the FP32 correction
- * is added to x; rhs is overwritten.  k <= 32. */
+ * is added to x; rhs is overwritten.  k <= 256, run 32 columns at a time.  A
+ * hierarchy keeps its work blocks inside: it serves one call at a time (calls
+ * on different streams must not overlap on the GPU). */
 int GCGE_CUDA_AMGPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs, double* const* x,
                      int k, int n, void* stream);
 /* AMG-PCG steps of the last GCGE_CUDA_AMGPCG call on this hierarchy. */

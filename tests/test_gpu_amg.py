@@ -305,3 +305,19 @@ def test_aggregates_match_the_oracle_exactly(cuda_lib, make, theta):
         Al = amg.level_csr(l + 1, "A")
     amg.close()
     dA.close()
+
+
+def test_amg_pcg_wider_than_32_columns(cuda_lib):
+    """Blocks over 32 columns (a W step with a block size above 32) run 32
+    columns at a time; every column reaches the residual target."""
+    A, _ = laplace3d_mass(16, seed=4)
+    dA = DeviceMatrix(A)
+    amg = AMG(dA, pcg_max_it=60, pcg_rate=1e-4)
+    lib = L.load()
+    b = np.random.default_rng(5).standard_normal((40, A.n))
+    x = _pcg(lib, dA, amg, b, 60, 1e-4)
+    As = A.to_scipy()
+    res = [np.linalg.norm(b[j] - As @ x[j]) / np.linalg.norm(b[j]) for j in range(40)]
+    assert max(res) < 1e-3, max(res)
+    amg.close()
+    dA.close()
