@@ -1,7 +1,8 @@
 """C callers of the library, compiled with gcc against include/*.h and linked
 with -lgcge_cuda, run on the GPU: the device-resident solver through the C
-API (tests/c/solve_c_api.c) and the GCGE_OPS table driven through its
-function pointers (tests/c/ops_table_gpu.c)."""
+API (tests/c/solve_c_api.c), the same with the W step handed to AMG-PCG on a
+device-built AMG hierarchy (tests/c/amg_c_api.c), and the GCGE_OPS table
+driven through its function pointers (tests/c/ops_table_gpu.c)."""
 import os
 import subprocess
 
@@ -40,3 +41,11 @@ def test_c_program_drives_the_gcge_ops_table(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ops table: OK" in r.stdout
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c_program_solves_with_the_amg_preconditioner(tmp_path, precision):
+    exe = _exe("amg_c_api.c", tmp_path / "amg_c_api")
+    r = subprocess.run([exe, "48", "10", precision], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "amg c api: OK" in r.stdout
