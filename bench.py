@@ -44,7 +44,7 @@ nnz = 109,215,352), nev = 100, at --c3tol (default 1e-11: with a mass matrix
 of size h^3 the residual bound 1e-10 leaves the eigenvalues free by more than
 1e-10 relative), and reports both times, the per-pair difference of the mixed
 result from the FP64 one and of each from the oracle port's solve
-(tests/golden/cfg3_port_summary.json) (not the default line).
+(tests/golden/cfg3_port_summary.json), as a JSON line of its own.
 
 --config 4 runs the differentiation configuration: 2D anisotropic diffusion
 (5-point, per-cell kappa ~ U(0.5, 2), y-edges weighted 10) on a 512 x 512
