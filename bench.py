@@ -591,8 +591,9 @@ def run_config3(args):
     return 0
 
 
-def _config4_grad(torch, M, m, nev, seed, ev_tol):
-    """Forward + backward of the config-4 loss; returns the problem, tensors and times."""
+def _config4_grad(torch, M, m, nev, seed, ev_tol, adjoint_amg=None):
+    """Forward + backward of the config-4 loss; returns the problem, tensors and times.
+    adjoint_amg: the eigenvector adjoint's CG preconditioner (None: diag(A))."""
     from gcge_old_gb300.autograd import eigpairs_csr
     A, B, Smap, kappa = M.aniso2d(m, seed=seed)
     rng = np.random.default_rng(seed + 1)
@@ -608,7 +609,7 @@ def _config4_grad(torch, M, m, nev, seed, ev_tol):
     t0 = time.time()
     a = torch.sparse.mm(St, kap[:, None])[:, 0]
     a.retain_grad()
-    lam, X = eigpairs_csr(a, A, nev, x0, b_val=b, B_pattern=B, **params)
+    lam, X = eigpairs_csr(a, A, nev, x0, b_val=b, B_pattern=B, adjoint_amg=adjoint_amg, **params)
     t1 = time.time()
     wt, mt = torch.from_numpy(w), torch.from_numpy(mask)
     loss_ev = (wt * lam).sum()
@@ -643,6 +644,15 @@ def run_config4(args):
     from gcge_old_gb300 import matrices as M
     nev = 32
     r = _config4_grad(torch, M, 512, nev, 0, 1e-12)
+    # the same forward + backward with the adjoint's CG preconditioned by an AMG
+    # V-cycle of A (hierarchy set-up inside the backward time)
+    ra = _config4_grad(torch, M, 512, nev, 0, 1e-12, adjoint_amg=True)
+    amg_arm = {"cg_steps": ra["adj"]["steps"], "backward_s": ra["t_bwd"],
+               "forward_s": ra["t_fwd"],
+               "gradA_rel_diff_vs_jacobi": float(np.abs(ra["ga"] - r["ga"]).max()
+                                                 / np.abs(r["ga"]).max()),
+               "gradB_rel_diff_vs_jacobi": float(np.abs(ra["gb"] - r["gb"]).max()
+                                                 / np.abs(r["gb"]).max())}
     kappa, Bv, Av, Smap = r["kappa"], r["B"].val, r["A"].val, r["S"]
     rng = np.random.default_rng(3)
     # the same solve from another initial block: the spread of the two losses is
@@ -709,7 +719,8 @@ def run_config4(args):
                       "loss": "sum w_k lambda_k + ||x_1 * mask||^2"},
            "forward_s": r["t_fwd"], "backward_s": r["t_bwd"],
            "eigenvector_adjoint": {"columns": r["adj"]["columns"], "cg_steps": r["adj"]["steps"],
-                                   "tol": 1e-10},
+                                   "tol": 1e-10, "preconditioner": "jacobi"},
+           "eigenvector_adjoint_amg": amg_arm,
            "fd_checks": checks,
            "fd_rel_best_eigenvalue_loss": {d: min(c["rel"] for c in checks["eigenvalue_loss"]
                                                   if c["direction"] == d)

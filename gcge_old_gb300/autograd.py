@@ -33,7 +33,7 @@ import torch
 
 from . import lib as L
 from .matrices import CSRMatrix
-from .solver import DeviceMatrix, GCGESolver
+from .solver import AMG, DeviceMatrix, GCGESolver
 
 
 def _with_values(pattern: CSRMatrix, values) -> CSRMatrix:
@@ -97,7 +97,7 @@ def eigvals_csr(a_val: torch.Tensor, A_pattern: CSRMatrix, nev: int, x0: np.ndar
 
 
 # step count and column count of the last eigenvector-adjoint solve
-last_adjoint = {"steps": 0, "columns": 0}
+last_adjoint = {"steps": 0, "columns": 0, "preconditioner": "jacobi"}
 
 
 def _signed(vec: np.ndarray) -> np.ndarray:
@@ -151,12 +151,20 @@ class _EigpairsCSR(torch.autograd.Function):
                 gp = (C.c_void_p * nev)(*[C.c_void_p(G[j].data_ptr()) if want[j] else None
                                           for j in range(nev)])
                 it = C.c_int(0)
-                L.check(lib.GCGE_CUDA_EigvecAdjointSolve(
-                    dA.handle, dB.handle if dB else None, xp, _dptr(ev), nev, gp, _cols(mu),
-                    _dptr(gx), int(ctx.adj["max_it"]), float(ctx.adj["tol"]), C.byref(it)),
-                    "EigvecAdjointSolve")
+                amg = None
+                if ctx.adj["amg"] is not None:
+                    amg = AMG(dA, **ctx.adj["amg"])
+                try:
+                    L.check(lib.GCGE_CUDA_EigvecAdjointSolveAMG(
+                        dA.handle, dB.handle if dB else None, xp, _dptr(ev), nev, gp, _cols(mu),
+                        _dptr(gx), int(ctx.adj["max_it"]), float(ctx.adj["tol"]), C.byref(it),
+                        amg.handle if amg else None), "EigvecAdjointSolve")
+                finally:
+                    if amg:
+                        amg.close()
                 last_adjoint["steps"] = it.value
                 last_adjoint["columns"] = int(want.sum())
+                last_adjoint["preconditioner"] = "amg" if amg else "jacobi"
             mp = _cols(mu) if mu is not None else None
             ga = gb = None
             if ctx.needs_input_grad[0]:
@@ -186,12 +194,17 @@ def _dptr(a: np.ndarray):
 
 def eigpairs_csr(a_val: torch.Tensor, A_pattern: CSRMatrix, nev: int, x0: np.ndarray,
                  b_val: torch.Tensor | None = None, B_pattern: CSRMatrix | None = None,
-                 adjoint_tol: float = 1e-10, adjoint_max_it: int = 100000, **params):
+                 adjoint_tol: float = 1e-10, adjoint_max_it: int = 100000,
+                 adjoint_amg: dict | bool | None = None, **params):
     """(lambda, X): the nev smallest eigenpairs of A x = lambda B x, X of shape
     (nev, n) with B-normalised rows, differentiable in a_val / b_val for losses
     of both.  adjoint_tol / adjoint_max_it: stopping rule of the projected CG of
-    the eigenvector adjoint (relative residual per column)."""
+    the eigenvector adjoint (relative residual per column).  adjoint_amg: True
+    or a dict of GCGE_CUDA_AMG_PARAM fields preconditions that CG by a V-cycle
+    of an AMG hierarchy of A built in the backward pass (GCGE_CUDA_AMG_Create);
+    None / False: diag(A)."""
     if (b_val is None) != (B_pattern is None):
         raise ValueError("b_val and B_pattern go together")
-    adj = {"tol": adjoint_tol, "max_it": adjoint_max_it}
+    amg = None if adjoint_amg in (None, False) else ({} if adjoint_amg is True else dict(adjoint_amg))
+    adj = {"tol": adjoint_tol, "max_it": adjoint_max_it, "amg": amg}
     return _EigpairsCSR.apply(a_val, b_val, A_pattern, B_pattern, nev, x0, params, adj)

@@ -15,6 +15,13 @@
 // solved by conjugate gradients on range(Q), preconditioned by Q D^-1 Q^T with
 // D = diag(A), all requested columns at once (one SpMM per step), with the step
 // scalars kept on the device and the residuals read back every few steps.
+// GCGE_CUDA_EigvecAdjointSolveAMG preconditions by Q M^-1 Q^T instead, M^-1 one
+// V-cycle of an AMG hierarchy of A: for v in range(Q), v^T (A - lambda_k B) v
+// lies between (1 - lambda_k / lambda_{nev+1}) v^T A v and v^T A v, so a
+// preconditioner of A serves the shifted system.  The V-cycle runs in FP32, which makes it a
+// slightly nonlinear operator; those solves take the flexible direction update
+// beta = -z_new^T U / p^T U (U the projected operator times p), which keeps
+// successive directions conjugate whatever the preconditioner.
 #include <math.h>
 #include <stdio.h>
 
@@ -174,14 +181,15 @@ __global__ void k_step(ColList<double> MU, ColList<double> R, ColList<double> P,
   }
 }
 
-// beta = rz_new / rz_old; P = Z + beta P  (active columns)
-__global__ void k_direction(ColList<double> Z, ColList<double> P, const double* __restrict__ rz_new,
-                            const double* __restrict__ rz_old, const int* __restrict__ active,
-                            int n) {
+// beta = sign num / den (rz_new / rz_old, or -z_new^T U / p^T U for the
+// flexible update); P = Z + beta P  (active columns)
+__global__ void k_direction(ColList<double> Z, ColList<double> P, const double* __restrict__ num,
+                            const double* __restrict__ den, double sign,
+                            const int* __restrict__ active, int n) {
   const int c = blockIdx.y;
   if (!active[c]) return;
   __shared__ double b_s;  // one division per block
-  if (threadIdx.x == 0) b_s = (rz_old[c] != 0.0) ? rz_new[c] / rz_old[c] : 0.0;
+  if (threadIdx.x == 0) b_s = (den[c] != 0.0) ? sign * num[c] / den[c] : 0.0;
   __syncthreads();
   const double b = b_s;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
@@ -221,14 +229,22 @@ int finish(cudaStream_t st) {
 
 }  // namespace
 
-extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT* B,
-                                            double* const* X, const double* eval, int nev,
-                                            double* const* G, double* const* MU, double* gx,
-                                            int max_it, double tol, int* iters) {
+extern "C" int GCGE_CUDA_EigvecAdjointSolveAMG(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT* B,
+                                               double* const* X, const double* eval, int nev,
+                                               double* const* G, double* const* MU, double* gx,
+                                               int max_it, double tol, int* iters,
+                                               GCGE_CUDA_AMG* amg) {
   if (!A || !X || !eval || !G || !MU || nev <= 0 || nev > GCGE_MAXCOLS || max_it < 0)
     return gcge_record_error(GCGE_CUDA_ERR_ARG, "EigvecAdjointSolve: bad argument");
   const int n = A->m.n;
   if (B && B->m.n != n) return gcge_record_error(GCGE_CUDA_ERR_ARG, "EigvecAdjointSolve: B size");
+  if (amg) {
+    int n0 = -1;
+    if (GCGE_CUDA_AMG_GetLevelInfo(amg, 0, &n0, nullptr, nullptr, nullptr) != GCGE_CUDA_OK ||
+        n0 != n)
+      return gcge_record_error(GCGE_CUDA_ERR_ARG,
+                               "EigvecAdjointSolveAMG: the hierarchy's finest level is not n rows");
+  }
   std::vector<int> ks;  // requested columns
   for (int k = 0; k < nev; k++)
     if (G[k]) {
@@ -307,8 +323,7 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
   if (cudaMemcpyAsync(hg.data(), Gm, sizeof(double) * nev * m, cudaMemcpyDeviceToHost, st) !=
       cudaSuccess)
     return finish(st);
-  int rc = finish(st);
-  if (rc) return rc;
+  if (int r = finish(st)) return r;
   for (int a = 0; a < m; a++) {
     const int k = ks[a];
     if (gx) gx[k] = hg[k + (size_t)a * nev];
@@ -323,13 +338,22 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
   if (shm > 48 * 1024)
     cudaFuncSetAttribute(k_sub_lincomb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   k_sub_lincomb<<<nb_rows, 256, shm, st>>>(R, BX, Gm, nev, nev, m, n);
-  // Z = Q D^-1 R = D^-1 R - X (BX^T D^-1 R); P = Z
-  auto precond = [&]() {
-    k_precond<<<gcol, 256, 0, st>>>(R, Z, dinv, n);
+  // Z = Q M^-1 R = M^-1 R - X (BX^T M^-1 R), M = D or one V-cycle; P = Z
+  auto precond = [&]() -> int {
+    if (amg) {
+      for (int c0 = 0; c0 < m; c0 += 32) {
+        const int r = GCGE_CUDA_AMG_Apply(amg, &R.p[c0], &Z.p[c0], std::min(32, m - c0), st);
+        if (r != GCGE_CUDA_OK) return r;
+      }
+    } else {
+      k_precond<<<gcol, 256, 0, st>>>(R, Z, dinv, n);
+    }
     pair_gram(BX, nev, Z, m, n, gp, Gm, st);
     k_sub_lincomb<<<nb_rows, 256, shm, st>>>(Z, Xl, Gm, nev, nev, m, n);
+    return GCGE_CUDA_OK;
   };
-  precond();
+  int rc = precond();
+  if (rc) return rc;
   k_copy_cols<<<gcol, 256, 0, st>>>(Z, P, n);
   dots(R, Z, m, n, partial, rz, st);
   dots(R, R, m, n, partial, rr, st);
@@ -358,9 +382,14 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
     k_sub_lincomb<<<nb_rows, 256, shm, st>>>(U, BX, Gm, nev, nev, m, n);
     dots(P, U, m, n, partial, pu, st);
     k_step<<<gcol, 256, 0, st>>>(Ml, R, P, U, rz, pu, active, n);
-    precond();
+    if ((rc = precond())) return rc;
     dots(R, Z, m, n, partial, rz2, st);
-    k_direction<<<gcol, 256, 0, st>>>(Z, P, rz2, rz, active, n);
+    if (amg) {
+      dots(Z, U, m, n, partial, rr, st);
+      k_direction<<<gcol, 256, 0, st>>>(Z, P, rr, pu, -1.0, active, n);
+    } else {
+      k_direction<<<gcol, 256, 0, st>>>(Z, P, rz2, rz, 1.0, active, n);
+    }
     std::swap(rz, rz2);
     it++;
     if (it % kCheckEvery == 0 || it == max_it) {
@@ -384,6 +413,14 @@ extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_C
     return gcge_record_error(GCGE_CUDA_ERR_NUMERIC, msg);
   }
   return GCGE_CUDA_OK;
+}
+
+extern "C" int GCGE_CUDA_EigvecAdjointSolve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT* B,
+                                            double* const* X, const double* eval, int nev,
+                                            double* const* G, double* const* MU, double* gx,
+                                            int max_it, double tol, int* iters) {
+  return GCGE_CUDA_EigvecAdjointSolveAMG(A, B, X, eval, nev, G, MU, gx, max_it, tol, iters,
+                                         nullptr);
 }
 
 extern "C" int GCGE_CUDA_EigGradCSR2(const GCGE_CUDA_MAT* M, double* const* X, double* const* MU,

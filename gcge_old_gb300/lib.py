@@ -141,6 +141,9 @@ SIGNATURES = {
     "GCGE_CUDA_EigvecAdjointSolve": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_double_p, C.c_int,
                                               c_pp, c_pp, c_double_p, C.c_int, C.c_double,
                                               c_int_p]),
+    "GCGE_CUDA_EigvecAdjointSolveAMG": (C.c_int, [C.c_void_p, C.c_void_p, c_pp, c_double_p,
+                                                 C.c_int, c_pp, c_pp, c_double_p, C.c_int,
+                                                 C.c_double, c_int_p, C.c_void_p]),
     "GCGE_CUDA_EigGradCSR2": (C.c_int, [C.c_void_p, c_pp, c_pp, c_double_p, c_double_p, C.c_int,
                                         C.c_void_p]),
     "GCGE_CUDA_EigGradCSR": (C.c_int, [C.c_void_p, c_pp, C.c_void_p, C.c_int, C.c_void_p]),

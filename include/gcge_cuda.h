@@ -227,6 +227,14 @@ int GCGE_CUDA_AMGPCG(void* ctx, const GCGE_CUDA_MAT* A, double* const* rhs, doub
                      int k, int n, void* stream);
 /* AMG-PCG steps of the last GCGE_CUDA_AMGPCG call on this hierarchy. */
 int GCGE_CUDA_AMG_GetLastSteps(const GCGE_CUDA_AMG* amg, int* steps);
+/* GCGE_CUDA_EigvecAdjointSolve with the projected CG preconditioned by one
+ * V-cycle of amg (a hierarchy of A, n rows on its finest level) in place of
+ * diag(A), with the flexible direction update -z^T U / p^T U that the FP32
+ * V-cycle calls for; amg NULL: the Jacobi-preconditioned solve. */
+int GCGE_CUDA_EigvecAdjointSolveAMG(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT* B,
+                                    double* const* X, const double* eval, int nev,
+                                    double* const* G, double* const* MU, double* gx, int max_it,
+                                    double tol, int* iters, GCGE_CUDA_AMG* amg);
 
 /* ---------------------------------------------------------------- multilevel eigensolver
  * The multilevel correction method of the reference's PASE add-on

@@ -158,3 +158,52 @@ def test_adjoint_rejects_bad_arguments(cuda_lib, prob):
     ev = np.array([1.0, 1.0])
     assert lib.GCGE_CUDA_EigvecAdjointSolve(None, None, None, ev.ctypes.data_as(L.c_double_p), 2,
                                             None, None, None, 10, 1e-8, None) == 1
+    assert lib.GCGE_CUDA_EigvecAdjointSolveAMG(None, None, None, ev.ctypes.data_as(L.c_double_p),
+                                               2, None, None, None, 10, 1e-8, None, None) == 1
+
+
+def test_eigenvector_adjoint_amg_matches_jacobi(cuda_lib):
+    """The projected CG preconditioned by an AMG V-cycle of A (adjoint_amg=True)
+    gives the gradients of the Jacobi-preconditioned solve in fewer steps."""
+    import torch
+    from gcge_old_gb300 import autograd as AG
+    A, B, _, _ = aniso2d(m=96, seed=5)  # n = 9216
+    nev = 8
+    x0 = initial_block(A.n, nev, seed=2)
+    rng = np.random.default_rng(4)
+    mask = torch.from_numpy((rng.uniform(size=A.n) < 0.3).astype(float))
+    q = torch.from_numpy(rng.standard_normal(A.n))
+    out = {}
+    for amg in (None, True):
+        a = torch.tensor(A.val, requires_grad=True)
+        b = torch.tensor(B.val, requires_grad=True)
+        lam, X = AG.eigpairs_csr(a, A, nev, x0, b_val=b, B_pattern=B, adjoint_amg=amg, **PARAMS)
+        (((X[0] * mask) ** 2).sum() + (X[2] @ q) ** 2).backward()
+        out[amg] = (a.grad.numpy(), b.grad.numpy(), dict(AG.last_adjoint))
+    (ga_j, gb_j, st_j), (ga_a, gb_a, st_a) = out[None], out[True]
+    assert st_j["preconditioner"] == "jacobi" and st_a["preconditioner"] == "amg"
+    assert st_a["columns"] == st_j["columns"] == 2
+    np.testing.assert_allclose(ga_a, ga_j, rtol=0, atol=1e-7 * np.abs(ga_j).max())
+    np.testing.assert_allclose(gb_a, gb_j, rtol=0, atol=1e-7 * np.abs(gb_j).max())
+    assert st_a["steps"] <= st_j["steps"] / 2, (st_a, st_j)
+
+
+def test_eigenvector_adjoint_amg_rejects_another_size(cuda_lib, prob):
+    """A hierarchy whose finest level is not A's size is an argument error."""
+    import ctypes as C
+    from gcge_old_gb300 import lib as L
+    from gcge_old_gb300 import solver as S
+    lib = L.load()
+    A2, _, _, _ = aniso2d(m=20, seed=1)
+    dA2 = S.DeviceMatrix(A2)
+    amg = S.AMG(dA2)
+    dA = S.DeviceMatrix(prob["A"])
+    ev = np.arange(1.0, NEV + 1.0)
+    xs = (C.c_void_p * NEV)()
+    assert lib.GCGE_CUDA_EigvecAdjointSolveAMG(dA.handle, None, xs,
+                                               ev.ctypes.data_as(L.c_double_p), NEV, xs, xs,
+                                               None, 10, 1e-8, None, amg.handle) == 1
+    assert "finest level" in lib.GCGE_CUDA_GetLastErrorMessage().decode()
+    amg.close()
+    dA.close()
+    dA2.close()
