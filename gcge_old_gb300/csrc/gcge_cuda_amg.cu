@@ -1526,12 +1526,23 @@ int coarsest_inverse(GCGE_CUDA_AMG_* amg, cudaStream_t st) {
   const Level& L = amg->lev[amg->nlev - 1];
   const int n = L.A.rows;
   if (n > kCoarseMax) return GCGE_CUDA_OK;  // smoothed instead
-  double *g = nullptr, *piv = nullptr, *col = nullptr;
-  int* bad = nullptr;
-  AMG_CHK(dalloc(&g, (size_t)n * 2 * n));
-  AMG_CHK(dalloc(&piv, (size_t)2 * n));
-  AMG_CHK(dalloc(&col, (size_t)n));
-  AMG_CHK(dalloc(&bad, 1));
+  // the elimination's scratch is freed however this function returns
+  struct Scratch {
+    double *g = nullptr, *piv = nullptr, *col = nullptr;
+    int* bad = nullptr;
+    ~Scratch() {
+      cudaFree(g);
+      cudaFree(piv);
+      cudaFree(col);
+      cudaFree(bad);
+    }
+  } w;
+  AMG_CHK(dalloc(&w.g, (size_t)n * 2 * n));
+  AMG_CHK(dalloc(&w.piv, (size_t)2 * n));
+  AMG_CHK(dalloc(&w.col, (size_t)n));
+  AMG_CHK(dalloc(&w.bad, 1));
+  double *g = w.g, *piv = w.piv, *col = w.col;
+  int* bad = w.bad;
   AMG_CU(cudaMemsetAsync(bad, 0, sizeof(int), st));
   k_dense_aug<<<n, 256, 0, st>>>(n, L.A.rp, L.A.ci, L.A.v, g);
   for (int k = 0; k < n; k++) {
@@ -1547,10 +1558,6 @@ int coarsest_inverse(GCGE_CUDA_AMG_* amg, cudaStream_t st) {
     AMG_CU(cudaGetLastError());
     AMG_CU(cudaStreamSynchronize(st));
   }
-  cudaFree(g);
-  cudaFree(piv);
-  cudaFree(col);
-  cudaFree(bad);
   return GCGE_CUDA_OK;  // a non-positive pivot leaves the coarsest level smoothed
 }
 
@@ -2095,11 +2102,18 @@ int galerkin(const View& R, const View& M, const View& P, View* C, cudaStream_t 
 int identity(int n, View* I, cudaStream_t st) {
   View v;
   v.rows = v.cols = v.nnz = n;
-  AMG_CHK(dalloc(&v.rp, (size_t)n + 1));
-  AMG_CHK(dalloc(&v.ci, (size_t)n));
-  AMG_CHK(dalloc(&v.v, (size_t)n));
+  int rc = dalloc(&v.rp, (size_t)n + 1);
+  if (rc == GCGE_CUDA_OK) rc = dalloc(&v.ci, (size_t)n);
+  if (rc == GCGE_CUDA_OK) rc = dalloc(&v.v, (size_t)n);
+  if (rc != GCGE_CUDA_OK) {
+    free_view(v);
+    return rc;
+  }
   k_identity<<<(n + 256) / 256, 256, 0, st>>>(n, v.rp, v.ci, v.v);
-  AMG_CU(cudaGetLastError());
+  if (cudaGetLastError() != cudaSuccess) {
+    free_view(v);
+    return gcge_record_error(GCGE_CUDA_ERR_CUDA, "AMG: identity kernel failed");
+  }
   *I = v;
   return GCGE_CUDA_OK;
 }

@@ -370,9 +370,20 @@ extern "C" int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT*
 
   // ---------------------------------------------------------------- auxiliary matrices + solver
   {
-    int* rp = nullptr;
-    int* ci = nullptr;
-    double* v = nullptr;
+    // the staging arrays are freed however this block is left
+    struct Staging {
+      int* rp = nullptr;
+      int* ci = nullptr;
+      double* v = nullptr;
+      void release() {
+        cudaFree(rp);
+        cudaFree(ci);
+        cudaFree(v);
+        rp = ci = nullptr;
+        v = nullptr;
+      }
+      ~Staging() { release(); }
+    } sg;
     int nnzH = 0;
     PASE_CU(cudaMemcpy(&nnzH, AHv.rp + nH, sizeof(int), cudaMemcpyDeviceToHost));
     int nnzBH = 0;
@@ -382,20 +393,21 @@ extern "C" int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT*
       const long long nnz = (long long)(which == 0 ? nnzH : nnzBH) + 2ll * nH * k + (long long)k * k;
       if (nnz > 2000000000ll)
         return gcge_record_error(GCGE_CUDA_ERR_ARG, "PASE_Solve: auxiliary matrix too large");
-      PASE_CHK(dalloc(&rp, (size_t)naux + 1));
-      PASE_CHK(dalloc(&ci, (size_t)nnz));
-      PASE_CHK(dalloc(&v, (size_t)nnz));
-      k_aux_rowptr<<<(naux + 256) / 256, 256, 0, s.st>>>(nH, k, M.rp, rp);
+      PASE_CHK(dalloc(&sg.rp, (size_t)naux + 1));
+      PASE_CHK(dalloc(&sg.ci, (size_t)nnz));
+      PASE_CHK(dalloc(&sg.v, (size_t)nnz));
+      k_aux_rowptr<<<(naux + 256) / 256, 256, 0, s.st>>>(nH, k, M.rp, sg.rp);
       PASE_CU(cudaMemsetAsync(s.RH, 0, sizeof(double) * nH * k, s.st));
       PASE_CU(cudaMemsetAsync(s.hh, 0, sizeof(double) * k * k, s.st));
-      k_aux_fill_sparse<<<(nH + 255) / 256, 256, 0, s.st>>>(nH, k, M.rp, M.ci, M.v, s.RH, rp, ci, v);
-      k_aux_fill_dense<<<dim3(grid_of(naux), k), 256, 0, s.st>>>(nH, k, s.RH, s.hh, rp, ci, v);
+      k_aux_fill_sparse<<<(nH + 255) / 256, 256, 0, s.st>>>(nH, k, M.rp, M.ci, M.v, s.RH, sg.rp,
+                                                            sg.ci, sg.v);
+      k_aux_fill_dense<<<dim3(grid_of(naux), k), 256, 0, s.st>>>(nH, k, s.RH, s.hh, sg.rp, sg.ci,
+                                                                 sg.v);
       PASE_CU(cudaGetLastError());
       PASE_CU(cudaStreamSynchronize(s.st));
-      const int rc = GCGE_CUDA_MatCreate(which == 0 ? &s.auxA : &s.auxB, naux, rp, ci, v, 1);
-      cudaFree(rp);
-      cudaFree(ci);
-      cudaFree(v);
+      const int rc =
+          GCGE_CUDA_MatCreate(which == 0 ? &s.auxA : &s.auxB, naux, sg.rp, sg.ci, sg.v, 1);
+      sg.release();
       if (rc) return rc;
     }
     PASE_CHK(GCGE_CUDA_SOLVER_Create(&s.aux));
