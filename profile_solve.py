@@ -140,6 +140,7 @@ def main():
     ap.add_argument("--diff27", type=int, default=0, help="27-point diffusion grid size")
     ap.add_argument("--amg", action="store_true", help="W step by AMG-PCG")
     ap.add_argument("--pase", action="store_true", help="the multilevel eigensolver")
+    ap.add_argument("--tol", type=float, default=1e-10, help="stopping residual of --pase")
     ap.add_argument("--gram", type=int, default=0,
                     help="only W-orthogonalisation Gram passes (80 x 10) at grid^3 rows")
     a = ap.parse_args()
@@ -163,7 +164,7 @@ def main():
     if a.pase:
         from gcge_old_gb300 import lib as L
         try:
-            ev, vec, st = S.pase_solve(A, B, a.nev, tol=1e-10, max_cycles=a.iters)
+            ev, vec, st = S.pase_solve(A, B, a.nev, tol=a.tol, max_cycles=a.iters)
             print(st)
         except L.GcgeCudaError as e:  # the cycle cap ends the run before convergence
             print("pase stopped at the cycle cap:", e)
