@@ -148,6 +148,38 @@ __global__ void k_scale_cols(ColList<double> X, DblList s, int k, int n) {
 
 int grid_of(long long n) { return (int)std::min<long long>((n + 255) / 256, 4 * 152); }
 
+// Y_c = R X_c for the restriction R (rows of a few hundred entries: an
+// aggregate's smoothed support): one warp per (row, group of RW columns), the
+// lanes striding over the row's entries, then a shuffle tree per column (a
+// fixed order).  Thread-per-row gathers serialise a whole row per thread.
+constexpr int RW = 8;
+__global__ void k_restrict_warp(int nr, const int* __restrict__ rp, const int* __restrict__ ci,
+                                const double* __restrict__ v, ColList<double> X, ColList<double> Y,
+                                int k) {
+  const int row = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= nr) return;  // whole warps leave together
+  const int c0 = blockIdx.y * RW;
+  const int nc = min(RW, k - c0);
+  double s[RW];
+#pragma unroll
+  for (int c = 0; c < RW; c++) s[c] = 0.0;
+  const int e1 = rp[row + 1];
+  for (int e = rp[row] + lane; e < e1; e += 32) {
+    const int j = ci[e];
+    const double a = v[e];
+#pragma unroll
+    for (int c = 0; c < RW; c++)
+      if (c < nc) s[c] = fma(a, X.p[c0 + c][j], s[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < RW; c++) {
+    double t = s[c];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0 && c < nc) Y.p[c0 + c][row] = t;
+  }
+}
+
 double now() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -171,6 +203,8 @@ struct Pase {
   double* RH = nullptr;     // nH x k restricted block (A, then B)
   double* RH2 = nullptr;
   double* hh = nullptr;     // k x k Gram
+  uint8_t* upl = nullptr;   // digit planes of U (k columns), cut once per cycle
+  uint8_t* mpl = nullptr;   // digit planes of A U, then of B U
   double* Yaux = nullptr;   // n_aux x k
   double* partial = nullptr;
   size_t partial_len = 0;
@@ -189,6 +223,8 @@ struct Pase {
     gcge::amg::free_view(Bid);
     for (double* p : {U, Z, AU, BU, rhs, RH, RH2, hh, Yaux, partial, dlam, rn}) cudaFree(p);
     cudaFree(lcs);
+    cudaFree(upl);
+    cudaFree(mpl);
     for (double* p : lvl) cudaFree(p);
     if (st) cudaStreamDestroy(st);
   }
@@ -232,8 +268,10 @@ int restrict_chain(Pase& s, const GCGE_CUDA_AMG* amg, const double* X0, double* 
   for (int l = 0; l < s.H; l++) {
     const View R = gcge::amg::restrict_to(amg, l);
     double* out = l == s.H - 1 ? dst : s.lvl[l];
-    gcge::spmm_f64(csr_of(R), cols(const_cast<double*>(src), lds, s.k), cols(out, R.rows, s.k), s.k,
-                   s.st);
+    const dim3 g((unsigned)(((size_t)R.rows * 32 + 255) / 256), (unsigned)((s.k + RW - 1) / RW));
+    k_restrict_warp<<<g, 256, 0, s.st>>>(R.rows, R.rp, R.ci, R.v,
+                                         cols(const_cast<double*>(src), lds, s.k),
+                                         cols(out, R.rows, s.k), s.k);
     src = out;
     lds = R.rows;
   }
@@ -345,6 +383,8 @@ extern "C" int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT*
   PASE_CHK(dalloc(&s.dlam, (size_t)k));
   PASE_CHK(dalloc(&s.rn, (size_t)2 * k));
   PASE_CU(cudaMalloc(&s.lcs, gcge::lincomb_oz_scratch_bytes(k, k)));
+  PASE_CU(cudaMalloc(&s.upl, gcge::planes_bytes(n, k)));
+  PASE_CU(cudaMalloc(&s.mpl, gcge::planes_bytes(n, k)));
   s.lam.assign(k, 0.0);
 
   // ---------------------------------------------------------------- initial pairs on level H
@@ -457,12 +497,14 @@ extern "C" int GCGE_CUDA_PASE_Solve(const GCGE_CUDA_MAT* A, const GCGE_CUDA_MAT*
     const ColList<double> Uc = cols(s.U, n, k), AUc = cols(s.AU, n, k), BUc = cols(s.BU, n, k);
     gcge::spmm_f64(A->m, Uc, AUc, k, s.st);
     gcge::apply_b_f64(Bm, Uc, BUc, k, n, s.st);
+    // U^T (M U) from digit planes: U's cut once for both products
+    gcge::cut_planes(Uc, k, n, s.upl, k, 0, s.st);
     for (int which = 0; which < 2 && rc == GCGE_CUDA_OK; which++) {
       const double* MU = which == 0 ? s.AU : s.BU;
       rc = restrict_chain(s, amg, MU, s.RH);
       if (rc) break;
-      gcge::gram_oz(Uc, k, cols(const_cast<double*>(MU), n, k), k, n, s.hh, k, false, s.partial,
-                    s.st);
+      gcge::cut_planes(cols(const_cast<double*>(MU), n, k), k, n, s.mpl, k, 0, s.st);
+      gcge::gram_oz_planes(s.upl, k, 0, k, s.mpl, k, 0, k, n, s.hh, k, s.partial, s.st);
       GCGE_CUDA_MAT* aux = which == 0 ? s.auxA : s.auxB;
       const View& M = which == 0 ? AHv : BHv;
       GcgeDevCsr& am = aux->m;
